@@ -1,0 +1,273 @@
+/*
+ * nrgpu.h -- C ABI of the GB300 (sm_103a) method-of-lines finite-difference
+ * evolution library (libnrgpu.so).
+ *
+ * What it replaces.  NRPy+/SENR drivers are C programs whose time loop
+ * #includes the generated MoLtimestepping/RK_MoL.h; every RK substep there
+ * calls a generated rhs_eval (plus Ricci_eval for BSSN), a flat
+ * LOOP_ALL_GFS_GPS RK update, apply_bcs_curvilinear and
+ * enforce_detgammabar_constraint.  Each entry point below is the drop-in for
+ * one of those calls and keeps its argument meaning, its gridfunction layout
+ * (IDX4S: i0 fastest, gridfunctions outermost, alphabetical gridfunction
+ * order) and its point set (interior points for RHS kernels, all points for
+ * the update and the det(gammabar) rescale).  The reference cites are file
+ * paths within zachetienne/nrpytutorial.
+ *
+ * Conventions that differ from the generated C, and why:
+ *  - Gridfunction arrays are DEVICE pointers (cudaMalloc'ed or torch CUDA
+ *    tensors).  Work is queued on the library's current stream
+ *    (nrgpu_set_stream) and is asynchronous; no entry point on the time-step
+ *    path synchronises the host or allocates memory.
+ *  - Every entry point returns an int status (NRGPU_OK == 0) instead of
+ *    calling exit(1); nrgpu_last_error() gives the message.
+ *  - Each physical system has its own rhs_eval name, because one library
+ *    serves all of them (a SENR driver compiles only one rhs_eval).
+ *  - "_f32" variants take FP32 gridfunctions and evaluate the RHS in FP32;
+ *    rfm precompute tables, the RK4 state y_n and its running total stay FP64.
+ */
+#ifndef NRGPU_H
+#define NRGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define NRGPU_OK               0
+#define NRGPU_ERR_ARG          1  /* bad pointer, size, order or coordinate system */
+#define NRGPU_ERR_CUDA         2  /* a CUDA runtime call failed                    */
+#define NRGPU_ERR_UNSUPPORTED  3  /* combination not built into this library        */
+#define NRGPU_ERR_BCMAP        4  /* ghost-zone map failed its Cartesian/parity check */
+#define NRGPU_ERR_SIZE         5  /* grid or batch larger than a fixed limit        */
+
+/* ------------------------------------------------------ coordinate systems */
+/* reference_metric.py:100-176 (Spherical, SinhSpherical), :398-428 (Cartesian) */
+#define NRGPU_COORD_CARTESIAN      0
+#define NRGPU_COORD_SPHERICAL      1
+#define NRGPU_COORD_SINHSPHERICAL  2
+
+/* ------------------------------------------------------------- systems */
+#define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
+#define NRGPU_SYS_MAXWELL     1   /* AU0..2, EU0..2, psi  (System I)          */
+#define NRGPU_SYS_BSSN        2   /* 24 evolved gfs, alphabetical             */
+
+#define NRGPU_PREC_FP64   0       /* everything FP64                          */
+#define NRGPU_PREC_MIXED  1       /* FP32 stage buffers + FP32 RHS, FP64 y_n  */
+
+/*
+ * paramstruct: the runtime parameters the generated kernels read through
+ * set_Cparameters.h (NRPy_param_funcs.py:216-304 emits the reference's struct).
+ * Field names follow the reference's C parameter names.
+ */
+typedef struct paramstruct {
+  int    CoordSystem;                 /* NRGPU_COORD_*                          */
+  int    FD_order;                    /* 2, 4, 6 or 8 (FD_CENTDERIVS_ORDER)     */
+  int    NGHOSTS;                     /* ghost zones per side                   */
+  int    Nxx0, Nxx1, Nxx2;            /* interior points                        */
+  int    Nxx_plus_2NGHOSTS0, Nxx_plus_2NGHOSTS1, Nxx_plus_2NGHOSTS2;
+  double dxx0, dxx1, dxx2;
+  double invdx0, invdx1, invdx2;
+  double xxmin0, xxmin1, xxmin2;      /* uniform-coordinate domain              */
+  double xxmax0, xxmax1, xxmax2;
+  double AMPL, SINHW;                 /* SinhSpherical  (reference_metric.py:123) */
+  double RMAX;                        /* Spherical      (reference_metric.py:107) */
+  double xmin, xmax, ymin, ymax, zmin, zmax;   /* Cartesian (:400-401)          */
+  double eta;                         /* Gamma-driver damping (BSSN_gauge_RHSs.py:233) */
+  double wavespeed;                   /* ScalarWave/CommonParams.py:24          */
+  double time;
+} paramstruct;
+
+/*
+ * rfm_struct: FP64 reference-metric precompute tables (the rfm_precompute
+ * arrays of reference_metric.py:603-886, here as dense derived quantities per
+ * (i0,i1) column), plus an FP32 copy for the mixed-precision kernels.
+ */
+typedef struct rfm_struct {
+  int     CoordSystem;
+  int     N0, N1;            /* table extents = Nxx_plus_2NGHOSTS0, 1          */
+  int     nquant;            /* doubles per (i0,i1)                            */
+  double *table64;           /* device, [nquant][N1][N0]                       */
+  float  *table32;           /* device, same layout                            */
+} rfm_struct;
+
+/*
+ * bc_struct: the compacted ghost-zone map of set_bcstruct.h:32-124
+ * (BCs_data_structs.h:2-49), flattened into device arrays.  Per ghost layer
+ * `g` (innermost first) the outer points are grouped by face direction
+ * (i0 faces, then i1, then i2, as set_bcstruct.h orders them) and followed by
+ * the inner (parity) points.
+ */
+#define NRGPU_MAX_GHOSTS 8
+typedef struct bc_struct {
+  int  NGHOSTS;
+  int  num_ob_gz_pts[NRGPU_MAX_GHOSTS];        /* outer points in layer g   */
+  int  num_ib_gz_pts[NRGPU_MAX_GHOSTS];        /* inner points in layer g   */
+  int  ob_dir_start[NRGPU_MAX_GHOSTS][4];      /* offsets into outer arrays */
+  int  ib_start[NRGPU_MAX_GHOSTS];             /* offsets into inner arrays */
+  int  total_outer, total_inner;
+  int *outer_dest;      /* device: idx3 of each outer ghost point            */
+  int *outer_step;      /* device: FACE*stride toward the interior            */
+  int *inner_dest;      /* device: idx3 of each inner ghost point            */
+  int *inner_src;       /* device: idx3 of its interior source point         */
+  int *inner_parity;    /* device: bit t set <=> parity type t is -1          */
+} bc_struct;
+
+/*
+ * MoL_gridfunctions: the four RK4 buffers of RK_Allocate_Memory.h
+ * (MoLtimestepping/C_Code_Generation.py:97-103) plus auxevol storage.
+ * y_n and the running total are always FP64; k_odd/k_even/auxevol are FP64
+ * for NRGPU_PREC_FP64 and FP32 for NRGPU_PREC_MIXED.  All device pointers,
+ * each NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot long (auxevol: 6 gfs for BSSN).
+ */
+typedef struct MoL_gridfunctions {
+  int     precision;                     /* NRGPU_PREC_*                     */
+  double *y_n_gfs;
+  double *y_nplus1_running_total_gfs;
+  void   *k_odd_gfs;
+  void   *k_even_gfs;
+  void   *auxevol_gfs;
+} MoL_gridfunctions;
+
+/* ------------------------------------------------------------ library */
+int         nrgpu_version(void);
+/* Queue all subsequent work on this cudaStream_t (NULL = legacy default). */
+int         nrgpu_set_stream(void *cuda_stream);
+void       *nrgpu_get_stream(void);
+/* Message of the last failing call in this process. */
+const char *nrgpu_last_error(void);
+/* Number of kernels this library has launched in this process. */
+long long   nrgpu_kernel_launch_count(void);
+/* FD coefficients the kernels use: kind 0 = centred 1st, 1 = centred 2nd,
+ * 2 = upwind (+1 shifted) 1st.  Writes order+1 doubles (offsets -order/2
+ * ... +order/2, shifted by +1 for kind 2).  Host only, no GPU needed.
+ * finite_difference.py:252-369 computes the reference's. */
+int         nrgpu_fd_coeffs(int order, int kind, double *out);
+
+/* --------------------------------------------------------- grid set-up */
+/* reference_metric.py:1330-1395 (set_Nxx_dxx_invdx_params__and__xx):
+ * sets Nxx*, Nxx_plus_2NGHOSTS*, dxx*, invdx*, xxmin/xxmax from CoordSystem,
+ * NGHOSTS and the coordinate parameters already in *params, and fills the
+ * caller-allocated host arrays xx[d][Nxx_plus_2NGHOSTS_d] with cell-centred
+ * coordinates.  EigenCoord=1 uses the eigen-coordinate domain (Spherical for
+ * the Spherical family), as the reference does before building BC maps. */
+int    set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3],
+                                         paramstruct *params, double *xx[3]);
+/* reference_metric.py:1412-1439 (find_timestep): CFL * min over interior
+ * points of the proper spacing dxx_i * scalefactor_i, / wavespeed.  Host. */
+double find_timestep(const paramstruct *params, double CFL_FACTOR);
+
+/* ----------------------------------------------- reference metric tables */
+/* rfm_struct__malloc.h / rfm_struct__define.h / rfm_struct__freemem.h
+ * (reference_metric.py:871-886).  define() runs an FP64 kernel. */
+int rfm_struct__malloc(const paramstruct *params, rfm_struct *rfm);
+int rfm_struct__define(const paramstruct *params, rfm_struct *rfm);
+int rfm_struct__freemem(rfm_struct *rfm);
+/* Copy the FP64 table back to the host (testing): host buffer of
+ * nquant*N0*N1 doubles. */
+int rfm_struct__download(const rfm_struct *rfm, double *host);
+
+/* ---------------------------------------------------------- boundaries */
+/* boundary_conditions/driver_bcstruct.h:8-44 (set_up__bc_gz_map_and_parity_condns
+ * + set_bcstruct), built on the host on the eigen-coordinate grid, uploaded. */
+int driver_bcstruct(const paramstruct *params, bc_struct *bcstruct);
+int bcstruct_freemem(bc_struct *bcstruct);
+/* Host copy of the flattened map (testing).  Buffers sized total_outer /
+ * total_inner as reported in *bcstruct. */
+int bcstruct_download(const bc_struct *bcstruct, int *outer_dest, int *outer_step,
+                      int *inner_dest, int *inner_src, int *inner_parity);
+/* apply_bcs_curvilinear.h:56-64: per ghost layer, quadratic extrapolation at
+ * outer points then parity copy at inner points.  gfs_parity is a HOST array
+ * of NUM_GFS parity types (0..9). */
+int apply_bcs_curvilinear(const paramstruct *params, const bc_struct *bcstruct,
+                          int NUM_GFS, const int8_t *gfs_parity, double *gfs);
+int apply_bcs_curvilinear_f32(const paramstruct *params, const bc_struct *bcstruct,
+                              int NUM_GFS, const int8_t *gfs_parity, float *gfs);
+
+/* -------------------------------------------------------- RHS kernels */
+/* ScalarWave Cartesian: rhs_eval(params, in_gfs, rhs_gfs)
+ * (Tutorial-Start_to_Finish-ScalarWave.ipynb, rhs_eval; ScalarWave_RHSs.py:46-71) */
+int ScalarWave_rhs_eval(const paramstruct *params, const double *in_gfs, double *rhs_gfs);
+int ScalarWave_rhs_eval_f32(const paramstruct *params, const float *in_gfs, float *rhs_gfs);
+/* ScalarWave curvilinear: rhs_eval(rfmstruct, params, in_gfs, rhs_gfs)
+ * (ScalarWaveCurvilinear_RHSs.py:43-98) */
+int ScalarWaveCurvilinear_rhs_eval(const rfm_struct *rfm, const paramstruct *params,
+                                   const double *in_gfs, double *rhs_gfs);
+int ScalarWaveCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+                                       const float *in_gfs, float *rhs_gfs);
+/* Vacuum Maxwell System I, Cartesian (VacuumMaxwell_Flat_Evol_Cartesian.py:54-74) */
+int Maxwell_rhs_eval(const paramstruct *params, const double *in_gfs, double *rhs_gfs);
+int Maxwell_rhs_eval_f32(const paramstruct *params, const float *in_gfs, float *rhs_gfs);
+/* Maxwell divergence constraint C = d_i E^i at interior points
+ * (VacuumMaxwell_Flat_Evol_Cartesian.py:49-52) into aux_gfs[0]. */
+int Maxwell_Constraints(const paramstruct *params, const double *in_gfs, double *aux_gfs);
+/* BSSN conformal Ricci tensor into auxevol_gfs (RbarDD00..22, 6 gfs):
+ * Ricci_eval(rfmstruct, params, in_gfs, auxevol_gfs)
+ * (BSSN_quantities.py:260-425; Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:501-502) */
+int BSSN_Ricci_eval(const rfm_struct *rfm, const paramstruct *params,
+                    const double *in_gfs, double *auxevol_gfs);
+int BSSN_Ricci_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+                        const float *in_gfs, float *auxevol_gfs);
+/* BSSN + gauge RHSs: rhs_eval(rfmstruct, params, auxevol_gfs, in_gfs, rhs_gfs)
+ * (BSSN_RHSs.py:28-328, BSSN_gauge_RHSs.py:33-293; ...Two_BHs_Collide.ipynb:477-478) */
+int BSSN_rhs_eval(const rfm_struct *rfm, const paramstruct *params,
+                  const double *auxevol_gfs, const double *in_gfs, double *rhs_gfs);
+int BSSN_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+                      const float *auxevol_gfs, const float *in_gfs, float *rhs_gfs);
+/* enforce_detgammabar_constraint(rfmstruct, params, in_gfs) at ALL points
+ * (Enforce_Detgammabar_Constraint.py:16-75).  Arithmetic is FP64 in both. */
+int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const paramstruct *params,
+                                        double *in_gfs);
+int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const paramstruct *params,
+                                            float *in_gfs);
+/* Hamiltonian constraint H at interior points into aux_gfs[0]
+ * (BSSN_constraints.py:19-74; Ricci evaluated inline). */
+int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *params,
+                                const double *in_gfs, double *aux_gfs);
+
+/* --------------------------------------------------------- initial data */
+/* Brill-Lindquist two-puncture data converted to rescaled BSSN variables in
+ * the grid's coordinates at ALL points (BrillLindquist.py:48-82,
+ * ADM_Exact_Spherical_or_Cartesian_to_BSSNCurvilinear.py:16-135,
+ * BSSN_ID_function_string.py:9-45). */
+int BSSN_initial_data_BrillLindquist(const paramstruct *params,
+                                     double BH1_mass, const double BH1_posn[3],
+                                     double BH2_mass, const double BH2_posn[3],
+                                     double *in_gfs);
+
+/* ------------------------------------------------------- RK4 MoL step */
+/* One RK4 step of MoLtimestepping/RK_MoL.h for RK_method "RK4"
+ * (C_Code_Generation.py:266-329, Butcher table RK_Butcher_Table_Dictionary.py:86-91):
+ * four substeps of RHS -> RK update -> apply_bcs_curvilinear ->
+ * (BSSN only) enforce_detgammabar_constraint.  The RK update is fused into
+ * the RHS kernel's epilogue at interior points; ghost points are set by the
+ * boundary conditions, as in the reference where every ghost point is a
+ * boundary point.  rfm may be NULL for Cartesian grids. */
+int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruct *params,
+                             const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
+/* The same step, unfused, exactly in the reference's order: separate RHS
+ * kernel, LOOP_ALL_GFS_GPS update over all points, BCs, rescale. */
+int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *params,
+                                     const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
+/* Host-buffer form for callers whose state lives in host memory: copies
+ * y_n_gfs (host, FP64, pinned or pageable) to gfs->y_n_gfs, runs n_steps
+ * steps, copies the state back, and synchronises the stream. */
+int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *params,
+                    const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt,
+                    int n_steps, double *y_n_gfs_host);
+
+/* --------------------------------------------------------- diagnostics */
+/* Sum over interior points of f^2 (and of 1) for gridfunction `gf` of an
+ * FP64 array, FP64 accumulation; result[0] = sum f^2, result[1] = count.
+ * `result` is a DEVICE pointer to 2 doubles.  Used for the RMS L2 norms of
+ * the constraint diagnostics (Tutorial-Start_to_Finish-Solving_Maxwells_
+ * Equations_in_Vacuum-Cartesian.ipynb:1089-1106). */
+int nrgpu_l2_norm_sq(const paramstruct *params, const double *gfs, int gf,
+                     double *scratch, int scratch_len, double *result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NRGPU_H */

@@ -1,0 +1,352 @@
+// bcs.cu -- curvilinear boundary conditions.
+//
+// Map construction (host, once per grid) follows
+// CurviBoundaryConditions/boundary_conditions/set_up__bc_gz_map_and_parity_condns.h:7-113
+// and set_bcstruct.h:32-124:
+//  * every point of the eigen-coordinate grid is mapped to Cartesian and back
+//    (EigenCoord_xx_to_Cart / EigenCoord_Cart_to_xx); if the returned index
+//    differs from the point's own, the point is an inner (parity) boundary
+//    point that copies from that interior index, else an outer point (or
+//    interior);
+//  * parities are dot products of the unit vectors at the two points
+//    (CurviBoundaryConditions.py:80-113), rank-2 types as products;
+//  * ghost layers are visited innermost first; within a layer the outer
+//    points are listed face by face (i0 min, i0 max, i1 min, i1 max, i2 min,
+//    i2 max) with the box widened after each face, then the inner points in
+//    the same face order.
+// Application (apply_bcs_curvilinear.h:7-64) runs per layer: the i0 faces,
+// then the i1 faces (which read the i0 ghost columns just written), then the
+// i2 faces, then the inner points.  Each of those four phases is one launch
+// covering all gridfunctions; inside a phase no point reads another's output.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "rfm.cuh"
+
+namespace nrgpu {
+
+static void eigen_xx_to_cart(int cs, double x0, double x1, double x2, double out[3]) {
+  if (cs == NRGPU_COORD_CARTESIAN) {
+    out[0] = x0; out[1] = x1; out[2] = x2;
+    return;
+  }
+  // Spherical eigen-coordinates (reference_metric.py:163-166)
+  out[0] = x0 * sin(x1) * cos(x2);
+  out[1] = x0 * sin(x1) * sin(x2);
+  out[2] = x0 * cos(x1);
+}
+
+static void eigen_cart_to_xx(int cs, const double c[3], double out[3]) {
+  if (cs == NRGPU_COORD_CARTESIAN) {
+    out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+    return;
+  }
+  // reference_metric.py:113-115
+  const double r = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  out[0] = r;
+  out[1] = acos(c[2] / r);
+  out[2] = atan2(c[1], c[0]);
+}
+
+// Unit vectors (rows) of the eigen-coordinate basis at (x0,x1,x2)
+// (reference_metric.py:180-182 for the Spherical family; identity otherwise).
+static void unit_vectors(int cs, double x1, double x2, double U[3][3]) {
+  if (cs == NRGPU_COORD_CARTESIAN) {
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) U[i][j] = (i == j) ? 1.0 : 0.0;
+    return;
+  }
+  const double st = sin(x1), ct = cos(x1), sp = sin(x2), cp = cos(x2);
+  U[0][0] = st * cp; U[0][1] = st * sp; U[0][2] = ct;
+  U[1][0] = ct * cp; U[1][1] = ct * sp; U[1][2] = -st;
+  U[2][0] = -sp;     U[2][1] = cp;      U[2][2] = 0.0;
+}
+
+struct GzMap {
+  int i0, i1, i2;    // -1 => not an inner boundary point
+  int parity_bits;   // bit t set <=> parity type t is -1
+};
+
+static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
+  // Eigen-coordinate grid: same Nxx and NGHOSTS, eigen domain.
+  paramstruct e = *p;
+  const int Nxx[3] = {p->Nxx0, p->Nxx1, p->Nxx2};
+  std::vector<double> xs[3];
+  const int np[3] = {p->Nxx_plus_2NGHOSTS0, p->Nxx_plus_2NGHOSTS1, p->Nxx_plus_2NGHOSTS2};
+  double *xxp[3];
+  for (int d = 0; d < 3; d++) {
+    xs[d].resize(np[d]);
+    xxp[d] = xs[d].data();
+  }
+  int st = set_Nxx_dxx_invdx_params__and__xx(1, Nxx, &e, xxp);
+  if (st) return st;
+  const int cs = (p->CoordSystem == NRGPU_COORD_CARTESIAN) ? NRGPU_COORD_CARTESIAN : NRGPU_COORD_SPHERICAL;
+  const int ng = p->NGHOSTS;
+  const double dxx[3] = {e.dxx0, e.dxx1, e.dxx2};
+  // set_up__bc_gz_map_and_parity_condns.h:17-19 recovers xxmin from xx[d][0].
+  double xxmin[3];
+  for (int d = 0; d < 3; d++) xxmin[d] = xs[d][0] - ((double)(0 - ng) + (1.0 / 2.0)) * dxx[d];
+  map.assign((size_t)np[0] * np[1] * np[2], GzMap{-1, -1, -1, 0});
+  for (int i2 = 0; i2 < np[2]; i2++)
+    for (int i1 = 0; i1 < np[1]; i1++)
+      for (int i0 = 0; i0 < np[0]; i0++) {
+        double c[3], xin[3], c2[3];
+        eigen_xx_to_cart(cs, xs[0][i0], xs[1][i1], xs[2][i2], c);
+        eigen_cart_to_xx(cs, c, xin);
+        int ib[3];
+        for (int d = 0; d < 3; d++)
+          ib[d] = (int)((xin[d] - xxmin[d] - (1.0 / 2.0) * dxx[d] + ((double)ng) * dxx[d]) / dxx[d] + 0.5);
+        for (int d = 0; d < 3; d++)
+          if (ib[d] < 0 || ib[d] >= np[d]) {
+            set_error("ghost-zone map: point (%d,%d,%d) maps outside the grid", i0, i1, i2);
+            return NRGPU_ERR_BCMAP;
+          }
+        eigen_xx_to_cart(cs, xs[0][ib[0]], xs[1][ib[1]], xs[2][ib[2]], c2);
+        for (int d = 0; d < 3; d++)
+          if (fabs(c[d] - c2[d]) > 1e-8) {
+            set_error("Cartesian disagreement at (%d,%d,%d): (%.15e %.15e %.15e) != (%.15e %.15e %.15e)",
+                      i0, i1, i2, c[0], c[1], c[2], c2[0], c2[1], c2[2]);
+            return NRGPU_ERR_BCMAP;
+          }
+        const size_t idx = (size_t)i0 + (size_t)np[0] * ((size_t)i1 + (size_t)np[1] * i2);
+        if (ib[0] == i0 && ib[1] == i1 && ib[2] == i2) continue;
+        double U[3][3], Ui[3][3], par[10];
+        unit_vectors(cs, xs[1][i1], xs[2][i2], U);
+        unit_vectors(cs, xs[1][ib[1]], xs[2][ib[2]], Ui);
+        par[0] = 1.0;
+        for (int t = 1; t <= 3; t++) {
+          par[t] = 0.0;
+          for (int i = 0; i < 3; i++) par[t] += U[t - 1][i] * Ui[t - 1][i];
+        }
+        int cnt = 4;
+        for (int i = 0; i < 3; i++)
+          for (int j = i; j < 3; j++) par[cnt++] = par[i + 1] * par[j + 1];
+        int bits = 0;
+        for (int t = 0; t < 10; t++) {
+          if ((par[t] > 0 && fabs(par[t] - 1.0) > 1e-8) || (par[t] <= 0 && fabs(par[t] + 1.0) > 1e-8)) {
+            set_error("parity %d evaluated to %e at (%d,%d,%d), not +-1", t, par[t], i0, i1, i2);
+            return NRGPU_ERR_BCMAP;
+          }
+          if (par[t] < 0.0) bits |= (1 << t);
+        }
+        map[idx] = GzMap{ib[0], ib[1], ib[2], bits};
+      }
+  return NRGPU_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+struct ParityTypes {
+  int8_t t[64];
+};
+
+template <typename T>
+__global__ void bc_outer_kernel(const int *__restrict__ dest, const int *__restrict__ step, int npts,
+                                int ngfs, long long ntot, T *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  T *f = gfs + (long long)gf * ntot;
+  const long long d = dest[p], s = step[p];
+  // +3 f1 - 3 f2 + 1 f3, left to right without contraction (BC_UPDATE_OUTER).
+  const T a = f[d + s], b = f[d + 2 * s], c = f[d + 3 * s];
+  T v;
+  if constexpr (sizeof(T) == 8) {
+    v = __dadd_rn(__dsub_rn(__dmul_rn(3.0, a), __dmul_rn(3.0, b)), c);
+  } else {
+    v = __fadd_rn(__fsub_rn(__fmul_rn(3.0f, a), __fmul_rn(3.0f, b)), c);
+  }
+  f[d] = v;
+}
+
+template <typename T>
+__global__ void bc_inner_kernel(const int *__restrict__ dest, const int *__restrict__ src,
+                                const int *__restrict__ parity, int npts, int ngfs, long long ntot,
+                                ParityTypes types, T *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  T *f = gfs + (long long)gf * ntot;
+  const bool neg = (parity[p] >> types.t[gf]) & 1;
+  const T v = f[src[p]];
+  f[dest[p]] = neg ? -v : v;
+}
+
+template <typename T>
+int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
+                          const int8_t *gfs_parity, T *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL argument");
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64, "NUM_GFS %d out of range", NUM_GFS);
+  NRGPU_REQUIRE(bc->NGHOSTS == p->NGHOSTS, "bcstruct built for NGHOSTS=%d, params say %d", bc->NGHOSTS,
+                p->NGHOSTS);
+  ParityTypes types;
+  memset(&types, 0, sizeof(types));
+  for (int g = 0; g < NUM_GFS; g++) {
+    const int t = gfs_parity ? gfs_parity[g] : 0;
+    NRGPU_REQUIRE(t >= 0 && t <= 9, "parity type %d of gf %d not in 0..9", t, g);
+    types.t[g] = (int8_t)t;
+  }
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  const int B = 128;
+  for (int g = 0; g < bc->NGHOSTS; g++) {
+    for (int d = 0; d < 3; d++) {
+      const int a = bc->ob_dir_start[g][d], b = bc->ob_dir_start[g][d + 1];
+      const int n = b - a;
+      if (n <= 0) continue;
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_outer_kernel<T><<<grid, B, 0, stream()>>>(bc->outer_dest + a, bc->outer_step + a, n, NUM_GFS, ntot, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+    const int n = bc->num_ib_gz_pts[g];
+    if (n > 0) {
+      const int a = bc->ib_start[g];
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_inner_kernel<T><<<grid, B, 0, stream()>>>(bc->inner_dest + a, bc->inner_src + a,
+                                                   bc->inner_parity + a, n, NUM_GFS, ntot, types, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+  }
+  return NRGPU_OK;
+}
+
+template int apply_bcs_impl<double>(const paramstruct *, const bc_struct *, int, const int8_t *, double *);
+template int apply_bcs_impl<float>(const paramstruct *, const bc_struct *, int, const int8_t *, float *);
+
+}  // namespace nrgpu
+
+using namespace nrgpu;
+
+extern "C" {
+
+int driver_bcstruct(const paramstruct *p, bc_struct *bc) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(bc != nullptr, "bcstruct is NULL");
+  memset(bc, 0, sizeof(*bc));
+  std::vector<GzMap> map;
+  st = build_gz_map(p, map);
+  if (st) return st;
+  const int ng = p->NGHOSTS;
+  const int n0 = p->Nxx_plus_2NGHOSTS0, n1 = p->Nxx_plus_2NGHOSTS1, n2 = p->Nxx_plus_2NGHOSTS2;
+  auto IDX3 = [&](int i0, int i1, int i2) { return i0 + n0 * (i1 + n1 * i2); };
+  const int stride[3] = {1, n0, n0 * n1};
+  std::vector<int> od, os, id_, is_, ip;
+  int imin[3] = {ng, ng, ng};
+  int imax[3] = {n0 - ng, n1 - ng, n2 - ng};
+  bc->NGHOSTS = ng;
+  for (int g = 0; g < ng; g++) {
+    // The six faces of this layer, each with the box widened afterwards
+    // (set_bcstruct.h:94-100 and :111-116 use the same sequence).
+    int lo[3] = {imin[0], imin[1], imin[2]}, hi[3] = {imax[0], imax[1], imax[2]};
+    struct Face { int d, side; int r[3][2]; };
+    Face faces[6];
+    int nf = 0;
+    for (int d = 0; d < 3; d++)
+      for (int side = 0; side < 2; side++) {
+        Face f;
+        f.d = d;
+        f.side = side;
+        for (int e = 0; e < 3; e++) { f.r[e][0] = lo[e]; f.r[e][1] = hi[e]; }
+        if (side == 0) { f.r[d][0] = lo[d] - 1; f.r[d][1] = lo[d]; lo[d]--; }
+        else           { f.r[d][0] = hi[d];     f.r[d][1] = hi[d] + 1; hi[d]++; }
+        faces[nf++] = f;
+      }
+    bc->ob_dir_start[g][0] = (int)od.size();
+    for (int fi = 0; fi < 6; fi++) {
+      const Face &f = faces[fi];
+      const int face_sign = (f.side == 0) ? +1 : -1;  // MINFACE = +1, MAXFACE = -1
+      for (int i2 = f.r[2][0]; i2 < f.r[2][1]; i2++)
+        for (int i1 = f.r[1][0]; i1 < f.r[1][1]; i1++)
+          for (int i0 = f.r[0][0]; i0 < f.r[0][1]; i0++) {
+            const int idx = IDX3(i0, i1, i2);
+            if (map[idx].i0 == -1) {
+              od.push_back(idx);
+              os.push_back(face_sign * stride[f.d]);
+            }
+          }
+      if (fi % 2 == 1) bc->ob_dir_start[g][fi / 2 + 1] = (int)od.size();
+    }
+    bc->num_ob_gz_pts[g] = (int)od.size() - bc->ob_dir_start[g][0];
+    bc->ib_start[g] = (int)id_.size();
+    for (int fi = 0; fi < 6; fi++) {
+      const Face &f = faces[fi];
+      for (int i2 = f.r[2][0]; i2 < f.r[2][1]; i2++)
+        for (int i1 = f.r[1][0]; i1 < f.r[1][1]; i1++)
+          for (int i0 = f.r[0][0]; i0 < f.r[0][1]; i0++) {
+            const int idx = IDX3(i0, i1, i2);
+            const GzMap &m = map[idx];
+            if (m.i0 != -1) {
+              id_.push_back(idx);
+              is_.push_back(IDX3(m.i0, m.i1, m.i2));
+              ip.push_back(m.parity_bits);
+            }
+          }
+    }
+    bc->num_ib_gz_pts[g] = (int)id_.size() - bc->ib_start[g];
+    for (int d = 0; d < 3; d++) { imin[d]--; imax[d]++; }
+  }
+  // Every point reached through an outer stencil must be a grid point.
+  const long long ntot = (long long)n0 * n1 * n2;
+  for (size_t k = 0; k < od.size(); k++)
+    if ((long long)od[k] + 3LL * os[k] < 0 || (long long)od[k] + 3LL * os[k] >= ntot) {
+      set_error("outer boundary stencil leaves the grid (grid too small for NGHOSTS)");
+      return NRGPU_ERR_BCMAP;
+    }
+  bc->total_outer = (int)od.size();
+  bc->total_inner = (int)id_.size();
+  auto upload = [&](int **dst, const std::vector<int> &v) -> int {
+    *dst = nullptr;
+    if (v.empty()) return NRGPU_OK;
+    NRGPU_CUDA_CHECK(cudaMalloc(dst, v.size() * sizeof(int)));
+    NRGPU_CUDA_CHECK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return NRGPU_OK;
+  };
+  if ((st = upload(&bc->outer_dest, od))) return st;
+  if ((st = upload(&bc->outer_step, os))) return st;
+  if ((st = upload(&bc->inner_dest, id_))) return st;
+  if ((st = upload(&bc->inner_src, is_))) return st;
+  if ((st = upload(&bc->inner_parity, ip))) return st;
+  return NRGPU_OK;
+}
+
+int bcstruct_freemem(bc_struct *bc) {
+  if (!bc) return NRGPU_OK;
+  int **ptrs[5] = {&bc->outer_dest, &bc->outer_step, &bc->inner_dest, &bc->inner_src, &bc->inner_parity};
+  for (int k = 0; k < 5; k++)
+    if (*ptrs[k]) {
+      cudaFree(*ptrs[k]);
+      *ptrs[k] = nullptr;
+    }
+  return NRGPU_OK;
+}
+
+int bcstruct_download(const bc_struct *bc, int *outer_dest, int *outer_step, int *inner_dest,
+                      int *inner_src, int *inner_parity) {
+  NRGPU_REQUIRE(bc != nullptr, "bcstruct is NULL");
+  auto dl = [&](int *dst, const int *src, int n) -> int {
+    if (n > 0 && dst && src) NRGPU_CUDA_CHECK(cudaMemcpy(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost));
+    return NRGPU_OK;
+  };
+  int st;
+  if ((st = dl(outer_dest, bc->outer_dest, bc->total_outer))) return st;
+  if ((st = dl(outer_step, bc->outer_step, bc->total_outer))) return st;
+  if ((st = dl(inner_dest, bc->inner_dest, bc->total_inner))) return st;
+  if ((st = dl(inner_src, bc->inner_src, bc->total_inner))) return st;
+  if ((st = dl(inner_parity, bc->inner_parity, bc->total_inner))) return st;
+  return NRGPU_OK;
+}
+
+int apply_bcs_curvilinear(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
+                          const int8_t *gfs_parity, double *gfs) {
+  return apply_bcs_impl<double>(p, bc, NUM_GFS, gfs_parity, gfs);
+}
+int apply_bcs_curvilinear_f32(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
+                              const int8_t *gfs_parity, float *gfs) {
+  return apply_bcs_impl<float>(p, bc, NUM_GFS, gfs_parity, gfs);
+}
+
+}  // extern "C"

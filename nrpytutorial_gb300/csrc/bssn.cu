@@ -1,0 +1,384 @@
+// bssn.cu -- BSSN dispatch, det(gammabar) = det(gammahat) rescale,
+// Hamiltonian constraint, Brill-Lindquist initial data, and the C ABI.
+#include <math.h>
+
+#include "bssn_kernels.cuh"
+
+namespace nrgpu {
+namespace bssn {
+
+NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 4)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 6)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
+
+#define NRGPU_BSSN_SWITCH(CALL)                                                               \
+  switch (p->CoordSystem * 16 + p->FD_order) {                                                \
+    case NRGPU_COORD_CARTESIAN * 16 + 4: return CALL(NRGPU_COORD_CARTESIAN, 4);               \
+    case NRGPU_COORD_CARTESIAN * 16 + 6: return CALL(NRGPU_COORD_CARTESIAN, 6);               \
+    case NRGPU_COORD_SINHSPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SINHSPHERICAL, 4);       \
+    case NRGPU_COORD_SPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SPHERICAL, 4);               \
+  }                                                                                           \
+  set_error("BSSN: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order); \
+  return NRGPU_ERR_UNSUPPORTED;
+
+static int check_bssn(const rfm_struct *rfm, const paramstruct *p) {
+  int st = check_params(p);
+  if (st) return st;
+  // The upwinded stencils reach FD_order/2 + 1 points (NGHOSTS rule of
+  // Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:835).
+  NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2+1 (have %d)", p->NGHOSTS);
+  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || (rfm && rfm->table64 && rfm->N0 == p->Nxx_plus_2NGHOSTS0 &&
+                                                             rfm->N1 == p->Nxx_plus_2NGHOSTS1),
+                "curvilinear BSSN needs an rfm_struct defined for this grid");
+  return NRGPU_OK;
+}
+
+// ---------------------------------------------------- det(gammabar) rescale
+// h'_ij = (|det ghat| / det gammabar)^(1/3) (delta_ij + h_ij) - delta_ij at
+// all points (Enforce_Detgammabar_Constraint.py:42-50), FP64 arithmetic for
+// either storage type.
+template <int CS, typename T>
+__global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__restrict__ gfs) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
+  if (i0 >= g.n0) return;
+  const long long idx = (long long)i0 + (long long)g.n0 * ((long long)i1 + (long long)g.n1 * i2);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  double h[3][3], gb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      h[i][j] = h[j][i] = (double)gfs[(long long)(HDD00 + S6(i, j)) * g.ntot + idx];
+      double v = RfmMask<CS>::trivial ? h[i][j] : h[i][j] * rf.ReDD(i, j);
+      if (i == j) v += rf.ghatDD(i);
+      gb[i][j] = gb[j][i] = v;
+    }
+  const double det = -gb[0][2] * gb[0][2] * gb[1][1] + 2.0 * gb[0][1] * gb[0][2] * gb[1][2] -
+                     gb[0][0] * gb[1][2] * gb[1][2] - gb[0][1] * gb[0][1] * gb[2][2] +
+                     gb[0][0] * gb[1][1] * gb[2][2];
+  const double f = cbrt(fabs(rf.detg()) / det);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      const double d = (i == j) ? 1.0 : 0.0;
+      gfs[(long long)(HDD00 + S6(i, j)) * g.ntot + idx] = (T)(f * (d + h[i][j]) - d);
+    }
+}
+
+// --------------------------------------------------- Hamiltonian constraint
+template <int CS, int ORDER>
+__global__ void __launch_bounds__(kBlockX *kBlockY)
+    hamiltonian_kernel(Grid g, const double *__restrict__ in, const double *__restrict__ tab,
+                       double *__restrict__ aux) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  using R = double;
+  using M = RfmMask<CS>;
+  Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const R inv[3] = {g.invdx0, g.invdx1, g.invdx2};
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  Metric<CS, R> m;
+  metric_point<ORDER, CS, R>(P, rf, inv, m);
+  R Rbar[6];
+  ricci_point<ORDER, CS, R>(P, rf, inv, m, Rbar);
+  const R cf = __ldg(P.gf(CF)), trK = __ldg(P.gf(TRK));
+  R Abar[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      const R a = __ldg(P.gf(ADD00 + S6(i, j)));
+      Abar[i][j] = Abar[j][i] = M::trivial ? a : a * rf.ReDD(i, j);
+    }
+  R H = (R)(2.0 / 3.0) * trK * trK;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R auu = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int l = 0; l < 3; l++) auu += m.gUU[i][k] * m.gUU[j][l] * Abar[k][l];
+      H -= Abar[i][j] * auu;
+    }
+  R cfd[3], phid[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    cfd[i] = D1<ORDER, R>(P, CF, i, inv);
+    phid[i] = -cfd[i] / (2.0 * cf);
+  }
+  R Rtr = 0.0, pp = 0.0, pdd = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Rtr += m.gUU[i][j] * Rbar[S6(i, j)];
+      pp += m.gUU[i][j] * phid[i] * phid[j];
+      R v = (-D2<ORDER, R>(P, CF, i, j, inv) + cfd[i] * cfd[j] / cf) / (2.0 * cf);
+#pragma unroll
+      for (int k = 0; k < 3; k++) v -= m.Gbar[k][i][j] * phid[k];
+      pdd += m.gUU[i][j] * v;
+    }
+  H += cf * cf * (Rtr - 8.0 * (pp + pdd));
+  aux[idx] = H;
+}
+
+// ------------------------------------------------- Brill-Lindquist data
+// Forward-mode dual numbers over (xx0, xx1, xx2): the initial Lambdabar^i
+// needs exact first derivatives of gammabar_ij (BSSN_in_terms_of_ADM.py:78-117).
+struct Dual {
+  double v, d[3];
+};
+__device__ __forceinline__ Dual dconst(double c) { return Dual{c, {0.0, 0.0, 0.0}}; }
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) {
+  return Dual{a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}};
+}
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) {
+  return Dual{a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}};
+}
+__device__ __forceinline__ Dual operator-(Dual a) { return Dual{-a.v, {-a.d[0], -a.d[1], -a.d[2]}}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
+  Dual r;
+  r.v = a.v * b.v;
+  for (int k = 0; k < 3; k++) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+__device__ __forceinline__ Dual operator*(double c, Dual a) { return Dual{c * a.v, {c * a.d[0], c * a.d[1], c * a.d[2]}}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+  Dual r;
+  r.v = a.v / b.v;
+  for (int k = 0; k < 3; k++) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+  return r;
+}
+__device__ __forceinline__ Dual chain(Dual a, double f, double df) {
+  return Dual{f, {df * a.d[0], df * a.d[1], df * a.d[2]}};
+}
+__device__ __forceinline__ Dual dexp(Dual a) { const double e = exp(a.v); return chain(a, e, e); }
+__device__ __forceinline__ Dual dsin(Dual a) { return chain(a, sin(a.v), cos(a.v)); }
+__device__ __forceinline__ Dual dcos(Dual a) { return chain(a, cos(a.v), -sin(a.v)); }
+__device__ __forceinline__ Dual dsqrt(Dual a) { const double s = sqrt(a.v); return chain(a, s, 0.5 / s); }
+__device__ __forceinline__ Dual dcbrt(Dual a) {
+  const double c = cbrt(a.v);
+  return chain(a, c, c / (3.0 * a.v));
+}
+
+struct BLParams {
+  double m1, x1[3], m2, x2[3];
+};
+
+template <int CS>
+__global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gfs) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
+  const int n0 = p.Nxx_plus_2NGHOSTS0, n1 = p.Nxx_plus_2NGHOSTS1, n2 = p.Nxx_plus_2NGHOSTS2;
+  if (i0 >= n0) return;
+  const long long ntot = (long long)n0 * n1 * n2;
+  const long long idx = (long long)i0 + (long long)n0 * ((long long)i1 + (long long)n1 * i2);
+  const Dual X0{xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS), {1.0, 0.0, 0.0}};
+  const Dual X1{xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS), {0.0, 1.0, 0.0}};
+  const Dual X2{xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS), {0.0, 0.0, 1.0}};
+  Dual xc[3], J[3][3], s[3];
+  if (CS == NRGPU_COORD_CARTESIAN) {
+    xc[0] = X0; xc[1] = X1; xc[2] = X2;
+    for (int a = 0; a < 3; a++) {
+      s[a] = dconst(1.0);
+      for (int b = 0; b < 3; b++) J[a][b] = dconst(a == b ? 1.0 : 0.0);
+    }
+  } else {
+    Dual r, dr;
+    if (CS == NRGPU_COORD_SINHSPHERICAL) {
+      const double den = exp(1.0 / p.SINHW) - exp(-1.0 / p.SINHW);
+      const Dual ep = dexp((1.0 / p.SINHW) * X0), em = dexp((-1.0 / p.SINHW) * X0);
+      r = (p.AMPL / den) * (ep - em);
+      dr = (p.AMPL / (p.SINHW * den)) * (ep + em);
+    } else {
+      r = X0;
+      dr = dconst(1.0);
+    }
+    const Dual st = dsin(X1), ct = dcos(X1), sp = dsin(X2), cp = dcos(X2);
+    xc[0] = r * st * cp; xc[1] = r * st * sp; xc[2] = r * ct;
+    J[0][0] = dr * st * cp; J[0][1] = r * ct * cp; J[0][2] = -(r * st * sp);
+    J[1][0] = dr * st * sp; J[1][1] = r * ct * sp; J[1][2] = r * st * cp;
+    J[2][0] = dr * ct;      J[2][1] = -(r * st);   J[2][2] = dconst(0.0);
+    s[0] = dr; s[1] = r; s[2] = r * st;
+  }
+  // psi = 1 + sum m/(2|x - x_BH|) (BrillLindquist.py:58-61)
+  Dual psi = dconst(1.0);
+  {
+    Dual dx = xc[0] - dconst(bl.x1[0]), dy = xc[1] - dconst(bl.x1[1]), dz = xc[2] - dconst(bl.x1[2]);
+    psi = psi + dconst(bl.m1) / (2.0 * dsqrt(dx * dx + dy * dy + dz * dz));
+    dx = xc[0] - dconst(bl.x2[0]); dy = xc[1] - dconst(bl.x2[1]); dz = xc[2] - dconst(bl.x2[2]);
+    psi = psi + dconst(bl.m2) / (2.0 * dsqrt(dx * dx + dy * dy + dz * dz));
+  }
+  const Dual psi2 = psi * psi, psi4 = psi2 * psi2;
+  // gamma_ij in the grid basis: psi^4 J^k_i J^k_j
+  Dual gam[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = i; j < 3; j++) {
+      Dual acc = dconst(0.0);
+      for (int k = 0; k < 3; k++) acc = acc + J[k][i] * J[k][j];
+      gam[i][j] = gam[j][i] = psi4 * acc;
+    }
+  auto det3 = [](Dual a[3][3]) {
+    return -(a[0][2] * a[0][2] * a[1][1]) + 2.0 * (a[0][1] * a[0][2] * a[1][2]) - a[0][0] * a[1][2] * a[1][2] -
+           a[0][1] * a[0][1] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+  };
+  const Dual detgam = det3(gam);
+  const Dual detghat = (s[0] * s[0]) * (s[1] * s[1]) * (s[2] * s[2]);
+  const Dual fac = dcbrt(detghat / detgam);
+  Dual gb[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) gb[i][j] = fac * gam[i][j];
+  const Dual detgb = det3(gb);
+  // inverse of gammabar (values) and of ghat
+  double g[3][3], gUU[3][3], dtmp;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) g[i][j] = gb[i][j].v;
+  sym_inverse<double>(g, gUU, dtmp);
+  double out[NUM_EVOL_GFS];
+  for (int k = 0; k < NUM_EVOL_GFS; k++) out[k] = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = i; j < 3; j++) {
+      const double ghat = (i == j) ? s[i].v * s[i].v : 0.0;
+      out[HDD00 + S6(i, j)] = (gb[i][j].v - ghat) / (s[i].v * s[j].v);
+    }
+  // W = (gamma / gammabar)^(-1/6)  (BSSN_in_terms_of_ADM.py:141-144)
+  out[CF] = pow(detgam.v / detgb.v, -1.0 / 6.0);
+  out[ALPHA] = 1.0 / psi2.v;
+  // Lambdabar^i = gammabar^jk (Gammabar^i_jk - Gammahat^i_jk), lambda^i = Lambdabar^i s_i
+  for (int i = 0; i < 3; i++) {
+    double Lb = 0.0;
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++) {
+        double Gb = 0.0;
+        for (int l = 0; l < 3; l++)
+          Gb += 0.5 * gUU[i][l] * (gb[l][j].d[k] + gb[l][k].d[j] - gb[j][k].d[l]);
+        // diagonal ghat: Gammahat^i_jk = (d_k g_ij + d_j g_ik - d_i g_jk)/(2 g_ii)
+        const double gii = s[i].v * s[i].v;
+        auto dg = [&](int a, int b, int c) { return a == b ? 2.0 * s[a].v * s[a].d[c] : 0.0; };
+        const double Gh = (dg(i, j, k) + dg(i, k, j) - dg(j, k, i)) / (2.0 * gii);
+        Lb += gUU[j][k] * (Gb - Gh);
+      }
+    out[LAMBDAU0 + i] = Lb * s[i].v;
+  }
+  for (int k = 0; k < NUM_EVOL_GFS; k++) gfs[(long long)k * ntot + idx] = out[k];
+}
+
+}  // namespace bssn
+
+using namespace bssn;
+
+#define RICCI_CALL(CS, ORD) ricci_launch_t<CS, ORD>(rfm, p, in, in_is_f64, prec, auxevol)
+int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64, int prec,
+                      void *auxevol) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(in && auxevol, "NULL gridfunctions");
+  NRGPU_BSSN_SWITCH(RICCI_CALL)
+}
+#define RHS_CALL(CS, ORD) rhs_launch_t<CS, ORD>(rfm, p, a)
+int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
+  NRGPU_BSSN_SWITCH(RHS_CALL)
+}
+
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(gfs != nullptr, "NULL gridfunctions");
+  Grid g = make_grid(p);
+  dim3 block(64), grid((g.n0 + 63) / 64, g.n1, g.n2);
+  const double *tab = rfm ? rfm->table64 : nullptr;
+  const bool cart = p->CoordSystem == NRGPU_COORD_CARTESIAN;
+#define ENF(T)                                                                                           \
+  if (cart) enforce_kernel<NRGPU_COORD_CARTESIAN, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);     \
+  else if (p->CoordSystem == NRGPU_COORD_SPHERICAL)                                                      \
+    enforce_kernel<NRGPU_COORD_SPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
+  else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
+  if (is_f64) { ENF(double) } else { ENF(float) }
+#undef ENF
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+}  // namespace nrgpu
+
+using namespace nrgpu;
+
+static int bssn_plain(const rfm_struct *rfm, const paramstruct *p, const void *aux, const void *in, void *rhs,
+                      int prec) {
+  NRGPU_REQUIRE(p && aux && in && rhs, "NULL argument");
+  StageArgs a{};
+  a.stage = -1;
+  a.prec = prec;
+  a.in = in;
+  a.in_is_f64 = (prec == NRGPU_PREC_FP64);
+  a.out = rhs;
+  a.auxevol = (void *)aux;
+  return bssn_rhs_launch(rfm, p, a);
+}
+
+extern "C" {
+int BSSN_Ricci_eval(const rfm_struct *rfm, const paramstruct *p, const double *in, double *aux) {
+  return bssn_ricci_launch(rfm, p, in, true, NRGPU_PREC_FP64, aux);
+}
+int BSSN_Ricci_eval_f32(const rfm_struct *rfm, const paramstruct *p, const float *in, float *aux) {
+  return bssn_ricci_launch(rfm, p, in, false, NRGPU_PREC_MIXED, aux);
+}
+int BSSN_rhs_eval(const rfm_struct *rfm, const paramstruct *p, const double *aux, const double *in, double *rhs) {
+  return bssn_plain(rfm, p, aux, in, rhs, NRGPU_PREC_FP64);
+}
+int BSSN_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *p, const float *aux, const float *in, float *rhs) {
+  return bssn_plain(rfm, p, aux, in, rhs, NRGPU_PREC_MIXED);
+}
+int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const paramstruct *p, double *gfs) {
+  return bssn_enforce_launch(rfm, p, gfs, true);
+}
+int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const paramstruct *p, float *gfs) {
+  return bssn_enforce_launch(rfm, p, gfs, false);
+}
+int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, const double *in, double *aux) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(in && aux, "NULL argument");
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  const double *tab = rfm ? rfm->table64 : nullptr;
+  switch (p->CoordSystem * 16 + p->FD_order) {
+    case NRGPU_COORD_CARTESIAN * 16 + 4:
+      hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_CARTESIAN * 16 + 6:
+      hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 6><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_SINHSPHERICAL * 16 + 4:
+      hamiltonian_kernel<NRGPU_COORD_SINHSPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_SPHERICAL * 16 + 4:
+      hamiltonian_kernel<NRGPU_COORD_SPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    default:
+      set_error("Hamiltonian: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
+      return NRGPU_ERR_UNSUPPORTED;
+  }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+int BSSN_initial_data_BrillLindquist(const paramstruct *p, double m1, const double x1[3], double m2,
+                                     const double x2[3], double *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(x1 && x2 && gfs, "NULL argument");
+  BLParams bl{m1, {x1[0], x1[1], x1[2]}, m2, {x2[0], x2[1], x2[2]}};
+  dim3 block(64), grid((p->Nxx_plus_2NGHOSTS0 + 63) / 64, p->Nxx_plus_2NGHOSTS1, p->Nxx_plus_2NGHOSTS2);
+  if (p->CoordSystem == NRGPU_COORD_CARTESIAN)
+    bl_id_kernel<NRGPU_COORD_CARTESIAN><<<grid, block, 0, stream()>>>(*p, bl, gfs);
+  else if (p->CoordSystem == NRGPU_COORD_SPHERICAL)
+    bl_id_kernel<NRGPU_COORD_SPHERICAL><<<grid, block, 0, stream()>>>(*p, bl, gfs);
+  else
+    bl_id_kernel<NRGPU_COORD_SINHSPHERICAL><<<grid, block, 0, stream()>>>(*p, bl, gfs);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+}

@@ -1,0 +1,107 @@
+// bssn_kernels.cuh -- BSSN Ricci / RHS kernels and their launchers,
+// templated on coordinate system and FD order.  Each (CS, ORDER) pair is
+// instantiated in its own translation unit (bssn_inst_*.cu) so the heavy
+// kernels compile in parallel.
+#pragma once
+#include "bssn.cuh"
+#include "epilogue.cuh"
+#include "systems.cuh"
+
+namespace nrgpu {
+namespace bssn {
+
+constexpr int kBlockX = 32, kBlockY = 4;
+
+template <typename R, typename Tin, int CS, int ORDER, typename TAux>
+__global__ void __launch_bounds__(kBlockX *kBlockY)
+    ricci_kernel(Grid g, const Tin *__restrict__ in, const R *__restrict__ tab, TAux *__restrict__ aux) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  Point<Tin> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  Metric<CS, R> m;
+  metric_point<ORDER, CS, R>(P, rf, inv, m);
+  R Rbar[6];
+  ricci_point<ORDER, CS, R>(P, rf, inv, m, Rbar);
+#pragma unroll
+  for (int k = 0; k < 6; k++) aux[(long long)k * g.ntot + idx] = (TAux)Rbar[k];
+}
+
+template <typename R, typename Tin, int CS, int ORDER, typename TStage>
+__global__ void __launch_bounds__(kBlockX *kBlockY)
+    rhs_kernel(Grid g, const Tin *__restrict__ in, const TStage *__restrict__ aux, const R *__restrict__ tab,
+               R eta, RKEpilogue<TStage> epi) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  Point<Tin> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  R Rbar[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) Rbar[k] = (R)__ldg(aux + (long long)k * g.ntot + idx);
+  R out[NUM_EVOL_GFS];
+  rhs_point<ORDER, CS, R>(P, rf, inv, Rbar, eta, out);
+#pragma unroll
+  for (int gf = 0; gf < NUM_EVOL_GFS; gf++) epi(gf, idx, out[gf]);
+}
+
+template <typename R> inline const R *table_of(const rfm_struct *rfm) {
+  if (!rfm) return nullptr;
+  if constexpr (sizeof(R) == 8) return (const R *)rfm->table64;
+  else return (const R *)rfm->table32;
+}
+
+template <int CS, int ORDER>
+int ricci_launch_t(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64, int prec,
+                   void *aux) {
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  if (prec == NRGPU_PREC_FP64) {
+    ricci_kernel<double, double, CS, ORDER, double>
+        <<<L.grid, L.block, 0, stream()>>>(g, (const double *)in, table_of<double>(rfm), (double *)aux);
+  } else if (in_is_f64) {
+    ricci_kernel<float, double, CS, ORDER, float>
+        <<<L.grid, L.block, 0, stream()>>>(g, (const double *)in, table_of<float>(rfm), (float *)aux);
+  } else {
+    ricci_kernel<float, float, CS, ORDER, float>
+        <<<L.grid, L.block, 0, stream()>>>(g, (const float *)in, table_of<float>(rfm), (float *)aux);
+  }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+template <int CS, int ORDER>
+int rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  if (a.prec == NRGPU_PREC_FP64) {
+    RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
+    rhs_kernel<double, double, CS, ORDER, double><<<L.grid, L.block, 0, stream()>>>(
+        g, (const double *)a.in, (const double *)a.auxevol, table_of<double>(rfm), p->eta, epi);
+  } else {
+    RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
+    if (a.in_is_f64)
+      rhs_kernel<float, double, CS, ORDER, float><<<L.grid, L.block, 0, stream()>>>(
+          g, (const double *)a.in, (const float *)a.auxevol, table_of<float>(rfm), (float)p->eta, epi);
+    else
+      rhs_kernel<float, float, CS, ORDER, float><<<L.grid, L.block, 0, stream()>>>(
+          g, (const float *)a.in, (const float *)a.auxevol, table_of<float>(rfm), (float)p->eta, epi);
+  }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+#define NRGPU_BSSN_DECLARE(CS, ORDER)                                                                 \
+  extern template int ricci_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const void *, \
+                                                bool, int, void *);                                    \
+  extern template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &);
+#define NRGPU_BSSN_INSTANTIATE(CS, ORDER)                                                         \
+  template int ricci_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const void *, \
+                                         bool, int, void *);                                    \
+  template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &);
+
+}  // namespace bssn
+}  // namespace nrgpu

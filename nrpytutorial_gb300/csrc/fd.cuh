@@ -1,0 +1,120 @@
+// fd.cuh -- finite-difference stencils on IDX4S gridfunctions.
+//
+// Coefficients are those of finite_difference.py:252-369 (Vandermonde
+// inverse, exact rationals), written out for orders 2..8:
+//   centred 1st derivative  f' = invdx * sum_{k=1..R} C1[k] (f[+k] - f[-k])
+//   centred 2nd derivative  f''= invdx^2 (C2[0] f[0] + sum_k C2[k](f[+k]+f[-k]))
+//   mixed 2nd derivative    product of two centred 1st-derivative stencils
+//   upwind 1st derivative   ("dupD", stencil shifted +1) and its mirror
+//                           ("ddnD", shifted -1, weights negated and reversed)
+// Control-vector upwinding (finite_difference_helpers.py:790-820) picks dupD
+// where the control component is > 0 and ddnD otherwise; here one stencil is
+// evaluated with a signed stride instead of blending both.
+#pragma once
+#include "common.cuh"
+
+namespace nrgpu {
+
+template <int ORDER> struct FDCoef;
+
+// Coefficients as constexpr functions of the (unrolled, hence constant)
+// offset, usable from both host and device code.
+#define NRGPU_FD_TABLE(NAME, ...)                                              \
+  __host__ __device__ static constexpr double NAME(int k) {                    \
+    constexpr double t[] = {__VA_ARGS__};                                      \
+    return t[k];                                                               \
+  }
+
+template <> struct FDCoef<2> {
+  static constexpr int R = 1;
+  static constexpr int UPLO = 0;  // dupD offsets 0..2
+  NRGPU_FD_TABLE(c1, 0.0, 1.0 / 2.0)
+  NRGPU_FD_TABLE(c2, -2.0, 1.0)
+  NRGPU_FD_TABLE(up, -3.0 / 2.0, 2.0, -1.0 / 2.0)
+};
+template <> struct FDCoef<4> {
+  static constexpr int R = 2;
+  static constexpr int UPLO = -1;  // dupD offsets -1..3
+  NRGPU_FD_TABLE(c1, 0.0, 2.0 / 3.0, -1.0 / 12.0)
+  NRGPU_FD_TABLE(c2, -5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0)
+  NRGPU_FD_TABLE(up, -1.0 / 4.0, -5.0 / 6.0, 3.0 / 2.0, -1.0 / 2.0, 1.0 / 12.0)
+};
+template <> struct FDCoef<6> {
+  static constexpr int R = 3;
+  static constexpr int UPLO = -2;  // dupD offsets -2..4
+  NRGPU_FD_TABLE(c1, 0.0, 3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0)
+  NRGPU_FD_TABLE(c2, -49.0 / 18.0, 3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0)
+  NRGPU_FD_TABLE(up, 1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0)
+};
+template <> struct FDCoef<8> {
+  static constexpr int R = 4;
+  static constexpr int UPLO = -3;  // dupD offsets -3..5
+  NRGPU_FD_TABLE(c1, 0.0, 4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0)
+  NRGPU_FD_TABLE(c2, -205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0)
+  NRGPU_FD_TABLE(up, -1.0 / 168.0, 1.0 / 14.0, -1.0 / 2.0, -9.0 / 20.0, 5.0 / 4.0, -1.0 / 2.0, 1.0 / 6.0,
+                 -1.0 / 28.0, 1.0 / 280.0)
+};
+#undef NRGPU_FD_TABLE
+
+// Loads go through the read-only path; p points at the stencil centre.
+template <typename T, typename R>
+__device__ __forceinline__ R ld(const T *p, long long off) {
+  return (R)__ldg(p + off);
+}
+
+// Centred first derivative along stride s (unscaled by invdx).
+template <int ORDER, typename R, typename T>
+__device__ __forceinline__ R fd_d1(const T *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  R acc = (R)C::c1(1) * (ld<T, R>(p, s) - ld<T, R>(p, -s));
+#pragma unroll
+  for (int k = 2; k <= C::R; k++) acc += (R)C::c1(k) * (ld<T, R>(p, k * s) - ld<T, R>(p, -k * s));
+  return acc;
+}
+
+// Centred second derivative along stride s (unscaled by invdx^2).
+template <int ORDER, typename R, typename T>
+__device__ __forceinline__ R fd_d2(const T *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  R acc = (R)C::c2(0) * ld<T, R>(p, 0);
+#pragma unroll
+  for (int k = 1; k <= C::R; k++) acc += (R)C::c2(k) * (ld<T, R>(p, k * s) + ld<T, R>(p, -k * s));
+  return acc;
+}
+
+// Mixed second derivative along strides s and t (unscaled).
+template <int ORDER, typename R, typename T>
+__device__ __forceinline__ R fd_d11(const T *__restrict__ p, long long s, long long t) {
+  using C = FDCoef<ORDER>;
+  R acc = (R)0;
+#pragma unroll
+  for (int a = 1; a <= C::R; a++) {
+    R inner = (R)0;
+#pragma unroll
+    for (int b = 1; b <= C::R; b++) {
+      const long long ps = a * s, qt = b * t;
+      inner += (R)C::c1(b) * ((ld<T, R>(p, ps + qt) - ld<T, R>(p, ps - qt)) -
+                              (ld<T, R>(p, -ps + qt) - ld<T, R>(p, -ps - qt)));
+    }
+    acc += (R)C::c1(a) * inner;
+  }
+  return acc;
+}
+
+// Upwinded first derivative (unscaled): dupD if positive, else ddnD.
+// ddnD weights are the negated mirror image of dupD's, so one loop with a
+// signed stride evaluates whichever one the control vector selects.
+template <int ORDER, typename R, typename T>
+__device__ __forceinline__ R fd_dupwind(const T *__restrict__ p, long long s, bool positive) {
+  using C = FDCoef<ORDER>;
+  const long long ss = positive ? s : -s;
+  R acc = (R)0;
+#pragma unroll
+  for (int j = 0; j <= ORDER; j++) {
+    const int k = j + C::UPLO;
+    if (C::up(j) != 0.0) acc += (R)C::up(j) * ld<T, R>(p, k * ss);
+  }
+  return positive ? acc : -acc;
+}
+
+}  // namespace nrgpu

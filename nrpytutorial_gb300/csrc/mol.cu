@@ -1,0 +1,288 @@
+// mol.cu -- RK4 method-of-lines step (MoLtimestepping/RK_MoL.h for "RK4"),
+// fused and unfused, the host-buffer evolve loop, per-system gridfunction
+// tables, and the interior L2-norm reduction used by constraint diagnostics.
+#include <string.h>
+
+#include "epilogue.cuh"
+#include "systems.cuh"
+
+namespace nrgpu {
+
+// ---------------------------------------------------------- system tables
+// Alphabetical gf order (grid.py:226-243); parity types per
+// CurviBoundaryConditions.py:122-213 (0 scalar, 1..3 vector component,
+// 4..9 rank-2 components 00,01,02,11,12,22).
+static const int8_t kParitySW[2] = {0, 0};                           // uu vv
+static const int8_t kParityMaxwell[7] = {1, 2, 3, 1, 2, 3, 0};       // AU0-2 EU0-2 psi
+static const int8_t kParityBSSN[24] = {4, 5, 6, 7, 8, 9,             // aDD00..aDD22
+                                       0,                            // alpha
+                                       1, 2, 3,                      // betU0..2
+                                       0,                            // cf
+                                       4, 5, 6, 7, 8, 9,             // hDD00..hDD22
+                                       1, 2, 3,                      // lambdaU0..2
+                                       0,                            // trK
+                                       1, 2, 3};                     // vetU0..2
+
+int system_num_gfs(int system) {
+  switch (system) {
+    case NRGPU_SYS_SCALARWAVE: return 2;
+    case NRGPU_SYS_MAXWELL: return 7;
+    case NRGPU_SYS_BSSN: return 24;
+  }
+  return -1;
+}
+const int8_t *system_parity(int system) {
+  switch (system) {
+    case NRGPU_SYS_SCALARWAVE: return kParitySW;
+    case NRGPU_SYS_MAXWELL: return kParityMaxwell;
+    case NRGPU_SYS_BSSN: return kParityBSSN;
+  }
+  return nullptr;
+}
+
+template <typename T>
+int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity, T *gfs);
+
+// ------------------------------------------------------- unfused update
+// LOOP_ALL_GFS_GPS RK update over all points of all gfs, reading the RHS the
+// RHS kernel stored in `k` (C_Code_Generation.py:159 and :277-329).
+template <typename TStage>
+__global__ void rk4_update_kernel(int stage, double dt, long long n, double *__restrict__ y_n,
+                                  double *__restrict__ rt, TStage *__restrict__ k) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double kdt = __dmul_rn((double)k[i], dt);
+    switch (stage) {
+      case 0:
+        rt[i] = __dmul_rn(kdt, 1.0 / 6.0);
+        k[i] = (TStage)__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0));
+        break;
+      case 1:
+        rt[i] = __dadd_rn(rt[i], __dmul_rn(kdt, 1.0 / 3.0));
+        k[i] = (TStage)__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0));
+        break;
+      case 2:
+        rt[i] = __dadd_rn(rt[i], __dmul_rn(kdt, 1.0 / 3.0));
+        k[i] = (TStage)__dadd_rn(y_n[i], kdt);
+        break;
+      default:
+        y_n[i] = __dadd_rn(__dadd_rn(y_n[i], rt[i]), __dmul_rn(kdt, 1.0 / 6.0));
+        break;
+    }
+  }
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
+  switch (system) {
+    case NRGPU_SYS_SCALARWAVE: return scalarwave_launch(rfm, p, a);
+    case NRGPU_SYS_MAXWELL: return maxwell_launch(p, a);
+    case NRGPU_SYS_BSSN: {
+      int st = bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
+      if (st) return st;
+      return bssn_rhs_launch(rfm, p, a);
+    }
+  }
+  set_error("unknown system %d", system);
+  return NRGPU_ERR_ARG;
+}
+
+// Boundary conditions, then (BSSN) the det(gammabar) rescale, on `gfs`.
+static int post_rhs(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc, void *gfs,
+                    bool is_f64) {
+  const int ngf = system_num_gfs(system);
+  int st = is_f64 ? apply_bcs_impl<double>(p, bc, ngf, system_parity(system), (double *)gfs)
+                  : apply_bcs_impl<float>(p, bc, ngf, system_parity(system), (float *)gfs);
+  if (st) return st;
+  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64);
+  return NRGPU_OK;
+}
+
+static int check_step_args(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
+                           const MoL_gridfunctions *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(system_num_gfs(system) > 0, "unknown system %d", system);
+  NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL bcstruct or gridfunctions");
+  NRGPU_REQUIRE(gfs->precision == NRGPU_PREC_FP64 || gfs->precision == NRGPU_PREC_MIXED,
+                "unknown precision %d", gfs->precision);
+  NRGPU_REQUIRE(gfs->y_n_gfs && gfs->y_nplus1_running_total_gfs && gfs->k_odd_gfs && gfs->k_even_gfs,
+                "MoL gridfunction buffer is NULL");
+  NRGPU_REQUIRE(system != NRGPU_SYS_BSSN || gfs->auxevol_gfs, "BSSN needs auxevol_gfs");
+  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || rfm != nullptr,
+                "curvilinear grids need an rfm_struct");
+  return NRGPU_OK;
+}
+
+}  // namespace nrgpu
+
+using namespace nrgpu;
+
+extern "C" {
+
+int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
+                             MoL_gridfunctions *gfs, double dt) {
+  int st = check_step_args(system, rfm, p, bc, gfs);
+  if (st) return st;
+  const bool mixed = gfs->precision == NRGPU_PREC_MIXED;
+  void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  for (int s = 0; s < 4; s++) {
+    StageArgs a{};
+    a.stage = s;
+    a.dt = dt;
+    a.prec = gfs->precision;
+    a.in = (s == 0) ? (const void *)gfs->y_n_gfs : (const void *)kbuf[(s + 1) % 2];
+    a.in_is_f64 = (s == 0) || !mixed;
+    a.y_n = gfs->y_n_gfs;
+    a.rt = gfs->y_nplus1_running_total_gfs;
+    a.out = (s == 3) ? nullptr : kbuf[s % 2];
+    a.auxevol = gfs->auxevol_gfs;
+    if ((st = rhs_stage(system, rfm, p, a))) return st;
+    void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
+    const bool post_f64 = (s == 3) || !mixed;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64))) return st;
+  }
+  return NRGPU_OK;
+}
+
+int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *p,
+                                     const bc_struct *bc, MoL_gridfunctions *gfs, double dt) {
+  int st = check_step_args(system, rfm, p, bc, gfs);
+  if (st) return st;
+  const bool mixed = gfs->precision == NRGPU_PREC_MIXED;
+  void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  const long long n = (long long)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 *
+                      p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 16);
+  for (int s = 0; s < 4; s++) {
+    StageArgs a{};
+    a.stage = -1;
+    a.dt = dt;
+    a.prec = gfs->precision;
+    a.in = (s == 0) ? (const void *)gfs->y_n_gfs : (const void *)kbuf[(s + 1) % 2];
+    a.in_is_f64 = (s == 0) || !mixed;
+    a.out = kbuf[s % 2];  // RHS_output: k_odd, k_even, k_odd, k_even
+    a.auxevol = gfs->auxevol_gfs;
+    if ((st = rhs_stage(system, rfm, p, a))) return st;
+    if (mixed)
+      rk4_update_kernel<float><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+                                                                 gfs->y_nplus1_running_total_gfs,
+                                                                 (float *)kbuf[s % 2]);
+    else
+      rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+                                                                  gfs->y_nplus1_running_total_gfs,
+                                                                  (double *)kbuf[s % 2]);
+    NRGPU_LAUNCH_CHECK();
+    void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
+    const bool post_f64 = (s == 3) || !mixed;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64))) return st;
+  }
+  return NRGPU_OK;
+}
+
+int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
+                    MoL_gridfunctions *gfs, double dt, int n_steps, double *y_host) {
+  int st = check_step_args(system, rfm, p, bc, gfs);
+  if (st) return st;
+  NRGPU_REQUIRE(y_host != nullptr && n_steps >= 0, "bad host buffer or step count");
+  const size_t bytes = sizeof(double) * (size_t)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 *
+                       p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  NRGPU_CUDA_CHECK(cudaMemcpyAsync(gfs->y_n_gfs, y_host, bytes, cudaMemcpyHostToDevice, stream()));
+  for (int n = 0; n < n_steps; n++)
+    if ((st = MoL_step_forward_in_time(system, rfm, p, bc, gfs, dt))) return st;
+  NRGPU_CUDA_CHECK(cudaMemcpyAsync(y_host, gfs->y_n_gfs, bytes, cudaMemcpyDeviceToHost, stream()));
+  NRGPU_CUDA_CHECK(cudaStreamSynchronize(stream()));
+  return NRGPU_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ L2 norms
+namespace nrgpu {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Pass 1: each block sums f^2 over a grid-stride share of the interior
+// points and writes one partial to scratch[blockIdx.x].
+__global__ void l2_partial_kernel(Grid g, const double *__restrict__ f, double *__restrict__ partial) {
+  const int nx = g.n0 - 2 * g.ng, ny = g.n1 - 2 * g.ng, nz = g.n2 - 2 * g.ng;
+  const long long n = (long long)nx * ny * nz;
+  double acc = 0.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i0 = (int)(t % nx) + g.ng;
+    const int i1 = (int)((t / nx) % ny) + g.ng;
+    const int i2 = (int)(t / ((long long)nx * ny)) + g.ng;
+    const double v = f[i0 + (long long)g.n0 * (i1 + (long long)g.n1 * i2)];
+    acc += v * v;
+  }
+  __shared__ double sh[32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  }
+}
+
+// Pass 2: one block adds the partials in a fixed order (deterministic).
+__global__ void l2_final_kernel(const double *__restrict__ partial, int nparts, double count,
+                                double *__restrict__ result) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partial[i];
+  __shared__ double sh[32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) {
+      result[0] = v;
+      result[1] = count;
+    }
+  }
+}
+
+int l2_norm_sq_impl(const paramstruct *p, const double *gfs, int gf, double *scratch, int scratch_len,
+                    double *result) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(gfs && scratch && result, "NULL argument");
+  NRGPU_REQUIRE(gf >= 0, "negative gridfunction index");
+  NRGPU_REQUIRE(scratch_len >= 1, "scratch_len must be >= 1");
+  Grid g = make_grid(p);
+  const long long n = (long long)p->Nxx0 * p->Nxx1 * p->Nxx2;
+  const int threads = 256;
+  int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 4);
+  blocks = std::max(1, std::min(blocks, scratch_len));
+  l2_partial_kernel<<<blocks, threads, 0, stream()>>>(g, gfs + (long long)gf * g.ntot, scratch);
+  NRGPU_LAUNCH_CHECK();
+  l2_final_kernel<<<1, 256, 0, stream()>>>(scratch, blocks, (double)n, result);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+}  // namespace nrgpu
+
+extern "C" int nrgpu_l2_norm_sq(const paramstruct *p, const double *gfs, int gf, double *scratch,
+                                int scratch_len, double *result) {
+  return nrgpu::l2_norm_sq_impl(p, gfs, gf, scratch, scratch_len, result);
+}

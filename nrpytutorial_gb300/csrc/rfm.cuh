@@ -1,0 +1,260 @@
+// rfm.cuh -- reference metric ("hatted" quantities) for orthogonal,
+// diagonal coordinate systems: Cartesian, Spherical, SinhSpherical.
+//
+// reference_metric.py:487-601 derives, from the orthogonal scale factors
+// s_i(xx) (ghat_ii = s_i^2, ReU_i = 1/s_i, ReDD_ij = s_i s_j), the first and
+// second derivatives of ReU, ReDD and ghat, the Christoffel symbols
+// GammahatUDD and their derivatives, and det(ghat) with derivatives.  Here
+// the same quantities are evaluated numerically in FP64 from closed-form
+// s_i, ds_i, d2s_i, once per (i0,i1) column of the grid (none depends on
+// xx2 for these systems), and stored as dense tables -- the analogue of the
+// rfm_precompute arrays of reference_metric.py:603-886.
+//
+// Which entries can be non-zero follows from which coordinates each s_i
+// depends on (the `dep` matrix).  Kernels test those masks with constexpr
+// functions of the (unrolled, hence constant) tensor indices, so structural
+// zeros cost no arithmetic and no loads; on Cartesian grids every hatted
+// quantity is a literal 0 or 1.
+#pragma once
+#include "common.cuh"
+
+namespace nrgpu {
+
+// ------------------------------------------------------ table slot layout
+namespace rq {
+constexpr int ReU = 0;          // [3]
+constexpr int ReUdD = 3;        // [3][3]      d_j ReU_i
+constexpr int ReUdDD = 12;      // [3][3][3]   d_j d_k ReU_i
+constexpr int ReDD = 39;        // [3][3]
+constexpr int ReDDdD = 48;      // [3][3][3]
+constexpr int ReDDdDD = 75;     // [3][3][3][3]
+constexpr int ghatDD = 156;     // [3][3]
+constexpr int ghatUU = 165;     // [3][3]
+constexpr int ghatDDdD = 174;   // [3][3][3]
+constexpr int ghatDDdDD = 201;  // [3][3][3][3]
+constexpr int GammahatUDD = 282;    // [3][3][3]
+constexpr int GammahatUDDdD = 309;  // [3][3][3][3]  d_l Gammahat^i_jk
+constexpr int detgammahat = 390;    // [1]
+constexpr int detgammahatdD = 391;  // [3]
+constexpr int detgammahatdDD = 394; // [3][3]
+constexpr int NQ = 403;
+}  // namespace rq
+
+// ------------------------------------------------------- dependency masks
+// dep(CS, i, k): does scale factor s_i depend on xx_k?
+__host__ __device__ constexpr bool dep(int cs, int i, int k) {
+  return cs == NRGPU_COORD_CARTESIAN ? false
+         // Spherical family: s0 = dr/dxx0, s1 = r(xx0), s2 = r(xx0) sin(xx1)
+         : (k == 0) ? true : (k == 1 ? i == 2 : false);
+}
+
+template <int CS> struct RfmMask {
+  static constexpr bool trivial = (CS == NRGPU_COORD_CARTESIAN);
+  static constexpr bool ReUdD(int i, int j) { return dep(CS, i, j); }
+  static constexpr bool ReUdDD(int i, int j, int k) { return dep(CS, i, j) && dep(CS, i, k); }
+  static constexpr bool ReDDdD(int i, int j, int k) { return dep(CS, i, k) || dep(CS, j, k); }
+  static constexpr bool ReDDdDD(int i, int j, int k, int l) {
+    return (dep(CS, i, k) && dep(CS, i, l)) || (dep(CS, j, k) && dep(CS, j, l)) ||
+           (dep(CS, i, k) && dep(CS, j, l)) || (dep(CS, i, l) && dep(CS, j, k));
+  }
+  static constexpr bool ghatDDdD(int i, int j, int k) { return i == j && dep(CS, i, k); }
+  static constexpr bool ghatDDdDD(int i, int j, int k, int l) {
+    return i == j && dep(CS, i, k) && dep(CS, i, l);
+  }
+  // Gammahat^i_kl = (1/2) ghat^ii (d_l ghat_ik + d_k ghat_il - d_i ghat_kl)
+  static constexpr bool Gammahat(int i, int k, int l) {
+    return (i == k && dep(CS, i, l)) || (i == l && dep(CS, i, k)) || (k == l && dep(CS, k, i));
+  }
+  static constexpr bool GammahatdD(int i, int k, int l, int n) {
+    return Gammahat(i, k, l) && (dep(CS, i, n) || (k == l && dep(CS, k, n)) ||
+                                 (i == k && dep(CS, i, n)) || (i == l && dep(CS, i, n)));
+  }
+  static constexpr bool detgdD(int k) { return dep(CS, 0, k) || dep(CS, 1, k) || dep(CS, 2, k); }
+  static constexpr bool detgdDD(int k, int l) {
+    return (dep(CS, 0, k) || dep(CS, 1, k) || dep(CS, 2, k)) &&
+           (dep(CS, 0, l) || dep(CS, 1, l) || dep(CS, 2, l));
+  }
+};
+
+// ------------------------------------------------------- point accessor
+// Reads hatted quantities at one (i0,i1) column.  R is the arithmetic type
+// of the caller; tables are FP64 (tab64) with an FP32 copy (tab32).
+template <int CS, typename R> struct Rfm {
+  using M = RfmMask<CS>;
+  const R *__restrict__ base;  // table + i1*N0 + i0
+  long long plane;             // N0*N1
+
+  __device__ __forceinline__ R q(int slot) const { return __ldg(base + slot * plane); }
+
+  __device__ __forceinline__ R ReU(int i) const { return M::trivial ? (R)1 : q(rq::ReU + i); }
+  __device__ __forceinline__ R ReUdD(int i, int j) const { return q(rq::ReUdD + 3 * i + j); }
+  __device__ __forceinline__ R ReUdDD(int i, int j, int k) const {
+    return q(rq::ReUdDD + 9 * i + 3 * j + k);
+  }
+  __device__ __forceinline__ R ReDD(int i, int j) const {
+    return M::trivial ? (R)1 : q(rq::ReDD + 3 * i + j);
+  }
+  __device__ __forceinline__ R ReDDdD(int i, int j, int k) const {
+    return q(rq::ReDDdD + 9 * i + 3 * j + k);
+  }
+  __device__ __forceinline__ R ReDDdDD(int i, int j, int k, int l) const {
+    return q(rq::ReDDdDD + 27 * i + 9 * j + 3 * k + l);
+  }
+  // ghatDD/ghatUU are only read where i == j.
+  __device__ __forceinline__ R ghatDD(int i) const {
+    return M::trivial ? (R)1 : q(rq::ghatDD + 4 * i);
+  }
+  __device__ __forceinline__ R ghatUU(int i) const {
+    return M::trivial ? (R)1 : q(rq::ghatUU + 4 * i);
+  }
+  __device__ __forceinline__ R ghatDDdD(int i, int j, int k) const {
+    return q(rq::ghatDDdD + 9 * i + 3 * j + k);
+  }
+  __device__ __forceinline__ R G(int i, int k, int l) const {
+    return q(rq::GammahatUDD + 9 * i + 3 * k + l);
+  }
+  __device__ __forceinline__ R GdD(int i, int k, int l, int n) const {
+    return q(rq::GammahatUDDdD + 27 * i + 9 * k + 3 * l + n);
+  }
+  __device__ __forceinline__ R detg() const { return M::trivial ? (R)1 : q(rq::detgammahat); }
+  __device__ __forceinline__ R detgdD(int k) const { return q(rq::detgammahatdD + k); }
+  __device__ __forceinline__ R detgdDD(int k, int l) const { return q(rq::detgammahatdDD + 3 * k + l); }
+};
+
+template <int CS, typename R>
+__device__ __forceinline__ Rfm<CS, R> rfm_at(const R *tab, int n0, int n1, int i0, int i1) {
+  Rfm<CS, R> r;
+  r.base = tab ? tab + (long long)i1 * n0 + i0 : nullptr;
+  r.plane = (long long)n0 * n1;
+  return r;
+}
+
+// --------------------------------------------------- scale-factor closed forms
+// s[i], ds[i][k] = d s_i / d xx_k, dds[i][k][l], at uniform coordinates
+// (xx0, xx1).  Spherical: r = xx0; SinhSpherical: r = AMPL sinh(xx0/SINHW) /
+// sinh(1/SINHW), written with exponentials as reference_metric.py:125-126 does.
+struct ScaleFactors {
+  double s[3], ds[3][3], dds[3][3][3];
+};
+
+__host__ __device__ inline void radial_map(int cs, double AMPL, double SINHW, double x,
+                                           double *r, double *r1, double *r2, double *r3) {
+  if (cs == NRGPU_COORD_SINHSPHERICAL) {
+    const double ep = exp(x / SINHW), em = exp(-x / SINHW);
+    const double den = exp(1.0 / SINHW) - exp(-1.0 / SINHW);
+    *r = AMPL * (ep - em) / den;
+    *r1 = AMPL * (ep + em) / (SINHW * den);
+    *r2 = *r / (SINHW * SINHW);
+    *r3 = *r1 / (SINHW * SINHW);
+  } else {
+    *r = x;
+    *r1 = 1.0;
+    *r2 = 0.0;
+    *r3 = 0.0;
+  }
+}
+
+__host__ __device__ inline void scale_factors(int cs, double AMPL, double SINHW, double xx0,
+                                              double xx1, ScaleFactors *S) {
+  for (int i = 0; i < 3; i++) {
+    S->s[i] = 1.0;
+    for (int k = 0; k < 3; k++) {
+      S->ds[i][k] = 0.0;
+      for (int l = 0; l < 3; l++) S->dds[i][k][l] = 0.0;
+    }
+  }
+  if (cs == NRGPU_COORD_CARTESIAN) return;
+  double r, r1, r2, r3;
+  radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
+  const double sn = sin(xx1), cs1 = cos(xx1);
+  S->s[0] = r1;
+  S->s[1] = r;
+  S->s[2] = r * sn;
+  S->ds[0][0] = r2;
+  S->ds[1][0] = r1;
+  S->ds[2][0] = r1 * sn;
+  S->ds[2][1] = r * cs1;
+  S->dds[0][0][0] = r3;
+  S->dds[1][0][0] = r2;
+  S->dds[2][0][0] = r2 * sn;
+  S->dds[2][0][1] = S->dds[2][1][0] = r1 * cs1;
+  S->dds[2][1][1] = -r * sn;
+}
+
+// Fills all rq::NQ derived quantities from scale factors (dense, FP64).
+__host__ __device__ inline void hatted_quantities(const ScaleFactors &S, double *out /*[rq::NQ]*/) {
+  const double *s = S.s;
+  for (int q = 0; q < rq::NQ; q++) out[q] = 0.0;
+  double g[3], dg[3][3], ddg[3][3][3];
+  for (int i = 0; i < 3; i++) {
+    g[i] = s[i] * s[i];
+    for (int k = 0; k < 3; k++) {
+      dg[i][k] = 2.0 * s[i] * S.ds[i][k];
+      for (int l = 0; l < 3; l++)
+        ddg[i][k][l] = 2.0 * (S.ds[i][k] * S.ds[i][l] + s[i] * S.dds[i][k][l]);
+    }
+  }
+  for (int i = 0; i < 3; i++) {
+    out[rq::ReU + i] = 1.0 / s[i];
+    out[rq::ghatDD + 4 * i] = g[i];
+    out[rq::ghatUU + 4 * i] = 1.0 / g[i];
+    for (int j = 0; j < 3; j++) {
+      out[rq::ReUdD + 3 * i + j] = -S.ds[i][j] / (s[i] * s[i]);
+      for (int k = 0; k < 3; k++)
+        out[rq::ReUdDD + 9 * i + 3 * j + k] =
+            -S.dds[i][j][k] / (s[i] * s[i]) + 2.0 * S.ds[i][j] * S.ds[i][k] / (s[i] * s[i] * s[i]);
+      out[rq::ReDD + 3 * i + j] = s[i] * s[j];
+      for (int k = 0; k < 3; k++) {
+        out[rq::ReDDdD + 9 * i + 3 * j + k] = S.ds[i][k] * s[j] + s[i] * S.ds[j][k];
+        for (int l = 0; l < 3; l++)
+          out[rq::ReDDdDD + 27 * i + 9 * j + 3 * k + l] =
+              S.dds[i][k][l] * s[j] + S.ds[i][k] * S.ds[j][l] + S.ds[i][l] * S.ds[j][k] +
+              s[i] * S.dds[j][k][l];
+      }
+    }
+    for (int k = 0; k < 3; k++) {
+      out[rq::ghatDDdD + 9 * i + 3 * i + k] = dg[i][k];
+      for (int l = 0; l < 3; l++) out[rq::ghatDDdDD + 27 * i + 9 * i + 3 * k + l] = ddg[i][k][l];
+    }
+  }
+  // Christoffel symbols of the diagonal metric and their derivatives:
+  // Gamma^i_kl = (1/2) ghat^ii (d_l g_ik + d_k g_il - d_i g_kl)
+  auto dgDD = [&](int a, int b, int k) { return a == b ? dg[a][k] : 0.0; };
+  auto ddgDD = [&](int a, int b, int k, int l) { return a == b ? ddg[a][k][l] : 0.0; };
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++)
+      for (int l = 0; l < 3; l++) {
+        const double bracket = dgDD(i, k, l) + dgDD(i, l, k) - dgDD(k, l, i);
+        out[rq::GammahatUDD + 9 * i + 3 * k + l] = 0.5 / g[i] * bracket;
+        for (int n = 0; n < 3; n++) {
+          const double dbracket = ddgDD(i, k, l, n) + ddgDD(i, l, k, n) - ddgDD(k, l, i, n);
+          const double dginv = -dg[i][n] / (g[i] * g[i]);
+          out[rq::GammahatUDDdD + 27 * i + 9 * k + 3 * l + n] =
+              0.5 * dginv * bracket + 0.5 / g[i] * dbracket;
+        }
+      }
+  // det(ghat) = g0 g1 g2 and derivatives.
+  out[rq::detgammahat] = g[0] * g[1] * g[2];
+  for (int k = 0; k < 3; k++) {
+    out[rq::detgammahatdD + k] = dg[0][k] * g[1] * g[2] + g[0] * dg[1][k] * g[2] + g[0] * g[1] * dg[2][k];
+    for (int l = 0; l < 3; l++)
+      out[rq::detgammahatdDD + 3 * k + l] =
+          ddg[0][k][l] * g[1] * g[2] + g[0] * ddg[1][k][l] * g[2] + g[0] * g[1] * ddg[2][k][l] +
+          dg[0][k] * dg[1][l] * g[2] + dg[0][l] * dg[1][k] * g[2] + dg[0][k] * g[1] * dg[2][l] +
+          dg[0][l] * g[1] * dg[2][k] + g[0] * dg[1][k] * dg[2][l] + g[0] * dg[1][l] * dg[2][k];
+  }
+}
+
+// Cell-centred uniform coordinate of index j (reference_metric.py:1001-1006).
+// Evaluated without FMA contraction, so device and host agree bit for bit
+// with the reference's `xxmin + ((REAL)(j-NGHOSTS) + (1.0/2.0))*dxx`.
+__host__ __device__ inline double xx_of(double xxmin, double dxx, int j, int ng) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(xxmin, __dmul_rn((double)(j - ng) + 0.5, dxx));
+#else
+  volatile double t = ((double)(j - ng) + 0.5) * dxx;
+  return xxmin + t;
+#endif
+}
+
+}  // namespace nrgpu

@@ -1,0 +1,73 @@
+"""Grids and gridfunction registries for the GB300 MoL evolution library.
+
+Mirrors the reference's driver set-up: paramstruct filled by
+set_Nxx_dxx_invdx_params__and__xx (reference_metric.py:1330-1395), cell-
+centred coordinate arrays xx[3], IDX4S layout (gf outermost, i0 fastest)
+and alphabetically sorted evolved gridfunctions (grid.py:226-243).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+# Evolved gridfunctions in memory order, with curvilinear parity types
+# (CurviBoundaryConditions.py:122-213).
+SYSTEM_GFS = {
+    "ScalarWave": (["uu", "vv"], [0, 0]),
+    "Maxwell": (["AU0", "AU1", "AU2", "EU0", "EU1", "EU2", "psi"], [1, 2, 3, 1, 2, 3, 0]),
+    "BSSN": (["aDD00", "aDD01", "aDD02", "aDD11", "aDD12", "aDD22", "alpha",
+              "betU0", "betU1", "betU2", "cf",
+              "hDD00", "hDD01", "hDD02", "hDD11", "hDD12", "hDD22",
+              "lambdaU0", "lambdaU1", "lambdaU2", "trK", "vetU0", "vetU1", "vetU2"],
+             [4, 5, 6, 7, 8, 9, 0, 1, 2, 3, 0, 4, 5, 6, 7, 8, 9, 1, 2, 3, 0, 1, 2, 3]),
+}
+AUXEVOL_GFS = {"BSSN": ["RbarDD00", "RbarDD01", "RbarDD02", "RbarDD11", "RbarDD12", "RbarDD22"]}
+
+
+def default_nghosts(system, fd_order):
+    """ScalarWave drivers use FD_order/2 ghosts; the upwinded BSSN and the
+    Maxwell drivers use FD_order/2 + 1 (Tutorial-Start_to_Finish-ScalarWave.ipynb,
+    ...BSSNCurvilinear-Two_BHs_Collide.ipynb:835)."""
+    return fd_order // 2 if system == "ScalarWave" else fd_order // 2 + 1
+
+
+class Grid:
+    """Numerical grid: paramstruct + cell-centred xx arrays (host, FP64)."""
+
+    def __init__(self, CoordSystem, Nxx, FD_order=4, NGHOSTS=2, *, AMPL=10.0, SINHW=0.2,
+                 RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0):
+        lib = _lib.load()
+        p = _lib.paramstruct()
+        p.CoordSystem = _lib.COORD[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
+        p.FD_order = FD_order
+        p.NGHOSTS = NGHOSTS
+        p.AMPL, p.SINHW, p.RMAX = AMPL, SINHW, RMAX
+        lo, hi = domain
+        p.xmin = p.ymin = p.zmin = lo
+        p.xmax = p.ymax = p.zmax = hi
+        p.eta, p.wavespeed, p.time = eta, wavespeed, 0.0
+        n = [int(v) for v in Nxx]
+        np_ = [v + 2 * NGHOSTS for v in n]
+        self.xx = [np.zeros(np_[d]) for d in range(3)]
+        arr = (C.POINTER(C.c_double) * 3)(*[x.ctypes.data_as(C.POINTER(C.c_double)) for x in self.xx])
+        _lib.check(lib.set_Nxx_dxx_invdx_params__and__xx(EigenCoord, (C.c_int * 3)(*n), C.byref(p), arr),
+                   "set_Nxx_dxx_invdx_params__and__xx")
+        self.params = p
+        self.CoordSystem = CoordSystem
+        self.Nxx = tuple(n)
+        self.NGHOSTS = NGHOSTS
+        self.FD_order = FD_order
+        self.shape = (np_[2], np_[1], np_[0])  # (i2, i1, i0) numpy order
+        self.ntot = np_[0] * np_[1] * np_[2]
+
+    @property
+    def interior(self):
+        g = self.NGHOSTS
+        return (slice(g, -g), slice(g, -g), slice(g, -g))
+
+    def n_interior(self):
+        return self.Nxx[0] * self.Nxx[1] * self.Nxx[2]
+
+    def find_timestep(self, CFL_FACTOR):
+        return float(_lib.load().find_timestep(C.byref(self.params), CFL_FACTOR))

@@ -1,0 +1,189 @@
+"""Method-of-lines evolutions on the GPU through the libnrgpu C ABI.
+
+`Evolution` owns the RK4 buffers of RK_Allocate_Memory.h (y_n, running total,
+k_odd, k_even; MoLtimestepping/C_Code_Generation.py:97-103) as torch CUDA
+tensors, the reference-metric tables and the boundary-condition map, and
+calls the library's entry points on the current torch stream.  PyTorch only
+provides device memory and streams here; every numerical operation is a
+libnrgpu kernel.
+"""
+import ctypes as C
+
+import torch
+
+from . import _lib
+from .grid import AUXEVOL_GFS, SYSTEM_GFS, Grid
+
+
+class Evolution:
+    def __init__(self, system, grid: Grid, precision="fp64", device="cuda"):
+        self.lib = _lib.load()
+        if system not in SYSTEM_GFS:
+            raise ValueError("unknown system %r" % system)
+        if precision not in _lib.PREC:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.system = system
+        self.sys_id = _lib.SYSTEM[system]
+        self.grid = grid
+        self.precision = precision
+        self.device = torch.device(device)
+        names, parity = SYSTEM_GFS[system]
+        self.gf_names = names
+        self.parity = (C.c_int8 * len(parity))(*parity)
+        self.ngf = len(names)
+        shape = (self.ngf,) + grid.shape
+        stage = torch.float64 if precision == "fp64" else torch.float32
+        z = dict(device=self.device)
+        self.y_n = torch.zeros(shape, dtype=torch.float64, **z)
+        self.rt = torch.zeros(shape, dtype=torch.float64, **z)
+        self.k_odd = torch.zeros(shape, dtype=stage, **z)
+        self.k_even = torch.zeros(shape, dtype=stage, **z)
+        naux = len(AUXEVOL_GFS.get(system, []))
+        self.auxevol = torch.zeros((max(naux, 1),) + grid.shape, dtype=stage, **z)
+        self.gfs = _lib.MoL_gridfunctions(_lib.PREC[precision], self.y_n.data_ptr(), self.rt.data_ptr(),
+                                          self.k_odd.data_ptr(), self.k_even.data_ptr(),
+                                          self.auxevol.data_ptr())
+        self._sync_stream()
+        self.rfm = _lib.rfm_struct()
+        self._rfm_ok = False
+        if grid.params.CoordSystem != 0:
+            _lib.check(self.lib.rfm_struct__malloc(C.byref(grid.params), C.byref(self.rfm)), "rfm_struct__malloc")
+            _lib.check(self.lib.rfm_struct__define(C.byref(grid.params), C.byref(self.rfm)), "rfm_struct__define")
+            self._rfm_ok = True
+        self.bc = _lib.bc_struct()
+        _lib.check(self.lib.driver_bcstruct(C.byref(grid.params), C.byref(self.bc)), "driver_bcstruct")
+        self.time = 0.0
+
+    # -- plumbing
+    def _sync_stream(self):
+        _lib.set_stream(torch.cuda.current_stream(self.device))
+
+    def _rfm(self):
+        return C.byref(self.rfm) if self._rfm_ok else None
+
+    def close(self):
+        if getattr(self, "_rfm_ok", False):
+            self.lib.rfm_struct__freemem(C.byref(self.rfm))
+            self._rfm_ok = False
+        if hasattr(self, "bc"):
+            self.lib.bcstruct_freemem(C.byref(self.bc))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the hot path
+    def step(self, dt, fused=True):
+        """One RK4 step (MoLtimestepping/RK_MoL.h)."""
+        self._sync_stream()
+        f = self.lib.MoL_step_forward_in_time if fused else self.lib.MoL_step_forward_in_time_unfused
+        _lib.check(f(self.sys_id, self._rfm(), C.byref(self.grid.params), C.byref(self.bc),
+                     C.byref(self.gfs), float(dt)), "MoL_step_forward_in_time")
+        self.time += dt
+
+    def evolve_host(self, y_host, dt, n_steps):
+        """Host-buffer evolution: y_host (numpy float64, IDX4S) in, state out."""
+        self._sync_stream()
+        _lib.check(self.lib.MoL_evolve_host(self.sys_id, self._rfm(), C.byref(self.grid.params),
+                                            C.byref(self.bc), C.byref(self.gfs), float(dt), int(n_steps),
+                                            y_host.ctypes.data_as(C.POINTER(C.c_double))),
+                   "MoL_evolve_host")
+
+    def rhs_eval(self, in_gfs, rhs_gfs, auxevol=None):
+        """The system's rhs_eval (plain store at interior points)."""
+        self._sync_stream()
+        p = C.byref(self.grid.params)
+        f32 = in_gfs.dtype == torch.float32
+        sfx = "_f32" if f32 else ""
+        if self.system == "ScalarWave":
+            if self.grid.params.CoordSystem == 0:
+                st = getattr(self.lib, "ScalarWave_rhs_eval" + sfx)(p, _lib.ptr(in_gfs), _lib.ptr(rhs_gfs))
+            else:
+                st = getattr(self.lib, "ScalarWaveCurvilinear_rhs_eval" + sfx)(
+                    self._rfm(), p, _lib.ptr(in_gfs), _lib.ptr(rhs_gfs))
+        elif self.system == "Maxwell":
+            st = getattr(self.lib, "Maxwell_rhs_eval" + sfx)(p, _lib.ptr(in_gfs), _lib.ptr(rhs_gfs))
+        else:
+            aux = self.auxevol if auxevol is None else auxevol
+            _lib.check(getattr(self.lib, "BSSN_Ricci_eval" + sfx)(self._rfm(), p, _lib.ptr(in_gfs), _lib.ptr(aux)),
+                       "BSSN_Ricci_eval")
+            st = getattr(self.lib, "BSSN_rhs_eval" + sfx)(self._rfm(), p, _lib.ptr(aux), _lib.ptr(in_gfs),
+                                                          _lib.ptr(rhs_gfs))
+        _lib.check(st, "rhs_eval")
+
+    def ricci_eval(self, in_gfs, auxevol):
+        self._sync_stream()
+        sfx = "_f32" if in_gfs.dtype == torch.float32 else ""
+        _lib.check(getattr(self.lib, "BSSN_Ricci_eval" + sfx)(self._rfm(), C.byref(self.grid.params),
+                                                              _lib.ptr(in_gfs), _lib.ptr(auxevol)),
+                   "BSSN_Ricci_eval")
+
+    def apply_bcs(self, gfs):
+        self._sync_stream()
+        f = self.lib.apply_bcs_curvilinear_f32 if gfs.dtype == torch.float32 else self.lib.apply_bcs_curvilinear
+        _lib.check(f(C.byref(self.grid.params), C.byref(self.bc), gfs.shape[0],
+                     C.cast(self.parity, C.POINTER(C.c_int8)), _lib.ptr(gfs)), "apply_bcs_curvilinear")
+
+    def enforce_detgammabar(self, gfs):
+        self._sync_stream()
+        f = (self.lib.BSSN_enforce_detgammabar_constraint_f32 if gfs.dtype == torch.float32
+             else self.lib.BSSN_enforce_detgammabar_constraint)
+        _lib.check(f(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs)), "enforce_detgammabar_constraint")
+
+    def hamiltonian(self, gfs=None):
+        """Hamiltonian constraint at interior points (FP64)."""
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        H = torch.zeros((1,) + self.grid.shape, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.BSSN_Hamiltonian_constraint(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs),
+                                                        _lib.ptr(H)), "BSSN_Hamiltonian_constraint")
+        return H
+
+    def maxwell_constraint(self, gfs=None):
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        Cc = torch.zeros((1,) + self.grid.shape, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.Maxwell_Constraints(C.byref(self.grid.params), _lib.ptr(gfs), _lib.ptr(Cc)),
+                   "Maxwell_Constraints")
+        return Cc
+
+    def l2_norm(self, gfs, gf=0):
+        """RMS over interior points of gridfunction `gf` of an FP64 array."""
+        self._sync_stream()
+        nblk = 1024
+        scratch = torch.empty(nblk, dtype=torch.float64, device=self.device)
+        res = torch.empty(2, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.nrgpu_l2_norm_sq(C.byref(self.grid.params), _lib.ptr(gfs), gf, _lib.ptr(scratch),
+                                             nblk, _lib.ptr(res)), "nrgpu_l2_norm_sq")
+        s, n = res.tolist()
+        return (s / n) ** 0.5
+
+    def initial_data_brill_lindquist(self, m1, pos1, m2, pos2, gfs=None):
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        _lib.check(self.lib.BSSN_initial_data_BrillLindquist(
+            C.byref(self.grid.params), float(m1), (C.c_double * 3)(*pos1), float(m2), (C.c_double * 3)(*pos2),
+            _lib.ptr(gfs)), "BSSN_initial_data_BrillLindquist")
+
+    def rfm_table(self):
+        import numpy as np
+        host = np.zeros((self.rfm.nquant, self.rfm.N1, self.rfm.N0))
+        _lib.check(self.lib.rfm_struct__download(C.byref(self.rfm), host.ctypes.data_as(C.POINTER(C.c_double))),
+                   "rfm_struct__download")
+        return host
+
+    def bc_map(self):
+        import numpy as np
+        b = self.bc
+        arrs = [np.zeros(max(b.total_outer, 1), dtype=np.int32) for _ in range(2)] + \
+               [np.zeros(max(b.total_inner, 1), dtype=np.int32) for _ in range(3)]
+        _lib.check(self.lib.bcstruct_download(C.byref(b), *[a.ctypes.data_as(C.POINTER(C.c_int)) for a in arrs]),
+                   "bcstruct_download")
+        return dict(outer_dest=arrs[0][:b.total_outer], outer_step=arrs[1][:b.total_outer],
+                    inner_dest=arrs[2][:b.total_inner], inner_src=arrs[3][:b.total_inner],
+                    inner_parity=arrs[4][:b.total_inner],
+                    num_ob=list(b.num_ob_gz_pts)[:b.NGHOSTS], num_ib=list(b.num_ib_gz_pts)[:b.NGHOSTS],
+                    ob_dir_start=[list(b.ob_dir_start[g]) for g in range(b.NGHOSTS)],
+                    ib_start=list(b.ib_start)[:b.NGHOSTS])

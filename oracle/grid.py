@@ -1,0 +1,150 @@
+"""Grid set-up and reference metric for the CPU oracle (numpy, FP64).
+
+TEST INFRASTRUCTURE (see oracle/__init__.py).
+
+- `GridParams` restates reference_metric.py:1330-1395
+  (set_Nxx_dxx_invdx_params__and__xx): domain per CoordSystem
+  (Spherical :106-108, SinhSpherical :118-120, Cartesian :400-403),
+  dxx = (xxmax - xxmin)/Nxx, cell-centred xx[j] = xxmin + (j - NGHOSTS + 1/2) dxx.
+- `hatted` restates reference_metric.py:487-601: for orthogonal scale factors
+  s_i (reference_metric.py:168-175: s0 = dr/dxx0, s1 = r, s2 = r sin(xx1);
+  Cartesian s_i = 1) it returns ReU, ReDD, ghat and their first and second
+  derivatives, GammahatUDD and its derivatives, det(ghat) and derivatives.
+  Where the reference differentiates symbolically, here the derivatives of
+  s_i are written in closed form and propagated by the product/quotient
+  rules, all as numpy arrays.
+- `find_timestep` restates reference_metric.py:1412-1439.
+"""
+import numpy as np
+
+CART, SPH, SINHSPH = 0, 1, 2
+NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH}
+
+
+class GridParams:
+    def __init__(self, CoordSystem, Nxx, NGHOSTS, FD_order=4, AMPL=10.0, SINHW=0.2, RMAX=10.0,
+                 domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0):
+        cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
+        self.CoordSystem = cs
+        self.FD_order = FD_order
+        self.NGHOSTS = NGHOSTS
+        self.AMPL, self.SINHW, self.RMAX = AMPL, SINHW, RMAX
+        self.eta, self.wavespeed = eta, wavespeed
+        self.Nxx = [int(n) for n in Nxx]
+        self.np = [n + 2 * NGHOSTS for n in self.Nxx]
+        ecs = SPH if (EigenCoord and cs == SINHSPH) else cs
+        if ecs == CART:
+            lo, hi = domain
+            self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
+        else:
+            self.xxmin = [0.0, 0.0, -np.pi]
+            self.xxmax = [RMAX if ecs == SPH else 1.0, np.pi, np.pi]
+        self.dxx = [(self.xxmax[d] - self.xxmin[d]) / float(self.Nxx[d]) for d in range(3)]
+        self.invdx = [1.0 / v for v in self.dxx]
+        self.xx = [self.xxmin[d] + ((np.arange(self.np[d]) - NGHOSTS) + 0.5) * self.dxx[d] for d in range(3)]
+
+    @property
+    def shape(self):
+        return (self.np[2], self.np[1], self.np[0])
+
+    def interior(self, f):
+        g = self.NGHOSTS
+        return f[..., g:-g, g:-g, g:-g]
+
+
+def scale_factors(gp, xx0, xx1):
+    """s[i], ds[i][k], dds[i][k][l] as arrays broadcast over (xx1, xx0)."""
+    x0, x1 = np.meshgrid(xx0, xx1)  # shape (n1, n0)
+    z = np.zeros_like(x0)
+    one = np.ones_like(x0)
+    s = [one.copy(), one.copy(), one.copy()]
+    ds = [[z.copy() for _ in range(3)] for _ in range(3)]
+    dds = [[[z.copy() for _ in range(3)] for _ in range(3)] for _ in range(3)]
+    if gp.CoordSystem == CART:
+        return s, ds, dds
+    if gp.CoordSystem == SINHSPH:
+        A, w = gp.AMPL, gp.SINHW
+        den = np.exp(1.0 / w) - np.exp(-1.0 / w)
+        r = A * (np.exp(x0 / w) - np.exp(-x0 / w)) / den
+        r1 = A * (np.exp(x0 / w) + np.exp(-x0 / w)) / (w * den)
+        r2 = r / w ** 2
+        r3 = r1 / w ** 2
+    else:
+        r, r1, r2, r3 = x0, one, z, z
+    st, ct = np.sin(x1), np.cos(x1)
+    s = [r1, r, r * st]
+    ds[0][0] = r2
+    ds[1][0] = r1
+    ds[2][0] = r1 * st
+    ds[2][1] = r * ct
+    dds[0][0][0] = r3
+    dds[1][0][0] = r2
+    dds[2][0][0] = r2 * st
+    dds[2][0][1] = dds[2][1][0] = r1 * ct
+    dds[2][1][1] = -r * st
+    return s, ds, dds
+
+
+def hatted(gp):
+    """Hatted quantities on the (n1, n0) plane; tensors indexed first."""
+    s, ds, dds = scale_factors(gp, gp.xx[0], gp.xx[1])
+    s = np.array(s)
+    ds = np.array(ds)
+    dds = np.array(dds)
+    shp = s.shape[1:]
+    q = {}
+    q["ReU"] = 1.0 / s
+    q["ReUdD"] = -ds / s[:, None] ** 2
+    q["ReUdDD"] = -dds / s[:, None, None] ** 2 + 2.0 * ds[:, :, None] * ds[:, None, :] / s[:, None, None] ** 3
+    q["ReDD"] = s[:, None] * s[None, :]
+    q["ReDDdD"] = ds[:, None, :] * s[None, :, None] + s[:, None, None] * ds[None, :, :]
+    q["ReDDdDD"] = (dds[:, None] * s[None, :, None, None] + ds[:, None, :, None] * ds[None, :, None, :]
+                    + ds[:, None, None, :] * ds[None, :, :, None] + s[:, None, None, None] * dds[None, :])
+    g = s ** 2
+    dg = 2.0 * s[:, None] * ds
+    ddg = 2.0 * (ds[:, :, None] * ds[:, None, :] + s[:, None, None] * dds)
+    eye = np.eye(3)
+    q["ghatDD"] = eye[:, :, None, None] * g[:, None]
+    q["ghatUU"] = eye[:, :, None, None] / g[:, None]
+    ghatDDdD = np.zeros((3, 3, 3) + shp)
+    ghatDDdDD = np.zeros((3, 3, 3, 3) + shp)
+    for i in range(3):
+        ghatDDdD[i, i] = dg[i]
+        ghatDDdDD[i, i] = ddg[i]
+    q["ghatDDdD"] = ghatDDdD
+    q["ghatDDdDD"] = ghatDDdDD
+    # Christoffels of the diagonal metric: (1/2) g^ii (g_ik,l + g_il,k - g_kl,i)
+    G = np.zeros((3, 3, 3) + shp)
+    GdD = np.zeros((3, 3, 3, 3) + shp)
+    for i in range(3):
+        for k in range(3):
+            for l in range(3):
+                br = ghatDDdD[i, k, l] + ghatDDdD[i, l, k] - ghatDDdD[k, l, i]
+                G[i, k, l] = 0.5 * br / g[i]
+                for n in range(3):
+                    dbr = ghatDDdDD[i, k, l, n] + ghatDDdDD[i, l, k, n] - ghatDDdDD[k, l, i, n]
+                    GdD[i, k, l, n] = 0.5 * dbr / g[i] - 0.5 * br * dg[i, n] / g[i] ** 2
+    q["GammahatUDD"] = G
+    q["GammahatUDDdD"] = GdD
+    det = g[0] * g[1] * g[2]
+    q["detgammahat"] = det
+    ddet = np.zeros((3,) + shp)
+    dddet = np.zeros((3, 3) + shp)
+    for k in range(3):
+        ddet[k] = dg[0, k] * g[1] * g[2] + g[0] * dg[1, k] * g[2] + g[0] * g[1] * dg[2, k]
+        for l in range(3):
+            dddet[k, l] = (ddg[0, k, l] * g[1] * g[2] + g[0] * ddg[1, k, l] * g[2] + g[0] * g[1] * ddg[2, k, l]
+                           + dg[0, k] * dg[1, l] * g[2] + dg[0, l] * dg[1, k] * g[2]
+                           + dg[0, k] * g[1] * dg[2, l] + dg[0, l] * g[1] * dg[2, k]
+                           + g[0] * dg[1, k] * dg[2, l] + g[0] * dg[1, l] * dg[2, k])
+    q["detgammahatdD"] = ddet
+    q["detgammahatdDD"] = dddet
+    return q
+
+
+def find_timestep(gp, CFL_FACTOR):
+    """CFL * min over interior points of dxx_i * s_i / wavespeed."""
+    g = gp.NGHOSTS
+    s, _, _ = scale_factors(gp, gp.xx[0][g:-g], gp.xx[1][g:-g])
+    dsmin = min(float(np.min(gp.dxx[d] * s[d])) for d in range(3))
+    return dsmin * CFL_FACTOR / gp.wavespeed

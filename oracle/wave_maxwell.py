@@ -1,0 +1,96 @@
+"""ScalarWave and vacuum-Maxwell RHSs, initial data and exact solutions (numpy).
+
+TEST INFRASTRUCTURE (see oracle/__init__.py).
+
+  ScalarWave/ScalarWave_RHSs.py:46-71              uu_rhs = vv, vv_rhs = c^2 sum_i uu_dDii
+  ScalarWave/ScalarWaveCurvilinear_RHSs.py:43-98    vv_rhs = c^2 (ghat^ij uu_dDij - ghat^ij Gammahat^k_ij uu_dDk)
+  Maxwell/VacuumMaxwell_Flat_Evol_Cartesian.py:49-74  System I RHSs and C = d_i E^i
+  Maxwell/InitialData.py:26-117                      toroidal dipole A, E = -d_t A, psi = 0
+"""
+import numpy as np
+
+from .fd import Stencils
+from .grid import CART, hatted
+
+
+def scalarwave_rhs_grid(gp, gfs):
+    S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+    uu, vv = gfs[0], gfs[1]
+    out = np.zeros((2,) + gp.shape)
+    c2 = gp.wavespeed ** 2
+    if gp.CoordSystem == CART:
+        lap = S.d2(uu, 0) + S.d2(uu, 1) + S.d2(uu, 2)
+        rhs_v = c2 * lap
+    else:
+        g = gp.NGHOSTS
+        q = {k: a[..., None, g:-g, g:-g] for k, a in hatted(gp).items()}
+        gUU, G = q["ghatUU"], q["GammahatUDD"]
+        contracted = np.einsum("ij...,kij...->k...", gUU, G)
+        acc = 0.0
+        for i in range(3):
+            acc = acc - contracted[i] * S.d1(uu, i)
+            for j in range(3):
+                if i == j:
+                    acc = acc + gUU[i, j] * S.d2(uu, i)
+        rhs_v = acc * c2
+    gp.interior(out[0])[...] = S.interior(vv)
+    gp.interior(out[1])[...] = rhs_v
+    return out
+
+
+def plane_wave(gp, t, kvec=(2 * np.pi / 20,) * 3, c=1.0):
+    """Plane wave u = sin(k.x - |k| c t), v = d_t u at every point (Cartesian)."""
+    x = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")  # (i2, i1, i0)
+    z, y, xx = x
+    k = np.asarray(kvec, dtype=float)
+    kn = np.sqrt((k ** 2).sum())
+    ph = k[0] * xx + k[1] * y + k[2] * z - kn * c * t
+    return np.array([np.sin(ph), -kn * c * np.cos(ph)])
+
+
+def maxwell_rhs_grid(gp, gfs):
+    S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+    A, E, psi = gfs[0:3], gfs[3:6], gfs[6]
+    out = np.zeros((7,) + gp.shape)
+    for i in range(3):
+        gp.interior(out[i])[...] = -S.interior(E[i]) - S.d1(psi, i)
+    for i in range(3):
+        acc = 0.0
+        for j in range(3):
+            if j == i:
+                continue  # -A^i_{,jj} + A^j_{,ji} cancels symbolically for j == i
+            acc = acc - S.d2(A[i], j) + S.d11(A[j], j, i)
+        gp.interior(out[3 + i])[...] = acc
+    gp.interior(out[6])[...] = -(S.d1(A[0], 0) + S.d1(A[1], 1) + S.d1(A[2], 2))
+    return out
+
+
+def maxwell_constraint_grid(gp, gfs):
+    S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+    out = np.zeros(gp.shape)
+    gp.interior(out)[...] = S.d1(gfs[3], 0) + S.d1(gfs[4], 1) + S.d1(gfs[5], 2)
+    return out
+
+
+def toroidal_dipole(gp, t, amp=1.0, lam=1.0):
+    """Exact toroidal-dipole solution (Maxwell/InitialData.py:41-104) at all
+    points of a Cartesian grid: A^i, E^i = -d_t A^i, psi = 0.
+
+    The reference sets A_phi = A_phi-hat / (r sin_theta) with its
+    sin_theta = z/r and A_phi-hat = amp sin_theta [(e^{-lam v^2} -
+    e^{-lam u^2})/r^2 - 2 lam (v e^{-lam v^2} + u e^{-lam u^2})/r],
+    u = t + r, v = t - r, then maps A^i_Cart = (dx^i/dphi) A_phi with
+    dx/dphi = (-y, x, 0).  The z/r factors cancel, leaving
+    A = F(r,t) (-y, x, 0) with F = amp/r [ ... ].
+    """
+    z, y, x = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
+    r = np.sqrt(x * x + y * y + z * z)
+    u, v = t + r, t - r
+    eu, ev = np.exp(-lam * u ** 2), np.exp(-lam * v ** 2)
+    deu, dev = -2 * lam * u * eu, -2 * lam * v * ev
+    F = amp / r * ((ev - eu) / r ** 2 - 2 * lam * (v * ev + u * eu) / r)
+    dF = amp / r * ((dev - deu) / r ** 2 - 2 * lam * (ev + v * dev + eu + u * deu) / r)
+    out = np.zeros((7,) + gp.shape)
+    out[0], out[1] = -y * F, x * F
+    out[3], out[4] = y * dF, -x * dF
+    return out

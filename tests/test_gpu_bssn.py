@@ -1,0 +1,131 @@
+"""BSSN on the GPU vs the CPU oracle: reference-metric tables, Ricci,
+rhs_eval, det(gammabar) rescale, Hamiltonian constraint, and the RK4 step,
+in FP64 (1e-12 normwise relative) and FP32 (mixed-precision bound)."""
+import numpy as np
+import pytest
+
+import oracle.bcs as ob
+import oracle.bssn as obs
+import oracle.grid as og
+from tests.helpers import bssn_random_state, grids, per_gf_rel
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 5e-5
+
+CASES = [("Cartesian", (8, 8, 8), 4), ("Cartesian", (8, 6, 10), 6),
+         ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4)]
+KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
+
+
+def _setup(cuda, coord, Nxx, order, prec="fp64"):
+    from nrpytutorial_gb300 import Evolution
+    G, gp = grids("BSSN", coord, Nxx, order, **KW)
+    return Evolution("BSSN", G, precision=prec, device=cuda), gp
+
+
+@pytest.mark.parametrize("coord", ["SinhSpherical", "Spherical"])
+def test_rfm_tables_match_oracle(cuda, coord):
+    ev, gp = _setup(cuda, coord, (10, 8, 6), 4)
+    tab = ev.rfm_table()
+    q = og.hatted(gp)
+    slots = [("ReU", 0), ("ReUdD", 3), ("ReUdDD", 12), ("ReDD", 39), ("ReDDdD", 48), ("ReDDdDD", 75),
+             ("ghatDD", 156), ("ghatUU", 165), ("ghatDDdD", 174), ("ghatDDdDD", 201), ("GammahatUDD", 282),
+             ("GammahatUDDdD", 309), ("detgammahat", 390), ("detgammahatdD", 391), ("detgammahatdDD", 394)]
+    for name, off in slots:
+        a = q[name]
+        n = int(np.prod(a.shape[:-2]))
+        got = tab[off:off + n].reshape(a.shape)
+        scale = np.abs(a).max() + 1e-300
+        assert np.abs(got - a).max() / scale < 1e-13, name
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_ricci_matches_oracle(cuda, coord, Nxx, order):
+    import torch
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    f = bssn_random_state(gp.shape, seed=order)
+    t = torch.tensor(f, device=cuda)
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+    ev.ricci_eval(t, aux)
+    ref = obs.ricci_grid(gp, f)
+    assert per_gf_rel(aux.cpu().numpy(), ref, gp.NGHOSTS) < FP64_TOL
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_rhs_matches_oracle(cuda, coord, Nxx, order):
+    import torch
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    f = bssn_random_state(gp.shape, seed=100 + order)
+    t = torch.tensor(f, device=cuda)
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+    out = torch.zeros_like(t)
+    ev.rhs_eval(t, out, auxevol=aux)  # Ricci then rhs (LeaveRicciSymbolic form)
+    ref = obs.rhs_grid(gp, f, RbarDD6=aux.cpu().numpy())
+    assert per_gf_rel(out.cpu().numpy(), ref, gp.NGHOSTS) < FP64_TOL
+    # and with the oracle's own Ricci
+    ref2 = obs.rhs_grid(gp, f)
+    assert per_gf_rel(out.cpu().numpy(), ref2, gp.NGHOSTS) < FP64_TOL
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES[:3])
+def test_fp32_rhs_close_to_fp64(cuda, coord, Nxx, order):
+    import torch
+    ev, gp = _setup(cuda, coord, Nxx, order, prec="mixed")
+    f = bssn_random_state(gp.shape, seed=7, amp=0.05).astype(np.float32)
+    t = torch.tensor(f, device=cuda)
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float32, device=cuda)
+    out = torch.zeros_like(t)
+    ev.rhs_eval(t, out, auxevol=aux)
+    ref = obs.rhs_grid(gp, f.astype(np.float64))
+    assert per_gf_rel(out.double().cpu().numpy(), ref, gp.NGHOSTS) < FP32_TOL
+
+
+@pytest.mark.parametrize("coord", ["Cartesian", "SinhSpherical"])
+def test_enforce_detgammabar_matches_oracle(cuda, coord):
+    import torch
+    ev, gp = _setup(cuda, coord, (8, 8, 6), 4)
+    f = bssn_random_state(gp.shape, seed=3)
+    t = torch.tensor(f, device=cuda)
+    ev.enforce_detgammabar(t)
+    ref = obs.enforce_detgammabar(gp, f)
+    assert per_gf_rel(t.cpu().numpy(), ref) < 1e-14
+    # FP32 storage, FP64 arithmetic
+    t32 = torch.tensor(f.astype(np.float32), device=cuda)
+    ev.enforce_detgammabar(t32)
+    ref32 = obs.enforce_detgammabar(gp, f.astype(np.float32).astype(np.float64))
+    assert per_gf_rel(t32.double().cpu().numpy(), ref32) < 1e-7
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES[:3])
+def test_hamiltonian_matches_oracle(cuda, coord, Nxx, order):
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    import torch
+    f = bssn_random_state(gp.shape, seed=9)
+    H = ev.hamiltonian(torch.tensor(f, device=cuda)).cpu().numpy()[0]
+    ref = obs.hamiltonian_grid(gp, f)
+    g = gp.NGHOSTS
+    assert per_gf_rel(H[None, g:-g, g:-g, g:-g], ref[None, g:-g, g:-g, g:-g]) < FP64_TOL
+
+
+@pytest.mark.parametrize("coord,Nxx,order", [CASES[0], CASES[2]])
+@pytest.mark.parametrize("fused", [True, False])
+def test_rk4_step_matches_oracle(cuda, coord, Nxx, order, fused):
+    import torch
+    from nrpytutorial_gb300 import SYSTEM_GFS
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    parity = SYSTEM_GFS["BSSN"][1]
+    layers = ob.build_bcstruct(gp)
+
+    def post(x):
+        ob.apply_bcs(layers, x, parity)
+        x[...] = obs.enforce_detgammabar(gp, x)
+
+    y = bssn_random_state(gp.shape, seed=21, amp=0.02)
+    post(y)
+    ev.y_n.copy_(torch.tensor(y, device=cuda))
+    dt = 0.05 * min(gp.dxx)
+    ev.step(dt, fused=fused)
+    yo, _, _ = ob.rk4_step(y, dt, lambda u: obs.rhs_grid(gp, u), post, gp.NGHOSTS)
+    assert per_gf_rel(ev.y_n.cpu().numpy(), yo) < 1e-12
