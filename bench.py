@@ -1,0 +1,444 @@
+#!/usr/bin/env python
+"""Benchmark: BSSN gridpoint-RHS/s of the RK4 method-of-lines step.
+
+Workload (the reference's BSSN curvilinear configuration): SinhSpherical
+reference metric (AMPL=64, SINHW=0.2), Nr x Ntheta x Nphi = 128 x 64 x 16
+interior points + 3 ghost zones, 4th-order FD, RK4, Brill-Lindquist data
+(m = 0.5, 0.5 at z = +-0.5), 1+log lapse, covariant Gamma-driver (eta = 2),
+CFL 0.5.  One step = one RK4 step = 4 RHS evaluations per interior point
+(the reference's gp/s definition, Nxx0*Nxx1*Nxx2*4 per step,
+Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:1165-1166).
+
+  python bench.py [--gpus N --steps K --warmup W]      GB300 arm (FP64 headline)
+  python bench.py --impl reference ...                 the reference's own
+      generated C (OpenMP, host cores) on the same workload
+
+Prints one JSON line (rank 0).  For N > 1 (torchrun) every rank evolves an
+independent replica ("replicas only": one evolution does not shard here).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = dict(name="BSSN SinhSpherical 128x64x16 FD4 RK4 Brill-Lindquist", coord="SinhSpherical",
+         Nxx=(128, 64, 16), fd=4, ng=3, AMPL=64.0, SINHW=0.2, eta=2.0, CFL=0.5,
+         m1=0.5, pos1=(0.0, 0.0, 0.5), m2=0.5, pos2=(0.0, 0.0, -0.5))
+METRIC = "BSSN gridpoint-RHS/s (RK4 step, FP64)"
+UNIT = "gridpoint-RHS/s"
+# Algorithmic bytes per interior point of one BSSN rhs_eval launch (FP64):
+# 24 evolved gfs + 6 RbarDD read once, 24 RHS written once.
+RHS_BYTES_F64 = (24 + 6 + 24) * 8
+RICCI_BYTES_F64 = (9 + 6) * 8
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.index)],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, smax, reasons, pw = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            c = [x.strip() for x in ln.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax.append(float(c[2]))
+                pw.append(float(c[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_median": float(np.median(pw)) if pw else None}
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# --------------------------------------------------------------- GB300 arm
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from nrpytutorial_gb300 import Evolution, Grid, _lib
+    lib = _lib.load()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    G = Grid(W["coord"], W["Nxx"], FD_order=W["fd"], NGHOSTS=W["ng"], AMPL=W["AMPL"], SINHW=W["SINHW"],
+             eta=W["eta"])
+    nint = G.n_interior()
+    dt = G.find_timestep(W["CFL"])
+    ev = Evolution("BSSN", G, precision="fp64", device=dev)
+    ev.initial_data_brill_lindquist(W["m1"], W["pos1"], W["m2"], W["pos2"])
+    ev.apply_bcs(ev.y_n)
+    ev.enforce_detgammabar(ev.y_n)
+    y0 = ev.y_n.clone()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    K, Wm = args.steps, args.warmup
+    sampler = ClockSampler(local)
+    sampler.start()
+
+    def timed_steps(e, n):
+        ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        for k in range(n):
+            flush.zero_()                    # evict L2 between timed steps (untimed)
+            ev_s[k].record()
+            e.step(dt)
+            ev_e[k].record()
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in zip(ev_s, ev_e)) / 1e3
+
+    # ---- FP64 headline
+    for _ in range(Wm):
+        ev.step(dt)
+    ev.y_n.copy_(y0)
+    barrier()
+    l0 = lib.nrgpu_kernel_launch_count()
+    t64 = timed_steps(ev, K)
+    launches = lib.nrgpu_kernel_launch_count() - l0
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t64], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t64 = float(tt.item())
+    y64 = ev.y_n.clone()
+    finite = bool(torch.isfinite(y64).all().item())
+    value = world * K * nint * 4 / t64
+
+    # ---- mixed precision (FP32 stage buffers and RHS, FP64 y_n/running total)
+    ev32 = Evolution("BSSN", G, precision="mixed", device=dev)
+    for _ in range(Wm):
+        ev32.y_n.copy_(y0)
+        ev32.step(dt)
+    ev32.y_n.copy_(y0)
+    torch.cuda.synchronize()
+    t32 = timed_steps(ev32, K)
+    g = W["ng"]
+    a = ev32.y_n[:, g:-g, g:-g, g:-g].double()
+    b = y64[:, g:-g, g:-g, g:-g]
+    rel_l2 = [float(torch.linalg.vector_norm(a[i] - b[i]) / torch.linalg.vector_norm(b[i]).clamp_min(1e-300))
+              for i in range(24)]
+    rel_max = [float((a[i] - b[i]).abs().max() / b[i].abs().max().clamp_min(1e-300)) for i in range(24)]
+    # Hamiltonian-constraint norms of both runs (FP64 diagnostics)
+    H64 = ev.l2_norm(ev.hamiltonian(y64))
+    H32 = ev.l2_norm(ev.hamiltonian(ev32.y_n))
+
+    # ---- dominant kernels alone: rhs_eval and Ricci_eval (plain stores)
+    aux = torch.zeros((6,) + G.shape, dtype=torch.float64, device=dev)
+    rhs = torch.zeros_like(y0)
+    R = 20
+    times = {"rhs": [], "ricci": []}
+    for r in range(R + 3):
+        flush.zero_()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        ev.ricci_eval(y0, aux)
+        e1.record()
+        flush.zero_()
+        e3 = torch.cuda.Event(enable_timing=True)
+        e3.record()
+        _rhs_only(ev, y0, aux, rhs)
+        e2.record()
+        torch.cuda.synchronize()
+        if r >= 3:
+            times["ricci"].append(e0.elapsed_time(e1) / 1e3)
+            times["rhs"].append(e3.elapsed_time(e2) / 1e3)
+    t_rhs = float(np.mean(times["rhs"]))
+    t_ric = float(np.mean(times["ricci"]))
+    # FP32 rhs kernel alone
+    y32 = y0.float()
+    aux32 = torch.zeros((6,) + G.shape, dtype=torch.float32, device=dev)
+    rhs32 = torch.zeros_like(y32)
+    ev32.ricci_eval(y32, aux32)
+    t32k = []
+    for r in range(R + 3):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _rhs_only(ev32, y32, aux32, rhs32)
+        e1.record()
+        torch.cuda.synchronize()
+        if r >= 3:
+            t32k.append(e0.elapsed_time(e1) / 1e3)
+    t_rhs32 = float(np.mean(t32k))
+
+    # ---- end to end through the C ABI with host buffers (H2D + step + D2H per step)
+    host = torch.empty(y0.shape, dtype=torch.float64, pin_memory=True)
+    host.copy_(y0.cpu())
+    hn = host.numpy()
+    ev.evolve_host(hn, dt, 1)  # warm
+    host.copy_(y0.cpu())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        ev.evolve_host(hn, dt, 1)
+    te2e = time.perf_counter() - t0
+    clocks = sampler.stop()
+
+    hbm, src = peaks()
+    achieved = nint * RHS_BYTES_F64 / t_rhs / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
+        "ms_per_step": t64 / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic: Brill-Lindquist initial data computed on the GPU",
+        "config": {"workload": W["name"], "Nxx": list(W["Nxx"]), "NGHOSTS": W["ng"], "FD_order": W["fd"],
+                   "AMPL": W["AMPL"], "SINHW": W["SINHW"], "eta": W["eta"], "CFL": W["CFL"], "dt": dt,
+                   "interior_points": nint, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed (256 MB write) before every timed step"},
+        "gpu_launches": int(launches),
+        "state_finite": finite,
+        "e2e": {"value": world * K * nint * 4 / te2e, "unit": UNIT,
+                "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
+                "path": "MoL_evolve_host (C ABI), pinned host state, 1 step per call"},
+        "roofline": {"bound": "hbm", "kernel": "bssn rhs_kernel FP64 (plain rhs_eval)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": None,
+                     "bytes_per_point": RHS_BYTES_F64, "launch_ms": t_rhs * 1e3,
+                     "note": "FP64 BSSN is FP64-ALU bound on GB300; the HBM fraction is reported as asked"},
+        "kernels_ms": {"rhs_f64": t_rhs * 1e3, "ricci_f64": t_ric * 1e3, "rhs_f32": t_rhs32 * 1e3,
+                       "ricci_f64_GBps": nint * RICCI_BYTES_F64 / t_ric / 1e9,
+                       "rhs_f32_GBps": nint * RHS_BYTES_F64 / 2 / t_rhs32 / 1e9},
+        "mixed": {"value": world * K * nint * 4 / t32, "unit": UNIT, "ms_per_step": t32 / K * 1e3,
+                  "speedup_vs_fp64": t64 / t32,
+                  "rel_l2_vs_fp64_max_over_gfs": max(rel_l2), "rel_max_vs_fp64_max_over_gfs": max(rel_max),
+                  "after_steps": K, "H_l2_fp64": H64, "H_l2_mixed": H32},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def _rhs_only(ev, y, aux, out):
+    """rhs_eval with a precomputed RbarDD (the reference's LeaveRicciSymbolic form)."""
+    import ctypes as C
+    from nrpytutorial_gb300 import _lib
+    ev._sync_stream()
+    f = ev.lib.BSSN_rhs_eval_f32 if y.dtype.itemsize == 4 else ev.lib.BSSN_rhs_eval
+    _lib.check(f(ev._rfm(), C.byref(ev.grid.params), _lib.ptr(aux), _lib.ptr(y), _lib.ptr(out)), "BSSN_rhs_eval")
+
+
+# ------------------------------------------------------------ CPU reference
+class RefStepper:
+    """The reference's generated Ricci_eval/rhs_eval/enforce (OpenMP -Ofast
+    build) plus our C restatement of its RK update and BCs."""
+
+    def __init__(self, flavour="fast"):
+        import ctypes as C
+        import oracle.bcs as ob
+        import oracle.grid as og
+        from oracle import ref_build
+        from oracle.ref import RefKernels, available
+        ref_build.build_if_present()
+        self.gp = gp = og.GridParams(W["coord"], W["Nxx"], W["ng"], W["fd"], AMPL=W["AMPL"], SINHW=W["SINHW"],
+                                     eta=W["eta"])
+        cfg = "bssn_sinhsph_fd4"
+        if not available(cfg, flavour):
+            raise FileNotFoundError("reference-generated kernels for %s not built" % cfg)
+        self.kind = "reference"
+        extra = {"BH1_mass": W["m1"], "BH1_posn_x": W["pos1"][0], "BH1_posn_y": W["pos1"][1],
+                 "BH1_posn_z": W["pos1"][2], "BH2_mass": W["m2"], "BH2_posn_x": W["pos2"][0],
+                 "BH2_posn_y": W["pos2"][1], "BH2_posn_z": W["pos2"][2]}
+        self.R = RefKernels(cfg, gp, flavour, extra=extra)
+        self.mol = C.CDLL(ref_build.MOL_LIB)
+        layers = ob.build_bcstruct(gp)
+        ob_start, od, os_, ib_start, idd, isrc, ipar = [0], [], [], [0], [], [], []
+        for outer, (d, s, p) in layers:
+            for arr in outer:
+                od += list(arr[:, 0]); os_ += list(arr[:, 1])
+            ob_start.append(len(od))
+            idd += list(d); isrc += list(s)
+            ipar += [int(sum((1 << t) for t in range(10) if row[t] < 0)) for row in p]
+            ib_start.append(len(idd))
+        i32 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.int32))
+        self.bc = [i32(ob_start), i32(od), i32(os_), i32(ib_start), i32(idd), i32(isrc), i32(ipar)]
+        from nrpytutorial_gb300.grid import SYSTEM_GFS
+        self.par = np.array(SYSTEM_GFS["BSSN"][1], dtype=np.int8)
+        self.ntot = int(np.prod(gp.shape))
+        shape = (24,) + gp.shape
+        self.y = self.R.initial_data(shape)
+        self.post(self.y)
+        self.rt = np.zeros(shape)
+        self.k = [np.zeros(shape), np.zeros(shape)]
+        self.aux = np.zeros((6,) + gp.shape)
+        self.dt = og.find_timestep(gp, W["CFL"])
+
+    def post(self, g):
+        import ctypes as C
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in self.bc]
+        self.mol.ref_apply_bcs(C.c_int(self.gp.NGHOSTS), ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5],
+                               ptrs[6], C.c_int(24), self.par.ctypes.data_as(C.POINTER(C.c_int8)),
+                               C.c_longlong(self.ntot), g.ctypes.data_as(C.POINTER(C.c_double)))
+        self.R.lib.ref_enforce_detgammabar_constraint(*self.R._x(), g.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def step(self):
+        import ctypes as C
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        n = C.c_longlong(24 * self.ntot)
+        ins = [self.y, self.k[0], self.k[1], self.k[0]]
+        outs = [self.k[0], self.k[1], self.k[0], self.k[1]]
+        for s in range(4):
+            self.R.lib.ref_Ricci_eval(*self.R._x(), dp(ins[s]), dp(self.aux))
+            self.R.lib.ref_rhs_eval(*self.R._x(), dp(self.aux), dp(ins[s]), dp(outs[s]))
+            self.mol.ref_rk4_update(C.c_int(s), C.c_double(self.dt), n, dp(self.y), dp(self.rt), dp(outs[s]))
+            self.post(self.y if s == 3 else outs[s])
+
+
+def cpu_baseline(args, steps=2):
+    """The reference-generated C on the host cores, bounded sample."""
+    nint = int(np.prod(W["Nxx"]))
+    try:
+        st = RefStepper()
+        st.step()  # warm
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            st.step()
+        dt = time.perf_counter() - t0
+        return {"value": steps * nint * 4 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                "sample": "%d full RK4 steps of the workload (Ricci_eval+rhs_eval+update+BCs+rescale), "
+                          "reference-generated C, gcc -Ofast -fopenmp, OMP threads=%s" %
+                          (steps, os.environ.get("OMP_NUM_THREADS", "all"))}
+    except Exception as e:  # noqa: BLE001
+        return port_baseline(str(e))
+
+
+def port_baseline(why):
+    """numpy oracle on one z-slab of the workload (bounded sample)."""
+    import oracle.bssn as obs
+    import oracle.grid as og
+    gp = og.GridParams(W["coord"], (W["Nxx"][0], W["Nxx"][1], 2), W["ng"], W["fd"], AMPL=W["AMPL"],
+                       SINHW=W["SINHW"], eta=W["eta"])
+    rng = np.random.default_rng(0)
+    f = 0.01 * rng.random((24,) + gp.shape)
+    f[obs.GF["cf"]] += 1
+    f[obs.GF["alpha"]] += 1
+    t0 = time.perf_counter()
+    obs.rhs_grid(gp, f)
+    dt = time.perf_counter() - t0
+    n = W["Nxx"][0] * W["Nxx"][1] * 2
+    return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "numpy oracle, one RHS evaluation on a 2-plane slab (%s)" % why[:120]}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    nint = int(np.prod(W["Nxx"]))
+    try:
+        st = RefStepper()
+    except Exception as e:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": "reference-generated kernels not built: %s" % e}))
+        return
+    for _ in range(max(0, args.warmup)):
+        st.step()
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st.step()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > args.ref_budget_s:
+            break
+    k = len(times)
+    tt = sum(times)
+    value = k * nint * 4 / tt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": k,
+        "warmup": args.warmup, "ms_per_step": tt / k * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: Brill-Lindquist (reference-generated initial_data)",
+        "config": {"workload": W["name"], "Nxx": list(W["Nxx"]), "NGHOSTS": W["ng"], "FD_order": W["fd"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                         "sample": "%d of %d requested full RK4 steps (time budget %.0f s), reference-generated "
+                                   "Ricci_eval/rhs_eval/enforce (gcc -Ofast -fopenmp) + C RK update/BCs"
+                                   % (k, args.steps, args.ref_budget_s)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--ref-budget-s", type=float, default=90.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -87,7 +87,22 @@ def scale_factors(gp, xx0, xx1):
 
 def hatted(gp):
     """Hatted quantities on the (n1, n0) plane; tensors indexed first."""
-    s, ds, dds = scale_factors(gp, gp.xx[0], gp.xx[1])
+    return hatted_from_scale_factors(*scale_factors(gp, gp.xx[0], gp.xx[1]))
+
+
+class _PointParams:
+    def __init__(self, cs, AMPL, SINHW):
+        self.CoordSystem, self.AMPL, self.SINHW = cs, AMPL, SINHW
+
+
+def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2):
+    """Hatted quantities at one point (xx0, xx1): arrays with point shape (1, 1)."""
+    cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else CoordSystem
+    return hatted_from_scale_factors(*scale_factors(_PointParams(cs, AMPL, SINHW),
+                                                    np.array([xx0]), np.array([xx1])))
+
+
+def hatted_from_scale_factors(s, ds, dds):
     s = np.array(s)
     ds = np.array(ds)
     dds = np.array(dds)

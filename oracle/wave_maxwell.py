@@ -38,6 +38,36 @@ def scalarwave_rhs_grid(gp, gfs):
     return out
 
 
+def scalarwave_pointwise(v, q, c, cartesian):
+    """uu_rhs, vv_rhs from symbol values (uu, vv, uu_dD[3], uu_dDD[3][3])."""
+    if cartesian:
+        return v["vv"], c * c * (v["uu_dDD"][0, 0] + v["uu_dDD"][1, 1] + v["uu_dDD"][2, 2])
+    gUU, G = q["ghatUU"], q["GammahatUDD"]
+    contracted = np.einsum("ij...,kij...->k...", gUU, G)
+    acc = 0.0
+    for i in range(3):
+        acc = acc - contracted[i] * v["uu_dD"][i]
+        for j in range(3):
+            acc = acc + gUU[i, j] * v["uu_dDD"][i, j]
+    return v["vv"], acc * c * c
+
+
+def maxwell_pointwise(v):
+    """System I RHSs and C from symbol values (VacuumMaxwell_Flat_Evol_Cartesian.py:49-74)."""
+    E, AdD, AdDD, psid = v["EU"], v["AU_dD"], v["AU_dDD"], v["psi_dD"]
+    Arhs = [-E[i] - psid[i] for i in range(3)]
+    Erhs = []
+    for i in range(3):
+        acc = 0.0
+        for j in range(3):
+            if j != i:
+                acc = acc - AdDD[i, j, j] + AdDD[j, j, i]
+        Erhs.append(acc)
+    psi_rhs = -(AdD[0, 0] + AdD[1, 1] + AdD[2, 2])
+    C = v["EU_dD"][0, 0] + v["EU_dD"][1, 1] + v["EU_dD"][2, 2]
+    return Arhs, Erhs, psi_rhs, C
+
+
 def plane_wave(gp, t, kvec=(2 * np.pi / 20,) * 3, c=1.0):
     """Plane wave u = sin(k.x - |k| c t), v = d_t u at every point (Cartesian)."""
     x = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")  # (i2, i1, i0)

@@ -1,0 +1,182 @@
+"""Regenerates the golden fixtures in tests/golden/ from the reference.
+
+Run in a container that has the reference checkout (default /root/reference,
+or $NRPY_REFERENCE) after `python -m oracle.gen_ref` and
+`python -m oracle.ref_build`:
+
+    python tests/golden/make_golden.py
+
+Writes:
+  senr_bc_spherical_4x4x4.npz  the SENR curvilinear-BC golden file
+      CurviBoundaryConditions/SENRout4x4x4-Spherical_NGHOSTS4oFD.txt as an
+      int array [1000 points, 10 gridfunctions] (points in i0-fastest order).
+  ref_<config>.npz  outputs of the reference-generated C (strict FP64 build)
+      on seeded inputs (tests/helpers.py bssn_random_state / numpy
+      default_rng): Ricci, rhs_eval, Hamiltonian at interior points,
+      enforce_detgammabar_constraint (hDD at all points), Brill-Lindquist
+      initial_data (interior points); rhs_eval for ScalarWave / Maxwell.
+  trusted_values.json  the reference's trusted-value unit tests for the
+      hot-path expressions: md5-seeded symbol values (exactly as
+      UnitTesting/cse_simplify_and_evaluate_sympy_expressions.py:53-67
+      assigns them) and the 30-digit expected values from
+      */tests/trusted_values_dict.py.
+"""
+import hashlib
+import json
+import os
+import random
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REF = os.environ.get("NRPY_REFERENCE", "/root/reference")
+
+KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
+BL = dict(BH1_mass=0.5, BH1_posn_x=0.0, BH1_posn_y=0.0, BH1_posn_z=0.5,
+          BH2_mass=0.5, BH2_posn_x=0.0, BH2_posn_y=0.0, BH2_posn_z=-0.5)
+FIXTURE_GRIDS = {
+    "bssn_cart_fd4": ("Cartesian", (6, 6, 6), 4, 3, 11),
+    "bssn_cart_fd6": ("Cartesian", (6, 6, 6), 6, 4, 12),
+    "bssn_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 13),
+    "bssn_sph_fd4": ("Spherical", (8, 6, 4), 4, 3, 14),
+    "sw_cart_fd4": ("Cartesian", (6, 6, 6), 4, 2, 15),
+    "sw_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 2, 16),
+    "maxwell_cart_fd4": ("Cartesian", (6, 6, 6), 4, 3, 17),
+}
+
+
+def senr_bc():
+    path = os.path.join(REF, "CurviBoundaryConditions", "SENRout4x4x4-Spherical_NGHOSTS4oFD.txt")
+    rows = []
+    for line in open(path):
+        left, right = line.split("|")
+        rows.append([int(v) for v in right.split()])
+    vals = np.array(rows, dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "senr_bc_spherical_4x4x4.npz"), values=vals)
+    print("senr", vals.shape)
+
+
+def ref_outputs():
+    import oracle.grid as og
+    from oracle.ref import RefKernels
+    from tests.helpers import bssn_random_state
+    cart = {"xmin": -2.0, "xmax": 2.0, "ymin": -2.0, "ymax": 2.0, "zmin": -2.0, "zmax": 2.0}
+    for cfg, (cs, N, fd, ng, seed) in FIXTURE_GRIDS.items():
+        gp = og.GridParams(cs, N, ng, fd, **KW)
+        R = RefKernels(cfg, gp, "strict", extra=dict(cart, **BL))
+        g = ng
+        I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+        out = dict(seed=seed, Nxx=np.array(N), fd=fd, ng=ng)
+        if cfg.startswith("bssn"):
+            f = bssn_random_state(gp.shape, seed=seed)
+            ric = R.ricci(f)
+            out["ricci"] = ric[I]
+            out["rhs"] = R.rhs_eval(f, aux=ric)[I]
+            out["hamiltonian"] = R.hamiltonian(f)[g:-g, g:-g, g:-g]
+            out["enforce_hDD"] = R.enforce(f)[11:17]
+            out["bl_id"] = R.initial_data((24,) + gp.shape)[I]
+        else:
+            ngf = 7 if cfg.startswith("maxwell") else 2
+            f = np.random.default_rng(seed).standard_normal((ngf,) + gp.shape)
+            out["rhs"] = R.rhs_eval(f)[I]
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % cfg), **out)
+        print(cfg, {k: getattr(v, "shape", v) for k, v in out.items()})
+
+
+# ------------------------------------------------------------ trusted values
+TRUSTED = [
+    # (name, module-relative trusted dict file, dict key, init code, call, globals)
+    ("BSSN_RHSs", "BSSN", "BSSN_RHSs__BSSN_RHSs__globals",
+     "import BSSN.BSSN_RHSs as M", "M.BSSN_RHSs()", ["cf_rhs", "trK_rhs", "lambda_rhsU", "a_rhsDD", "h_rhsDD"]),
+    ("gauge_RHSs", "BSSN", "gauge_RHSs__BSSN_gauge_RHSs__globals",
+     "import BSSN.BSSN_RHSs as rhs\nrhs.BSSN_RHSs()\nimport BSSN.BSSN_gauge_RHSs as M", "M.BSSN_gauge_RHSs()",
+     ["alpha_rhs", "bet_rhsU", "vet_rhsU"]),
+    ("Ricci", "BSSN", "BSSN_quantities__RicciBar__gammabarDD_dHatD__DGammaUDD__DGammaU__globals",
+     "import reference_metric as rfm\nrfm.reference_metric()\nrfm.ref_metric__hatted_quantities()\n"
+     "import BSSN.BSSN_quantities as M", "M.RicciBar__gammabarDD_dHatD__DGammaUDD__DGammaU()",
+     ["RbarDD", "DGammaU"]),
+    ("constraints", "BSSN", "BSSN_constraints__BSSN_constraints__globals",
+     "import BSSN.BSSN_constraints as M", "M.BSSN_constraints()", ["H"]),
+    ("ScalarWave_RHSs", "ScalarWave", "ScalarWave_RHSs__ScalarWave_RHSs__globals",
+     "import ScalarWave.ScalarWave_RHSs as M", "M.ScalarWave_RHSs()", ["uu_rhs", "vv_rhs"]),
+    ("ScalarWaveCurvilinear_RHSs", "ScalarWave", "ScalarWaveCurvilinear_RHSs__ScalarWaveCurvilinear_RHSs__globals",
+     "import ScalarWave.ScalarWaveCurvilinear_RHSs as M", "M.ScalarWaveCurvilinear_RHSs()", ["uu_rhs", "vv_rhs"]),
+    ("Maxwell_I", "Maxwell", "VacuumMaxwell_Flat_Evol_Cartesian_System_I__VacuumMaxwellRHSs__globals",
+     "import NRPy_param_funcs as par\n"
+     "par.initialize_param(par.glb_param('char', 'Maxwell.InitialData','System_to_use','System_I'))\n"
+     "import Maxwell.VacuumMaxwell_Flat_Evol_Cartesian as M", "M.VacuumMaxwellRHSs()",
+     ["ArhsU", "ErhsU", "C", "psi_rhs"]),
+]
+for cs in ("Spherical", "SinhSpherical", "Cartesian"):
+    TRUSTED.append(("rfm_" + cs, "tests", "rfm_%s__reference_metric__True__globals" % cs,
+                    "import NRPy_param_funcs as par\n"
+                    "import reference_metric as M\n"
+                    "par.set_parval_from_str('reference_metric::CoordSystem', '%s')" % cs, "M.reference_metric(True)",
+                    ["ReU", "ReDD", "ghatDD", "ghatUU", "detgammahat", "detgammahatdD", "detgammahatdDD",
+                     "ReUdD", "ReUdDD", "ReDDdD", "ReDDdDD", "ghatDDdD", "ghatDDdDD", "GammahatUDD",
+                     "GammahatUDDdD"]))
+
+WORKER = r'''
+import sys, json, hashlib, random
+sys.dont_write_bytecode = True
+REF = sys.argv[1]
+sys.path.insert(0, REF); sys.path.insert(0, REF + "/UnitTesting")
+spec = json.loads(sys.argv[2])
+exec(spec["init"])
+exec(spec["call"])
+import sympy as sp
+exprs = {}
+def expand(name, obj, idx=""):
+    if isinstance(obj, list):
+        for i, o in enumerate(obj):
+            expand(name, o, idx + "[%d]" % i)
+    else:
+        exprs[name + idx] = sp.sympify(obj)
+for g in spec["globals"]:
+    expand(g, getattr(M, g))
+syms = set()
+for e in exprs.values():
+    syms |= e.free_symbols
+vals = {}
+for s in syms:
+    n = str(s)
+    if n == "M_PI" or n == "M_SQRT1_2":
+        continue
+    random.seed(int(hashlib.md5(n.encode()).hexdigest(), 16))
+    vals[n] = random.random()
+print(json.dumps({"inputs": vals, "names": sorted(exprs)}))
+'''
+
+
+def trusted():
+    import importlib.util
+    out = {}
+    for name, mod, key, init, call, globs in TRUSTED:
+        spec = json.dumps({"init": init, "call": call, "globals": globs})
+        r = subprocess.run([sys.executable, "-c", WORKER, REF, spec], capture_output=True, text=True,
+                           env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"), cwd="/tmp")
+        if r.returncode != 0:
+            raise RuntimeError("%s: %s" % (name, r.stderr[-3000:]))
+        res = json.loads(r.stdout.strip().splitlines()[-1])
+        path = os.path.join(REF, mod, "tests", "trusted_values_dict.py") if mod != "tests" else \
+            os.path.join(REF, "tests", "trusted_values_dict.py")
+        sp_ = importlib.util.spec_from_file_location("tvd_" + name, path)
+        sys.path.insert(0, REF)
+        m = importlib.util.module_from_spec(sp_)
+        sp_.loader.exec_module(m)
+        tv = m.trusted_values_dict[key]
+        expected = {k: str(v) for k, v in tv.items() if k in res["names"]}
+        out[name] = {"key": key, "inputs": res["inputs"], "expected": expected}
+        print(name, len(res["inputs"]), "symbols,", len(expected), "values")
+    with open(os.path.join(HERE, "trusted_values.json"), "w") as f:
+        json.dump(out, f, indent=0, sort_keys=True)
+
+
+if __name__ == "__main__":
+    senr_bc()
+    ref_outputs()
+    trusted()

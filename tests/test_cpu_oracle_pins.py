@@ -1,0 +1,216 @@
+"""Pins the CPU oracle to the reference (no GPU):
+
+1. the reference's trusted-value unit tests (md5-seeded symbol values in,
+   30-digit expected values out) for BSSN_RHSs, BSSN_gauge_RHSs, the
+   conformal Ricci tensor, the Hamiltonian constraint, ScalarWave (Cartesian
+   and curvilinear), Maxwell System I, and the reference metric
+   (Spherical, SinhSpherical, Cartesian);
+2. outputs of the reference's own generated C (strict FP64 build) on seeded
+   grids, stored in tests/golden/ref_*.npz by tests/golden/make_golden.py;
+3. the SENR curvilinear-boundary-condition golden file (Spherical 4x4x4,
+   NGHOSTS 3), from the reference's Tutorial-Start_to_Finish-Curvilinear_BCs test.
+"""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle.bcs as ob
+import oracle.bssn as obs
+import oracle.grid as og
+import oracle.wave_maxwell as ow
+from tests.helpers import bssn_random_state, per_gf_rel
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TV = json.load(open(os.path.join(GOLD, "trusted_values.json")))
+
+RANK = {"hDD": 2, "aDD": 2, "lambdaU": 1, "vetU": 1, "betU": 1, "alpha": 0, "cf": 0, "trK": 0,
+        "uu": 0, "vv": 0, "EU": 1, "AU": 1, "psi": 0}
+SYMM2 = {"hDD", "aDD"}
+
+
+def symbols(inputs, bases):
+    """Arrays of gridfunction and derivative symbol values, completed by the
+    reference's index symmetries (sym01 gridfunctions, symmetric 2nd
+    derivatives); symbols absent from the expressions are 0."""
+    v = {}
+
+    def name(base, op, idx):
+        r = RANK[base]
+        a = list(idx[:r])
+        d = list(idx[r:])
+        if base in SYMM2:
+            a = sorted(a)
+        if op == "dDD":
+            d = sorted(d)
+        return base + ("_" + op if op else "") + "".join(map(str, a + d))
+
+    for base in bases:
+        r = RANK[base]
+        for op, nd in (("", 0), ("dD", 1), ("dupD", 1), ("dDD", 2)):
+            arr = np.zeros((3,) * (r + nd) + (1,))
+            for idx in itertools.product(range(3), repeat=r + nd):
+                arr[idx] = inputs.get(name(base, op, idx), 0.0)
+            v[base + ("_" + op if op else "")] = arr if r + nd else arr.reshape(1)
+    return v
+
+
+def expect(case):
+    return {k: float(x) for k, x in TV[case]["expected"].items()}
+
+
+def close(got, want, rtol):
+    return abs(got - want) <= rtol * max(abs(want), 1e-300) or abs(got - want) < 1e-12
+
+
+def _bssn_case(case):
+    inp = TV[case]["inputs"]
+    v = symbols(inp, ["hDD", "aDD", "lambdaU", "vetU", "betU", "alpha", "cf", "trK"])
+    q = og.hatted_at("Spherical", inp.get("xx0", 0.0), inp.get("xx1", 0.0))
+    q = {k: a[..., 0] for k, a in q.items()}  # point shape (1,)
+    return inp, v, q
+
+
+def test_trusted_bssn_rhss():
+    inp, v, q = _bssn_case("BSSN_RHSs")
+    out = obs.rhs(v, q, inp.get("eta", 0.0))
+    ex = expect("BSSN_RHSs")
+    for k, want in ex.items():
+        if k == "cf_rhs":
+            got = out["cf"][0]
+        elif k == "trK_rhs":
+            got = out["trK"][0]
+        else:
+            base, idx = k.split("[", 1)
+            ij = sorted(int(c) for c in idx if c.isdigit())
+            nm = {"lambda_rhsU": "lambdaU", "a_rhsDD": "aDD", "h_rhsDD": "hDD"}[base]
+            got = out[nm + "".join(map(str, ij))][0]
+        assert close(got, want, 1e-11), (k, got, want)
+
+
+def test_trusted_bssn_gauge_rhss():
+    inp, v, q = _bssn_case("gauge_RHSs")
+    out = obs.rhs(v, q, inp["eta"])
+    for k, want in expect("gauge_RHSs").items():
+        if k == "alpha_rhs":
+            got = out["alpha"][0]
+        else:
+            base, idx = k.split("[")
+            nm = {"bet_rhsU": "betU", "vet_rhsU": "vetU"}[base]
+            got = out[nm + idx[0]][0]
+        assert close(got, want, 1e-11), (k, got, want)
+
+
+def test_trusted_ricci_and_delta():
+    inp, v, q = _bssn_case("Ricci")
+    Q = obs._Q(v, q)
+    R = obs.ricci(v, q, Q)
+    for k, want in expect("Ricci").items():
+        idx = [int(c) for c in k if c.isdigit()]
+        got = R[idx[0], idx[1], 0] if k.startswith("RbarDD") else Q.DGammaU[idx[0], 0]
+        assert close(got, want, 1e-11), (k, got, want)
+
+
+def test_trusted_hamiltonian():
+    inp, v, q = _bssn_case("constraints")
+    H = obs.hamiltonian(v, q)[0]
+    want = expect("constraints")["H"]
+    assert close(H, want, 1e-11), (H, want)
+
+
+@pytest.mark.parametrize("case,cart", [("ScalarWave_RHSs", True), ("ScalarWaveCurvilinear_RHSs", False)])
+def test_trusted_scalarwave(case, cart):
+    inp = TV[case]["inputs"]
+    v = symbols(inp, ["uu", "vv"])
+    q = og.hatted_at("Spherical", inp.get("xx0", 0.0), inp.get("xx1", 0.0))
+    q = {k: a[..., 0] for k, a in q.items()}
+    u, w = ow.scalarwave_pointwise(v, q, inp.get("wavespeed", 1.0), cart)
+    ex = expect(case)
+    assert close(float(np.ravel(u)[0]), ex["uu_rhs"], 1e-13)
+    assert close(float(np.ravel(w)[0]), ex["vv_rhs"], 1e-12)
+
+
+def test_trusted_maxwell_system_I():
+    inp = TV["Maxwell_I"]["inputs"]
+    v = symbols(inp, ["EU", "AU", "psi"])
+    A, E, psi, C = ow.maxwell_pointwise(v)
+    ex = expect("Maxwell_I")
+    for i in range(3):
+        assert close(float(A[i][0]), ex["ArhsU[%d]" % i], 1e-13)
+        assert close(float(E[i][0]), ex["ErhsU[%d]" % i], 1e-13)
+    assert close(float(psi[0]), ex["psi_rhs"], 1e-13)
+    assert close(float(C[0]), ex["C"], 1e-13)
+
+
+@pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "Cartesian"])
+def test_trusted_reference_metric(cs):
+    inp = TV["rfm_" + cs]["inputs"]
+    q = og.hatted_at(cs, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("AMPL", 10.0), inp.get("SINHW", 0.2))
+    n = 0
+    for k, want in expect("rfm_" + cs).items():
+        base, _, rest = k.partition("[")
+        idx = tuple(int(c) for c in rest if c.isdigit())
+        got = float(q[base][idx][0, 0]) if idx else float(q[base][0, 0])
+        assert close(got, want, 1e-12), (k, got, want)
+        n += 1
+    assert n == 403
+
+
+# ------------------------------------------------- reference-generated C
+KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
+CFGS = {"bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical",
+        "bssn_sph_fd4": "Spherical"}
+
+
+@pytest.mark.parametrize("cfg", sorted(CFGS))
+def test_oracle_matches_reference_generated_bssn(cfg):
+    z = np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))
+    gp = og.GridParams(CFGS[cfg], tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    ric = obs.ricci_grid(gp, f)
+    assert per_gf_rel(ric[I], z["ricci"]) < 1e-13
+    # rhs_eval fed the reference's own RbarDD (LeaveRicciSymbolic form)
+    R6 = np.zeros((6,) + gp.shape)
+    R6[I] = z["ricci"]
+    assert per_gf_rel(obs.rhs_grid(gp, f, RbarDD6=R6)[I], z["rhs"]) < 1e-13
+    assert per_gf_rel(obs.hamiltonian_grid(gp, f)[None, g:-g, g:-g, g:-g], z["hamiltonian"][None]) < 1e-13
+    assert per_gf_rel(obs.enforce_detgammabar(gp, f)[11:17], z["enforce_hDD"]) < 1e-14
+
+
+@pytest.mark.parametrize("cfg,cs,fn,ngf", [("sw_cart_fd4", "Cartesian", ow.scalarwave_rhs_grid, 2),
+                                          ("sw_sinhsph_fd4", "SinhSpherical", ow.scalarwave_rhs_grid, 2),
+                                          ("maxwell_cart_fd4", "Cartesian", ow.maxwell_rhs_grid, 7)])
+def test_oracle_matches_reference_generated_wave_maxwell(cfg, cs, fn, ngf):
+    z = np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))
+    gp = og.GridParams(cs, tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
+    f = np.random.default_rng(int(z["seed"])).standard_normal((ngf,) + gp.shape)
+    g = gp.NGHOSTS
+    assert per_gf_rel(fn(gp, f)[:, g:-g, g:-g, g:-g], z["rhs"]) < 1e-13
+
+
+# ---------------------------------------------------------- SENR BC file
+SENR_PARITY = [1, 2, 3, 4, 5, 6, 7, 8, 9, 0]  # rankoneU0-2, ranktwosymmDD00..22, rankzero
+
+
+def senr_bc_case(apply):
+    """The Discrete test of Tutorial-Start_to_Finish-Curvilinear_BCs.ipynb:
+    value = linear index over all 10 gfs, ghosts set to NaN, BCs applied."""
+    gp = og.GridParams("Spherical", (4, 4, 4), 3, 4)
+    f = np.arange(10 * 1000, dtype=np.float64).reshape((10,) + gp.shape)
+    ng = 3
+    for i2, i1, i0 in itertools.product(range(10), repeat=3):
+        if min(i0, i1, i2) < ng or max(i0, i1, i2) >= 10 - ng:
+            f[:, i2, i1, i0] = np.nan
+    f = apply(gp, f)
+    return f.reshape(10, -1).T  # (points i0-fastest, gfs)
+
+
+def test_oracle_bcs_match_senr_golden_file():
+    want = np.load(os.path.join(GOLD, "senr_bc_spherical_4x4x4.npz"))["values"]
+    got = senr_bc_case(lambda gp, f: ob.apply_bcs(ob.build_bcstruct(gp), f, SENR_PARITY))
+    assert not np.isnan(got).any()
+    assert np.array_equal(got.astype(np.int64), want.astype(np.int64))
