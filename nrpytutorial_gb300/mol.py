@@ -83,6 +83,32 @@ class Evolution:
                      C.byref(self.gfs), float(dt)), "MoL_step_forward_in_time")
         self.time += dt
 
+    def capture(self, dt, n_steps=1, fused=True):
+        """Captures n_steps RK4 steps into a CUDA graph; returns a callable
+        that replays them on the current stream.  The step path launches
+        kernels only (no allocation, no host synchronisation), so the graph
+        holds the same launches the eager step would issue; dt and every
+        buffer address are fixed at capture time."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.step(dt, fused)  # warm-up launch outside the graph (module load, first-use costs)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        snapshot = self.y_n.clone()
+        with torch.cuda.graph(g):
+            for _ in range(n_steps):
+                self.step(dt, fused)
+        self.y_n.copy_(snapshot)  # undo the warm-up step
+        self.time -= dt * (n_steps + 1)
+        self._sync_stream()
+
+        def replay():
+            g.replay()
+            self.time += dt * n_steps
+        replay.graph = g
+        return replay
+
     def evolve_host(self, y_host, dt, n_steps):
         """Host-buffer evolution: y_host (numpy float64, IDX4S) in, state out."""
         self._sync_stream()

@@ -1,0 +1,112 @@
+"""The CUDA path against the reference directly: outputs of the reference's
+own generated C (tests/golden/ref_*.npz, strict FP64 build) on the same
+seeded inputs, the SENR curvilinear-BC golden file, and the reference's
+Brill-Lindquist initial_data."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import bssn_random_state, grids, per_gf_rel
+from tests.test_cpu_oracle_pins import SENR_PARITY, senr_bc_case
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
+CFGS = {"bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical",
+        "bssn_sph_fd4": "Spherical"}
+TOL = 1e-12
+
+
+def _load(cfg):
+    return np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))
+
+
+@pytest.mark.parametrize("cfg", sorted(CFGS))
+def test_bssn_matches_reference_generated_c(cuda, cfg):
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    z = _load(cfg)
+    G, gp = grids("BSSN", CFGS[cfg], tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]), **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    t = torch.tensor(f, device=cuda)
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+    ev.ricci_eval(t, aux)
+    assert per_gf_rel(aux.cpu().numpy()[I], z["ricci"]) < TOL
+    # rhs_eval with the reference's RbarDD as auxevol input
+    aux_ref = np.zeros((6,) + gp.shape)
+    aux_ref[I] = z["ricci"]
+    out = torch.zeros_like(t)
+    from bench import _rhs_only
+    _rhs_only(ev, t, torch.tensor(aux_ref, device=cuda), out)
+    assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
+    H = ev.hamiltonian(t).cpu().numpy()[0]
+    assert per_gf_rel(H[None, g:-g, g:-g, g:-g], z["hamiltonian"][None]) < TOL
+    t2 = t.clone()
+    ev.enforce_detgammabar(t2)
+    assert per_gf_rel(t2.cpu().numpy()[11:17], z["enforce_hDD"]) < 1e-14
+
+
+@pytest.mark.parametrize("cfg", sorted(CFGS))
+def test_brill_lindquist_matches_reference_initial_data(cuda, cfg):
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    z = _load(cfg)
+    G, gp = grids("BSSN", CFGS[cfg], tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]), **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    ev.initial_data_brill_lindquist(0.5, (0.0, 0.0, 0.5), 0.5, (0.0, 0.0, -0.5))
+    g = gp.NGHOSTS
+    got = ev.y_n.cpu().numpy()[:, g:-g, g:-g, g:-g]
+    want = z["bl_id"]
+    # every gf: normwise relative, or absolute for identically-zero ones
+    for k in range(24):
+        nb = np.linalg.norm(want[k])
+        err = np.linalg.norm(got[k] - want[k])
+        assert err <= 1e-12 * max(nb, 1.0), (k, err, nb)
+
+
+@pytest.mark.parametrize("cfg,cs,system,ngf", [("sw_cart_fd4", "Cartesian", "ScalarWave", 2),
+                                              ("sw_sinhsph_fd4", "SinhSpherical", "ScalarWave", 2),
+                                              ("maxwell_cart_fd4", "Cartesian", "Maxwell", 7)])
+def test_wave_maxwell_match_reference_generated_c(cuda, cfg, cs, system, ngf):
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    z = _load(cfg)
+    G, gp = grids(system, cs, tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]), **KW)
+    ev = Evolution(system, G, device=cuda)
+    f = np.random.default_rng(int(z["seed"])).standard_normal((ngf,) + gp.shape)
+    t = torch.tensor(f, device=cuda)
+    out = torch.zeros_like(t)
+    ev.rhs_eval(t, out)
+    g = gp.NGHOSTS
+    assert per_gf_rel(out.cpu().numpy()[:, g:-g, g:-g, g:-g], z["rhs"]) < TOL
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_gpu_bcs_match_senr_golden_file(cuda, dtype):
+    import torch
+    from nrpytutorial_gb300 import Grid, _lib
+    import ctypes as C
+    want = np.load(os.path.join(GOLD, "senr_bc_spherical_4x4x4.npz"))["values"]
+    lib = _lib.load()
+
+    def apply(gp, f):
+        G = Grid("Spherical", (4, 4, 4), FD_order=4, NGHOSTS=3)
+        bc = _lib.bc_struct()
+        _lib.check(lib.driver_bcstruct(C.byref(G.params), C.byref(bc)), "driver_bcstruct")
+        t = torch.tensor(f.astype(dtype), device=cuda)
+        _lib.set_stream(torch.cuda.current_stream())
+        par = (C.c_int8 * 10)(*SENR_PARITY)
+        fn = lib.apply_bcs_curvilinear if dtype == "float64" else lib.apply_bcs_curvilinear_f32
+        _lib.check(fn(C.byref(G.params), C.byref(bc), 10, C.cast(par, C.POINTER(C.c_int8)), _lib.ptr(t)), "bcs")
+        out = t.double().cpu().numpy()
+        lib.bcstruct_freemem(C.byref(bc))
+        return out
+
+    got = senr_bc_case(apply)
+    assert not np.isnan(got).any()
+    assert np.array_equal(got.astype(np.int64), want.astype(np.int64))
