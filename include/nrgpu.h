@@ -266,6 +266,17 @@ int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *params
  * Equations_in_Vacuum-Cartesian.ipynb:1089-1106). */
 int nrgpu_l2_norm_sq(const paramstruct *params, const double *gfs, int gf,
                      double *scratch, int scratch_len, double *result);
+/* The same reduction for callers that cannot allocate device memory: host
+ * codes that pass this library only the arrays they own and allow no device
+ * allocation inside their time loop, and C/Fortran drivers with no device
+ * allocator of their own.  No counterpart in the reference.  Its partial sums
+ * live in a fixed 2048-double (16 KB) device array inside the library, held
+ * by every GPU that loads it until the process exits; a call that would need
+ * more partials fails with NRGPU_ERR_SIZE.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress) with the device
+ * current, so make the first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU race; no cudaMalloc/cudaFree. */
+int nrgpu_l2_norm_sq_static(const paramstruct *params, const double *gfs, int gf, double *result);
 
 #ifdef __cplusplus
 }

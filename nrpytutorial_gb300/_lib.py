@@ -102,6 +102,7 @@ _PROTOS = {
     "MoL_evolve_host": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),
                                   P(MoL_gridfunctions), C.c_double, C.c_int, P(C.c_double)]),
     "nrgpu_l2_norm_sq": (C.c_int, [P(paramstruct), vp, C.c_int, vp, C.c_int, vp]),
+    "nrgpu_l2_norm_sq_static": (C.c_int, [P(paramstruct), vp, C.c_int, vp]),
 }
 
 _lib = None

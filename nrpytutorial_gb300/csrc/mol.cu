@@ -3,6 +3,9 @@
 // tables, and the interior L2-norm reduction used by constraint diagnostics.
 #include <string.h>
 
+#include <algorithm>
+#include <mutex>
+
 #include "epilogue.cuh"
 #include "systems.cuh"
 
@@ -285,4 +288,64 @@ int l2_norm_sq_impl(const paramstruct *p, const double *gfs, int gf, double *scr
 extern "C" int nrgpu_l2_norm_sq(const paramstruct *p, const double *gfs, int gf, double *scratch,
                                 int scratch_len, double *result) {
   return nrgpu::l2_norm_sq_impl(p, gfs, gf, scratch, scratch_len, result);
+}
+
+// ------------------------------------------- allocation-free L2 norm
+// Some callers cannot allocate device memory: host codes that hand this
+// library only the state arrays they own and forbid any allocation during
+// their time loop (arena-managed frameworks, drivers whose device memory is
+// fixed at start-up), and plain C/Fortran drivers that have no device
+// allocator of their own.  For them the per-block partial sums of the L2
+// reduction live in this fixed file-scope array instead of a caller-supplied
+// scratch buffer.  Every GPU that loads the library holds these 16 KB until
+// the process exits.
+#define NRGPU_L2_STATIC_MAX_PARTIALS 2048
+static __device__ __align__(256) double g_l2_static_partials[NRGPU_L2_STATIC_MAX_PARTIALS];
+
+namespace nrgpu {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_l2_static_mutex;
+double *g_l2_static_ptr[kMaxDevices] = {nullptr};
+}  // namespace
+}  // namespace nrgpu
+
+extern "C" int nrgpu_l2_norm_sq_static(const paramstruct *p, const double *gfs, int gf, double *result) {
+  using namespace nrgpu;
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(gfs && result, "NULL argument");
+  NRGPU_REQUIRE(gf >= 0, "negative gridfunction index");
+  int dev = 0;
+  NRGPU_CUDA_CHECK(cudaGetDevice(&dev));
+  NRGPU_REQUIRE(dev >= 0 && dev < kMaxDevices, "device %d beyond the %d this entry point tracks", dev, kMaxDevices);
+  double *partials;
+  {
+    // One-time set-up per device, with that device current: the host-side
+    // name of the array is not a device address, so look the address up.
+    std::lock_guard<std::mutex> lock(g_l2_static_mutex);
+    if (!g_l2_static_ptr[dev]) {
+      void *addr = nullptr;
+      NRGPU_CUDA_CHECK(cudaGetSymbolAddress(&addr, g_l2_static_partials));
+      g_l2_static_ptr[dev] = (double *)addr;
+    }
+    partials = g_l2_static_ptr[dev];
+  }
+  Grid g = make_grid(p);
+  const long long n = (long long)p->Nxx0 * p->Nxx1 * p->Nxx2;
+  const int threads = 256;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + threads - 1) / threads,
+                                                                      (long long)sm_count() * 4));
+  if (blocks > NRGPU_L2_STATIC_MAX_PARTIALS) {
+    set_error("nrgpu_l2_norm_sq_static: needs %d partial sums, the static scratch holds %d", blocks,
+              NRGPU_L2_STATIC_MAX_PARTIALS);
+    return NRGPU_ERR_SIZE;
+  }
+  // Every partial the final pass reads is written by this call's first pass,
+  // so the array needs no clearing between calls.
+  l2_partial_kernel<<<blocks, threads, 0, stream()>>>(g, gfs + (long long)gf * g.ntot, partials);
+  NRGPU_LAUNCH_CHECK();
+  l2_final_kernel<<<1, 256, 0, stream()>>>(partials, blocks, (double)n, result);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
 }
