@@ -292,6 +292,9 @@ def run_gpu(args):
         del ev32, aux, rhs, y32, aux32, rhs32
         torch.cuda.empty_cache()
         out["mixed_cartesian_256"] = run_config3(dev, args.config3_steps, flush)
+    if args.config4_steps > 0:
+        torch.cuda.empty_cache()
+        out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -383,6 +386,68 @@ def run_config3(dev, K, flush):
     res["rhs_f32_kernel"] = {"launch_ms": t * 1e3, "bytes_per_point": 54 * 4,
                              "achieved_GBps": nint * 216 / t / 1e9, "frac_of_hbm": nint * 216 / t / 1e9 / hbm}
     del e64, emix
+    return res
+
+
+def run_config4(dev, K, flush):
+    """Configuration 4: 512 independent ScalarWave evolutions on Spherical
+    grids (RMAX 10), Nr ~ U{32..160} (seeded), Ntheta 32, Nphi 8, FD4, RK4 with
+    each instance's own CFL-0.5 time step, Gaussian pulses
+    u = A exp(-(r-r0)^2/w^2) with A ~ U[0.1,1], r0 ~ U[1,4], w ~ U[0.5,2].
+    FP32 RHS / FP64 accumulation, K steps replayed from one CUDA graph, tile
+    autotuned; compared with the FP64 batch over the same K steps."""
+    import torch
+    from nrpytutorial_gb300 import _lib
+    from nrpytutorial_gb300.batch import ScalarWaveBatch
+    rng = np.random.default_rng(4)
+    n = 512
+    Nr = rng.integers(32, 161, n)
+    A, r0, w = rng.uniform(0.1, 1.0, n), rng.uniform(1.0, 4.0, n), rng.uniform(0.5, 2.0, n)
+    res = {"workload": "512 x ScalarWave Spherical Nr~U{32..160} x 32 x 8 FD4 RK4, seed 4", "steps": K}
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        B = ScalarWaveBatch(Nr, 32, 8, CoordSystem="Spherical", RMAX=10.0, precision=prec, device=dev)
+        B.initial_data_gaussian(A, r0, w)
+        tile = B.autotune(reps=3)
+        y0 = B.y_n.clone()
+        replay = B.capture(n_steps=K)
+        lib = _lib.load()
+        c0 = lib.nrgpu_kernel_launch_count()
+        B.step()
+        launches = lib.nrgpu_kernel_launch_count() - c0
+        B.y_n.copy_(y0)
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        replay()
+        b.record()
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        runs[prec] = (B, t)
+        res[prec] = {"tile": {"tx": tile[0], "ty": tile[1], "grid": tile[2], "rhs_launch_ms": tile[3]},
+                     "seconds": t, "ms_per_step": t / K * 1e3, "launches_per_step": int(launches)}
+    B64, t64 = runs["fp64"]
+    B32, t32 = runs["mixed"]
+    nint = B32.interior_points()
+    errs = []
+    for i in range(n):
+        u32 = B32.instance(i)[0]
+        u64 = B64.instance(i)[0]
+        errs.append(float(torch.linalg.vector_norm(u32 - u64) / torch.linalg.vector_norm(u64)))
+    hbm, _ = peaks()
+    # algorithmic bytes per interior point of one RK4 step (2 gfs):
+    # mixed 2 x (20 + 32 + 32 + 28) B, FP64 2 x (24 + 40 + 40 + 32) B
+    for prec, t, bpp in (("fp64", t64, 272), ("mixed", t32, 224)):
+        res[prec].update({"gp_updates_per_s": K * nint / t, "instance_steps_per_s": K * n / t,
+                          "bytes_per_point_step": bpp, "achieved_GBps": K * nint * bpp / t / 1e9,
+                          "frac_of_hbm": K * nint * bpp / t / 1e9 / hbm})
+    res.update({"interior_points": nint, "total_points_per_gf_set": B32.total,
+                "speedup_mixed_vs_fp64": t64 / t32,
+                "u_rel_l2_vs_fp64_max_over_instances": max(errs),
+                "u_rel_l2_vs_fp64_median": float(np.median(errs))})
+    del runs, B64, B32
+    torch.cuda.empty_cache()
     return res
 
 
@@ -543,6 +608,8 @@ def main():
     ap.add_argument("--ref-budget-s", type=float, default=90.0)
     ap.add_argument("--config3-steps", type=int, default=4,
                     help="RK4 steps of the 256^3 Cartesian mixed-vs-FP64 comparison (0 skips it)")
+    ap.add_argument("--config4-steps", type=int, default=400,
+                    help="RK4 steps of the 512-instance batched ScalarWave run (0 skips it)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -258,6 +258,49 @@ int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *params
                     const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt,
                     int n_steps, double *y_n_gfs_host);
 
+/* ---------------------------------------------- batched ScalarWave */
+/* Many independent curvilinear ScalarWave evolutions (Spherical or
+ * SinhSpherical, FD4, NGHOSTS 2, each with its own radial resolution Nr[i]
+ * and the shared Ntheta, Nphi) stepped together.  Each instance is exactly the
+ * evolution of Tutorial-Start_to_Finish-ScalarWaveCurvilinear.ipynb (RHS
+ * ScalarWaveCurvilinear_RHSs.py:43-98, RK4 RK_MoL.h, apply_bcs_curvilinear)
+ * with its own find_timestep(CFL_FACTOR) time step; the reference evolves
+ * one grid per process and has no batched counterpart.  State arrays are
+ * packed instance-major: instance i's gridfunction g starts at
+ * base[i] + g*ntot[i] (nrgpu_batch_offsets), nrgpu_batch_total_points
+ * values in all.  One RHS launch covers every instance (persistent grid over
+ * (instance, i2, i1-block) work items) and one launch per boundary phase
+ * covers every instance's ghost zones. */
+typedef struct nrgpu_batch nrgpu_batch;
+int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int CoordSystem,
+                       double RMAX, double AMPL, double SINHW, double wavespeed,
+                       double CFL_FACTOR, int precision, nrgpu_batch **batch);
+int nrgpu_batch_free(nrgpu_batch *batch);
+long long nrgpu_batch_total_points(const nrgpu_batch *batch);
+/* base[ninst], ntot[ninst]; n0n1n2[3*ninst] (Nxx_plus_2NGHOSTS0..2) may be NULL */
+int nrgpu_batch_offsets(const nrgpu_batch *batch, long long *base, long long *ntot, int *n0n1n2);
+int nrgpu_batch_timesteps(const nrgpu_batch *batch, double *dt);
+int nrgpu_batch_set_timesteps(nrgpu_batch *batch, const double *dt);
+/* u = A exp(-(r-r0)^2/w^2), v = 0 at all points of each instance (host
+ * arrays A, r0, w of ninst values; y_n_gfs an FP64 device array). */
+int nrgpu_batch_initial_data_gaussian(nrgpu_batch *batch, const double *A, const double *r0,
+                                      const double *w, double *y_n_gfs);
+/* RHS of every instance at interior points (FP64: double in/out; MIXED:
+ * float in/out, FP32 arithmetic). */
+int nrgpu_batch_rhs_eval(nrgpu_batch *batch, const void *in_gfs, void *rhs_gfs);
+int nrgpu_batch_apply_bcs(nrgpu_batch *batch, void *gfs, int is_f64);
+/* One RK4 step of every instance; gfs->precision must equal the batch's.
+ * MIXED: FP32 RHS and FP32 stage buffers, FP64 y_n and running total.
+ * Neither allocates nor synchronises (graph-capturable). */
+int nrgpu_batch_step(nrgpu_batch *batch, MoL_gridfunctions *gfs);
+/* Tile autotuner: times the RHS launch for each built tile shape (TX along
+ * i0 x TY rows of i1) and persistent grid size, keeps the fastest.  Writes
+ * rhs_scratch; synchronises; call outside stream capture. */
+int nrgpu_batch_autotune(nrgpu_batch *batch, const void *in_gfs, void *rhs_scratch, int reps,
+                         float *best_ms);
+int nrgpu_batch_set_tile(nrgpu_batch *batch, int tx, int ty, int grid);
+int nrgpu_batch_get_tile(const nrgpu_batch *batch, int *tx, int *ty, int *grid);
+
 /* --------------------------------------------------------- diagnostics */
 /* Sum over interior points of f^2 (and of 1) for gridfunction `gf` of an
  * FP64 array, FP64 accumulation; result[0] = sum f^2, result[1] = count.

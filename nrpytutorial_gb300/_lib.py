@@ -103,6 +103,20 @@ _PROTOS = {
                                   P(MoL_gridfunctions), C.c_double, C.c_int, P(C.c_double)]),
     "nrgpu_l2_norm_sq": (C.c_int, [P(paramstruct), vp, C.c_int, vp, C.c_int, vp]),
     "nrgpu_l2_norm_sq_static": (C.c_int, [P(paramstruct), vp, C.c_int, vp]),
+    "nrgpu_batch_create": (C.c_int, [C.c_int, P(C.c_int), C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_double, C.c_int, P(vp)]),
+    "nrgpu_batch_free": (C.c_int, [vp]),
+    "nrgpu_batch_total_points": (C.c_longlong, [vp]),
+    "nrgpu_batch_offsets": (C.c_int, [vp, P(C.c_longlong), P(C.c_longlong), P(C.c_int)]),
+    "nrgpu_batch_timesteps": (C.c_int, [vp, P(C.c_double)]),
+    "nrgpu_batch_set_timesteps": (C.c_int, [vp, P(C.c_double)]),
+    "nrgpu_batch_initial_data_gaussian": (C.c_int, [vp, P(C.c_double), P(C.c_double), P(C.c_double), vp]),
+    "nrgpu_batch_rhs_eval": (C.c_int, [vp, vp, vp]),
+    "nrgpu_batch_apply_bcs": (C.c_int, [vp, vp, C.c_int]),
+    "nrgpu_batch_step": (C.c_int, [vp, P(MoL_gridfunctions)]),
+    "nrgpu_batch_autotune": (C.c_int, [vp, vp, vp, C.c_int, P(C.c_float)]),
+    "nrgpu_batch_set_tile": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+    "nrgpu_batch_get_tile": (C.c_int, [vp, P(C.c_int), P(C.c_int), P(C.c_int)]),
 }
 
 _lib = None

@@ -1,0 +1,546 @@
+// batch.cu -- many independent small ScalarWave evolutions (curvilinear,
+// ragged grid sizes) advanced together: one persistent launch per RK4
+// substep covers every instance, and one launch per boundary phase covers
+// every instance's ghost zones.
+//
+// Physics per instance is exactly the single-grid path: the curvilinear
+// ScalarWave RHS (ScalarWave/ScalarWaveCurvilinear_RHSs.py:43-98), FD4, the
+// RK4 low-storage step (MoLtimestepping/C_Code_Generation.py:266-329) and
+// apply_bcs_curvilinear (boundary_conditions/apply_bcs_curvilinear.h:19-64).
+//
+// Layout: instance-major packed arrays, [instance][gf][i2][i1][i0]; a table of
+// BatchInstance records gives each instance's extents and offsets.  Work is a
+// list of (instance, i2, i1-block) items; a persistent grid walks the list
+// with a fixed stride, so instances of any size share one launch.  The item
+// shape (TX threads along i0, TY rows of i1) is chosen by a timing autotuner.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "epilogue.cuh"
+#include "fd.cuh"
+#include "rfm.cuh"
+
+namespace nrgpu {
+
+template <typename T>
+int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity, T *gfs);
+
+struct BatchInstance {
+  int n0, n1, n2;          // Nxx_plus_2NGHOSTS0..2
+  int pad;
+  long long base;          // offset of (gf 0, point 0) in packed state arrays
+  long long ntot;          // points per gridfunction
+  long long tab;           // offset of this instance's [6][n1][n0] metric table
+  double invdx0, invdx1, invdx2;
+  double dxx0, dxx1;       // uniform spacings, for the coordinates xx0, xx1
+  double dt;               // this instance's time step
+};
+
+constexpr int kBatchNG = 2;     // FD4 ScalarWave ghost zones
+constexpr int kBatchTab = 6;    // ghatUU0..2, contracted Gammahat^0..2
+
+struct BatchWork {
+  int inst, i2, i1;
+};
+
+// vv_rhs = c^2 (ghat^ii d_i d_i uu - ghat^ij Gammahat^k_ij d_k uu), per point.
+template <typename R, typename Tin, typename TStage, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY)
+    sw_batch_rhs_kernel(const BatchInstance *__restrict__ insts, const BatchWork *__restrict__ work, int nwork,
+                        const Tin *__restrict__ in, const R *__restrict__ tab, R c2, RKEpilogue<TStage> epi) {
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BatchWork it = work[w];
+    const BatchInstance I = insts[it.inst];
+    const int i1 = it.i1 + threadIdx.y;
+    if (i1 >= I.n1 - kBatchNG) continue;
+    const int i2 = it.i2;
+    const long long st[3] = {1, I.n0, (long long)I.n0 * I.n1};
+    const R inv[3] = {(R)I.invdx0, (R)I.invdx1, (R)I.invdx2};
+    const long long plane = (long long)I.n0 * I.n1;
+    for (int i0 = kBatchNG + threadIdx.x; i0 < I.n0 - kBatchNG; i0 += TX) {
+      const long long idx = i0 + I.n0 * ((long long)i1 + (long long)I.n1 * i2);
+      const Tin *uu = in + I.base + idx;
+      const R vv = (R)__ldg(in + I.base + I.ntot + idx);
+      const R *t = tab + I.tab + (long long)i1 * I.n0 + i0;
+      R lap = (R)0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        lap += __ldg(t + d * plane) * (fd_d2<4, R>(uu, st[d]) * (inv[d] * inv[d]));
+        if (d < 2) lap -= __ldg(t + (3 + d) * plane) * (fd_d1<4, R>(uu, st[d]) * inv[d]);
+      }
+      // the epilogue indexes gf g at base + g*ntot + idx of this instance
+      RKEpilogue<TStage> e = epi;
+      e.ntot = I.ntot;
+      e.dt = I.dt;
+      e.y_n = epi.y_n ? epi.y_n + I.base : nullptr;
+      e.rt = epi.rt ? epi.rt + I.base : nullptr;
+      e.out = epi.out ? epi.out + I.base : nullptr;
+      e(0, idx, vv);
+      e(1, idx, c2 * lap);
+    }
+  }
+}
+
+// Metric table of every instance: ghatUU (diagonal) and the contracted
+// Christoffels ghat^ij Gammahat^k_ij, from the FP64 hatted quantities.
+__global__ void sw_batch_table_kernel(const BatchInstance *__restrict__ insts, int ninst, int cs, double xxmin0,
+                                      double xxmin1, double AMPL, double SINHW, double *tab64, float *tab32) {
+  const int inst = blockIdx.y;
+  if (inst >= ninst) return;
+  const BatchInstance I = insts[inst];
+  const long long plane = (long long)I.n0 * I.n1;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < plane; c += gridDim.x * (long long)blockDim.x) {
+    const int i0 = (int)(c % I.n0), i1 = (int)(c / I.n0);
+    const double xx0 = xx_of(xxmin0, I.dxx0, i0, kBatchNG);
+    const double xx1 = xx_of(xxmin1, I.dxx1, i1, kBatchNG);
+    ScaleFactors S;
+    scale_factors(cs, AMPL, SINHW, xx0, xx1, &S);
+    double q[rq::NQ];
+    hatted_quantities(S, q);
+    double v[kBatchTab];
+    for (int i = 0; i < 3; i++) v[i] = q[rq::ghatUU + 4 * i];
+    for (int k = 0; k < 3; k++) {
+      double s = 0.0;
+      for (int i = 0; i < 3; i++) s += q[rq::ghatUU + 4 * i] * q[rq::GammahatUDD + 9 * k + 4 * i];
+      v[3 + k] = s;
+    }
+    for (int j = 0; j < kBatchTab; j++) {
+      tab64[I.tab + j * plane + c] = v[j];
+      tab32[I.tab + j * plane + c] = (float)v[j];
+    }
+  }
+}
+
+// Gaussian pulse u = A exp(-(r - r0)^2 / w^2), v = 0 at every point.
+__global__ void sw_batch_gaussian_kernel(const BatchInstance *__restrict__ insts, int ninst, int cs,
+                                         double xxmin0, double AMPL, double SINHW, const double *__restrict__ A,
+                                         const double *__restrict__ r0, const double *__restrict__ w,
+                                         double *__restrict__ y) {
+  const int inst = blockIdx.y;
+  if (inst >= ninst) return;
+  const BatchInstance I = insts[inst];
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < I.ntot; c += gridDim.x * (long long)blockDim.x) {
+    const int i0 = (int)(c % I.n0);
+    const double xx0 = xx_of(xxmin0, I.dxx0, i0, kBatchNG);
+    double r, r1, r2, r3;
+    radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
+    const double x = (r - r0[inst]) / w[inst];
+    y[I.base + c] = A[inst] * exp(-x * x);
+    y[I.base + I.ntot + c] = 0.0;
+  }
+}
+
+// Batched boundary conditions: per ghost layer and phase, one launch over the
+// points of every instance (both gridfunctions per thread).
+template <typename T>
+__global__ void sw_batch_bc_outer(const long long *__restrict__ dest, const int *__restrict__ step,
+                                  const long long *__restrict__ gfstride, int n, T *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const long long s = step[p];
+#pragma unroll
+  for (int g = 0; g < 2; g++) {
+    T *f = gfs + dest[p] + g * gfstride[p];
+    T v;
+    if constexpr (sizeof(T) == 8) v = __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[s]), __dmul_rn(3.0, f[2 * s])), f[3 * s]);
+    else v = __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[s]), __fmul_rn(3.0f, f[2 * s])), f[3 * s]);
+    *f = v;
+  }
+}
+
+template <typename T>
+__global__ void sw_batch_bc_inner(const long long *__restrict__ dest, const long long *__restrict__ src,
+                                  const long long *__restrict__ gfstride, int n, T *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+#pragma unroll
+  for (int g = 0; g < 2; g++) gfs[dest[p] + g * gfstride[p]] = gfs[src[p] + g * gfstride[p]];  // scalars: parity +1
+}
+
+}  // namespace nrgpu
+
+using namespace nrgpu;
+
+// Opaque batch state (host handle).
+struct nrgpu_batch {
+  int ninst, cs, N1, N2, prec;
+  double RMAX, AMPL, SINHW, xxmin0, xxmin1, c2;
+  long long total_points;   // per gridfunction-set: sum of 2*ntot
+  std::vector<BatchInstance> h_insts;
+  BatchInstance *d_insts = nullptr;
+  BatchWork *d_work[4] = {nullptr, nullptr, nullptr, nullptr};  // for TY = 1, 2, 4, 8
+  int nwork[4] = {0, 0, 0, 0};
+  double *d_tab64 = nullptr;
+  float *d_tab32 = nullptr;
+  // boundary phases: per layer g (2) x {outer d0, d1, d2, inner}
+  long long *d_bc_dest[8] = {}, *d_bc_src[8] = {}, *d_bc_gfs[8] = {};
+  int *d_bc_step[8] = {};
+  int bc_n[8] = {};
+  // tuned launch shape
+  int tx = 64, tyi = 1, grid = 0;
+};
+
+static void batch_destroy(nrgpu_batch *b) {
+  if (!b) return;
+  cudaFree(b->d_insts);
+  for (int t = 0; t < 4; t++) cudaFree(b->d_work[t]);
+  for (int ph = 0; ph < 8; ph++) {
+    cudaFree(b->d_bc_dest[ph]);
+    cudaFree(b->d_bc_src[ph]);
+    cudaFree(b->d_bc_gfs[ph]);
+    cudaFree(b->d_bc_step[ph]);
+  }
+  cudaFree(b->d_tab64);
+  cudaFree(b->d_tab32);
+  delete b;
+}
+
+static int batch_launch_rhs(nrgpu_batch *b, const void *in, bool in_f64, int stage, double *y_n,
+                            double *rt, void *out) {
+  const int TYs[4] = {1, 2, 4, 8};
+  const int ty = TYs[b->tyi];
+  const int grid = b->grid > 0 ? b->grid : 152 * 8;
+  const BatchWork *work = b->d_work[b->tyi];
+  const int nwork = b->nwork[b->tyi];
+#define LAUNCH(R, Tin, TS, TX, TY)                                                                          \
+  sw_batch_rhs_kernel<R, Tin, TS, TX, TY><<<grid, dim3(TX, TY), 0, stream()>>>(                            \
+      b->d_insts, work, nwork, (const Tin *)in, (const R *)(sizeof(R) == 8 ? (const void *)b->d_tab64      \
+                                                                            : (const void *)b->d_tab32),    \
+      (R)b->c2, RKEpilogue<TS>{stage, 0.0, 0, y_n, rt, (TS *)out})
+#define SHAPES(R, Tin, TS)                                                   \
+  switch (b->tx * 16 + ty) {                                                 \
+    case 32 * 16 + 1: LAUNCH(R, Tin, TS, 32, 1); break;                      \
+    case 32 * 16 + 2: LAUNCH(R, Tin, TS, 32, 2); break;                      \
+    case 32 * 16 + 4: LAUNCH(R, Tin, TS, 32, 4); break;                      \
+    case 32 * 16 + 8: LAUNCH(R, Tin, TS, 32, 8); break;                      \
+    case 64 * 16 + 1: LAUNCH(R, Tin, TS, 64, 1); break;                      \
+    case 64 * 16 + 2: LAUNCH(R, Tin, TS, 64, 2); break;                      \
+    case 64 * 16 + 4: LAUNCH(R, Tin, TS, 64, 4); break;                      \
+    case 128 * 16 + 1: LAUNCH(R, Tin, TS, 128, 1); break;                    \
+    case 128 * 16 + 2: LAUNCH(R, Tin, TS, 128, 2); break;                    \
+    default: set_error("unsupported batch tile %dx%d", b->tx, ty); return NRGPU_ERR_ARG; \
+  }
+  if (b->prec == NRGPU_PREC_FP64) {
+    SHAPES(double, double, double)
+  } else if (in_f64) {
+    SHAPES(float, double, float)
+  } else {
+    SHAPES(float, float, float)
+  }
+#undef SHAPES
+#undef LAUNCH
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+template <typename T> static int batch_bcs(nrgpu_batch *b, T *gfs) {
+  for (int ph = 0; ph < 8; ph++) {
+    const int n = b->bc_n[ph];
+    if (n == 0) continue;
+    const int B = 128;
+    if (ph % 4 < 3)
+      sw_batch_bc_outer<T><<<(n + B - 1) / B, B, 0, stream()>>>(b->d_bc_dest[ph], b->d_bc_step[ph], b->d_bc_gfs[ph], n, gfs);
+    else
+      sw_batch_bc_inner<T><<<(n + B - 1) / B, B, 0, stream()>>>(b->d_bc_dest[ph], b->d_bc_src[ph], b->d_bc_gfs[ph], n, gfs);
+    NRGPU_LAUNCH_CHECK();
+  }
+  return NRGPU_OK;
+}
+
+extern "C" {
+
+int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int CoordSystem, double RMAX, double AMPL,
+                       double SINHW, double wavespeed, double CFL_FACTOR, int precision, nrgpu_batch **out) {
+  NRGPU_REQUIRE(out && Nr && ninst >= 1, "bad arguments");
+  NRGPU_REQUIRE(CoordSystem == NRGPU_COORD_SPHERICAL || CoordSystem == NRGPU_COORD_SINHSPHERICAL,
+                "batched ScalarWave needs a Spherical-family CoordSystem");
+  NRGPU_REQUIRE(precision == NRGPU_PREC_FP64 || precision == NRGPU_PREC_MIXED, "bad precision");
+  NRGPU_REQUIRE(ninst <= 65535, "at most 65535 instances (grid y dimension)");
+  nrgpu_batch *b = new nrgpu_batch();
+  b->ninst = ninst;
+  b->cs = CoordSystem;
+  b->N1 = Ntheta;
+  b->N2 = Nphi;
+  b->prec = precision;
+  b->RMAX = RMAX;
+  b->AMPL = AMPL;
+  b->SINHW = SINHW;
+  b->c2 = wavespeed * wavespeed;
+  long long base = 0, tab = 0;
+  std::vector<BatchWork> work[4];
+  const int TYs[4] = {1, 2, 4, 8};
+  std::vector<long long> bdest[8], bsrc[8], bgfs[8];
+  std::vector<int> bstep[8];
+  for (int i = 0; i < ninst; i++) {
+    paramstruct p{};
+    p.CoordSystem = CoordSystem;
+    p.FD_order = 4;
+    p.NGHOSTS = kBatchNG;
+    p.RMAX = RMAX;
+    p.AMPL = AMPL;
+    p.SINHW = SINHW;
+    p.wavespeed = wavespeed;
+    const int Nxx[3] = {Nr[i], Ntheta, Nphi};
+    int st = set_Nxx_dxx_invdx_params__and__xx(0, Nxx, &p, nullptr);
+    if (st) {
+      batch_destroy(b);
+      return st;
+    }
+    if (i == 0) {
+      b->xxmin0 = p.xxmin0;
+      b->xxmin1 = p.xxmin1;
+    }
+    BatchInstance I{};
+    I.n0 = p.Nxx_plus_2NGHOSTS0;
+    I.n1 = p.Nxx_plus_2NGHOSTS1;
+    I.n2 = p.Nxx_plus_2NGHOSTS2;
+    I.ntot = (long long)I.n0 * I.n1 * I.n2;
+    I.base = base;
+    I.tab = tab;
+    I.invdx0 = p.invdx0;
+    I.invdx1 = p.invdx1;
+    I.invdx2 = p.invdx2;
+    I.dxx0 = p.dxx0;
+    I.dt = find_timestep(&p, CFL_FACTOR);
+    I.dxx1 = p.dxx1;
+    base += 2 * I.ntot;
+    tab += (long long)kBatchTab * I.n0 * I.n1;
+    b->h_insts.push_back(I);
+    for (int t = 0; t < 4; t++)
+      for (int i2 = kBatchNG; i2 < I.n2 - kBatchNG; i2++)
+        for (int i1 = kBatchNG; i1 < I.n1 - kBatchNG; i1 += TYs[t]) work[t].push_back(BatchWork{i, i2, i1});
+    // this instance's boundary map, offset into the packed arrays
+    bc_struct bc;
+    st = driver_bcstruct(&p, &bc);
+    if (st) {
+      batch_destroy(b);
+      return st;
+    }
+    std::vector<int> od(bc.total_outer), os(bc.total_outer), id_(bc.total_inner), is(bc.total_inner),
+        ip(bc.total_inner);
+    st = bcstruct_download(&bc, od.data(), os.data(), id_.data(), is.data(), ip.data());
+    bcstruct_freemem(&bc);
+    if (st) {
+      batch_destroy(b);
+      return st;
+    }
+    for (int g = 0; g < kBatchNG; g++) {
+      for (int d = 0; d < 3; d++)
+        for (int k = bc.ob_dir_start[g][d]; k < bc.ob_dir_start[g][d + 1]; k++) {
+          bdest[g * 4 + d].push_back(I.base + od[k]);
+          bstep[g * 4 + d].push_back(os[k]);
+          bgfs[g * 4 + d].push_back(I.ntot);
+        }
+      for (int k = bc.ib_start[g]; k < bc.ib_start[g] + bc.num_ib_gz_pts[g]; k++) {
+        bdest[g * 4 + 3].push_back(I.base + id_[k]);
+        bsrc[g * 4 + 3].push_back(I.base + is[k]);
+        bgfs[g * 4 + 3].push_back(I.ntot);
+      }
+    }
+  }
+  b->total_points = base;
+  auto up = [&](void **dst, const void *src, size_t bytes) -> int {
+    *dst = nullptr;
+    if (!bytes) return NRGPU_OK;
+    NRGPU_CUDA_CHECK(cudaMalloc(dst, bytes));
+    NRGPU_CUDA_CHECK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    return NRGPU_OK;
+  };
+  int st;
+#define NRGPU_BATCH_TRY(x)  \
+  if ((st = (x))) {         \
+    batch_destroy(b);       \
+    return st;              \
+  }
+  NRGPU_BATCH_TRY(up((void **)&b->d_insts, b->h_insts.data(), b->h_insts.size() * sizeof(BatchInstance)))
+  for (int t = 0; t < 4; t++) {
+    b->nwork[t] = (int)work[t].size();
+    NRGPU_BATCH_TRY(up((void **)&b->d_work[t], work[t].data(), work[t].size() * sizeof(BatchWork)))
+  }
+  for (int ph = 0; ph < 8; ph++) {
+    b->bc_n[ph] = (int)bdest[ph].size();
+    NRGPU_BATCH_TRY(up((void **)&b->d_bc_dest[ph], bdest[ph].data(), bdest[ph].size() * 8))
+    NRGPU_BATCH_TRY(up((void **)&b->d_bc_src[ph], bsrc[ph].data(), bsrc[ph].size() * 8))
+    NRGPU_BATCH_TRY(up((void **)&b->d_bc_gfs[ph], bgfs[ph].data(), bgfs[ph].size() * 8))
+    NRGPU_BATCH_TRY(up((void **)&b->d_bc_step[ph], bstep[ph].data(), bstep[ph].size() * 4))
+  }
+  NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab64, tab * sizeof(double)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
+  NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab32, tab * sizeof(float)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
+#undef NRGPU_BATCH_TRY
+  sw_batch_table_kernel<<<dim3(64, ninst), 128, 0, stream()>>>(b->d_insts, ninst, CoordSystem, b->xxmin0, b->xxmin1,
+                                                                AMPL, SINHW, b->d_tab64, b->d_tab32);
+  if (cudaGetLastError() != cudaSuccess) {
+    set_error("batch metric table launch failed");
+    batch_destroy(b);
+    return NRGPU_ERR_CUDA;
+  }
+  count_launch();
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  b->grid = sms * 8;
+  *out = b;
+  return NRGPU_OK;
+}
+
+long long nrgpu_batch_total_points(const nrgpu_batch *b) { return b ? b->total_points : -1; }
+
+int nrgpu_batch_offsets(const nrgpu_batch *b, long long *base, long long *ntot, int *n0n1n2) {
+  NRGPU_REQUIRE(b && base && ntot, "NULL argument");
+  for (int i = 0; i < b->ninst; i++) {
+    base[i] = b->h_insts[i].base;
+    ntot[i] = b->h_insts[i].ntot;
+    if (n0n1n2) {
+      n0n1n2[3 * i] = b->h_insts[i].n0;
+      n0n1n2[3 * i + 1] = b->h_insts[i].n1;
+      n0n1n2[3 * i + 2] = b->h_insts[i].n2;
+    }
+  }
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_set_tile(nrgpu_batch *b, int tx, int ty, int grid) {
+  NRGPU_REQUIRE(b, "NULL batch");
+  int tyi = ty == 1 ? 0 : ty == 2 ? 1 : ty == 4 ? 2 : ty == 8 ? 3 : -1;
+  NRGPU_REQUIRE(tyi >= 0, "TY must be 1, 2, 4 or 8");
+  NRGPU_REQUIRE((tx == 32 && ty <= 8) || (tx == 64 && ty <= 4) || (tx == 128 && ty <= 2),
+                "tile %dx%d not built (TX in {32,64,128}, TX*TY <= 256)", tx, ty);
+  NRGPU_REQUIRE(grid >= 1, "grid must be positive");
+  b->tx = tx;
+  b->tyi = tyi;
+  b->grid = grid;
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_get_tile(const nrgpu_batch *b, int *tx, int *ty, int *grid) {
+  NRGPU_REQUIRE(b && tx && ty && grid, "NULL argument");
+  const int TYs[4] = {1, 2, 4, 8};
+  *tx = b->tx;
+  *ty = TYs[b->tyi];
+  *grid = b->grid;
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_timesteps(const nrgpu_batch *b, double *dt) {
+  NRGPU_REQUIRE(b && dt, "NULL argument");
+  for (int i = 0; i < b->ninst; i++) dt[i] = b->h_insts[i].dt;
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_set_timesteps(nrgpu_batch *b, const double *dt) {
+  NRGPU_REQUIRE(b && dt, "NULL argument");
+  for (int i = 0; i < b->ninst; i++) {
+    NRGPU_REQUIRE(dt[i] > 0.0 && isfinite(dt[i]), "time step of instance %d is not positive", i);
+    b->h_insts[i].dt = dt[i];
+  }
+  NRGPU_CUDA_CHECK(cudaMemcpy(b->d_insts, b->h_insts.data(), b->h_insts.size() * sizeof(BatchInstance),
+                              cudaMemcpyHostToDevice));
+  return NRGPU_OK;
+}
+
+// Times the RHS launch (plain store into rhs_scratch) for every built tile
+// shape and several persistent grid sizes; keeps the fastest.
+int nrgpu_batch_autotune(nrgpu_batch *b, const void *in, void *rhs_scratch, int reps, float *best_ms) {
+  NRGPU_REQUIRE(b && in && rhs_scratch && reps >= 1, "bad arguments");
+  const int shapes[][2] = {{32, 1}, {32, 2}, {32, 4}, {32, 8}, {64, 1}, {64, 2}, {64, 4}, {128, 1}, {128, 2}};
+  const int mult[] = {2, 4, 8, 16, 32};
+  int dev = 0, sms = 152;
+  NRGPU_CUDA_CHECK(cudaGetDevice(&dev));
+  NRGPU_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaEvent_t e0, e1;
+  NRGPU_CUDA_CHECK(cudaEventCreate(&e0));
+  NRGPU_CUDA_CHECK(cudaEventCreate(&e1));
+  const bool f64 = b->prec == NRGPU_PREC_FP64;
+  float best = 1e30f;
+  int btx = b->tx, btyi = b->tyi, bgrid = b->grid, st = NRGPU_OK;
+  for (const auto &sh : shapes) {
+    for (int m : mult) {
+      if ((st = nrgpu_batch_set_tile(b, sh[0], sh[1], m * sms))) break;
+      if ((st = batch_launch_rhs(b, in, f64, -1, nullptr, nullptr, rhs_scratch))) break;  // warm-up
+      cudaEventRecord(e0, stream());
+      for (int r = 0; r < reps && st == NRGPU_OK; r++)
+        st = batch_launch_rhs(b, in, f64, -1, nullptr, nullptr, rhs_scratch);
+      cudaEventRecord(e1, stream());
+      if (st) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) { st = NRGPU_ERR_CUDA; break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (ms < best) {
+        best = ms;
+        btx = b->tx;
+        btyi = b->tyi;
+        bgrid = b->grid;
+      }
+    }
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tx = btx;
+  b->tyi = btyi;
+  b->grid = bgrid;
+  if (st) return st;
+  if (best_ms) *best_ms = best;
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_initial_data_gaussian(nrgpu_batch *b, const double *A, const double *r0, const double *w,
+                                      double *y_n) {
+  NRGPU_REQUIRE(b && A && r0 && w && y_n, "NULL argument");
+  double *d = nullptr;
+  const size_t n = (size_t)b->ninst;
+  NRGPU_CUDA_CHECK(cudaMalloc(&d, 3 * n * sizeof(double)));
+  NRGPU_CUDA_CHECK(cudaMemcpy(d, A, n * sizeof(double), cudaMemcpyHostToDevice));
+  NRGPU_CUDA_CHECK(cudaMemcpy(d + n, r0, n * sizeof(double), cudaMemcpyHostToDevice));
+  NRGPU_CUDA_CHECK(cudaMemcpy(d + 2 * n, w, n * sizeof(double), cudaMemcpyHostToDevice));
+  sw_batch_gaussian_kernel<<<dim3(64, b->ninst), 128, 0, stream()>>>(b->d_insts, b->ninst, b->cs, b->xxmin0, b->AMPL,
+                                                                     b->SINHW, d, d + n, d + 2 * n, y_n);
+  cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(stream());
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error("gaussian initial data: %s", cudaGetErrorString(e));
+    return NRGPU_ERR_CUDA;
+  }
+  count_launch();
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_rhs_eval(nrgpu_batch *b, const void *in, void *rhs) {
+  NRGPU_REQUIRE(b && in && rhs, "NULL argument");
+  return batch_launch_rhs(b, in, b->prec == NRGPU_PREC_FP64, -1, nullptr, nullptr, rhs);
+}
+
+int nrgpu_batch_apply_bcs(nrgpu_batch *b, void *gfs, int is_f64) {
+  NRGPU_REQUIRE(b && gfs, "NULL argument");
+  return is_f64 ? batch_bcs<double>(b, (double *)gfs) : batch_bcs<float>(b, (float *)gfs);
+}
+
+int nrgpu_batch_step(nrgpu_batch *b, MoL_gridfunctions *gfs) {
+  NRGPU_REQUIRE(b && gfs && gfs->y_n_gfs && gfs->y_nplus1_running_total_gfs && gfs->k_odd_gfs && gfs->k_even_gfs,
+                "NULL argument");
+  NRGPU_REQUIRE(gfs->precision == b->prec, "buffers' precision differs from the batch's");
+  const bool mixed = b->prec == NRGPU_PREC_MIXED;
+  void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  int st;
+  for (int s = 0; s < 4; s++) {
+    const void *in = (s == 0) ? (const void *)gfs->y_n_gfs : kbuf[(s + 1) % 2];
+    const bool in_f64 = (s == 0) || !mixed;
+    void *out = (s == 3) ? nullptr : kbuf[s % 2];
+    if ((st = batch_launch_rhs(b, in, in_f64, s, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, out))) return st;
+    void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
+    if ((st = (s == 3 || !mixed) ? batch_bcs<double>(b, (double *)post) : batch_bcs<float>(b, (float *)post))) return st;
+  }
+  return NRGPU_OK;
+}
+
+int nrgpu_batch_free(nrgpu_batch *b) {
+  batch_destroy(b);
+  return NRGPU_OK;
+}
+
+}  // extern "C"

@@ -80,6 +80,26 @@ def test_bad_arguments_return_status_not_abort():
     assert lib.nrgpu_fd_coeffs(3, 0, (C.c_double * 4)()) == 1
 
 
+def test_batch_create_validates_before_touching_the_device():
+    """Argument errors of the batched ScalarWave API are reported as status
+    codes before any CUDA call (so they are checkable without a GPU)."""
+    L, lib = _lib()
+    h = C.c_void_p()
+    nr = (C.c_int * 2)(16, 24)
+    args = (32, 8, 0, 10.0, 10.0, 0.2, 1.0, 0.5, 1)
+    assert lib.nrgpu_batch_create(2, nr, *args, C.byref(h)) == 1   # Cartesian is not supported
+    assert b"Spherical" in lib.nrgpu_last_error()
+    ok = (32, 8, 1, 10.0, 10.0, 0.2, 1.0, 0.5)
+    assert lib.nrgpu_batch_create(0, nr, *ok, 1, C.byref(h)) == 1  # empty batch
+    assert lib.nrgpu_batch_create(2, nr, *ok, 7, C.byref(h)) == 1  # unknown precision
+    assert lib.nrgpu_batch_create(2, None, *ok, 1, C.byref(h)) == 1
+    assert h.value is None
+    assert lib.nrgpu_batch_set_tile(None, 32, 1, 1) == 1
+    assert lib.nrgpu_batch_step(None, None) == 1
+    assert lib.nrgpu_batch_total_points(None) == -1
+    assert lib.nrgpu_batch_free(None) == 0
+
+
 def test_oracle_mixed_derivative_is_product_of_first():
     from oracle.fd import Stencils
     gp = og.GridParams("Cartesian", (6, 6, 6), 2, 4)
