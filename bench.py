@@ -40,6 +40,33 @@ RHS_BYTES_F64 = (24 + 6 + 24) * 8
 RICCI_BYTES_F64 = (9 + 6) * 8
 
 
+def state_errors(a, b, c0, names):
+    """Errors of state `a` against the FP64 state `b` (interior points,
+    (ngf, ...) tensors; c0 the common initial state): whole-state normwise
+    relative error, and per field the relative error, the error relative to
+    the field's change since c0, and the max-norm relative error.  Fields
+    whose FP64 norm is below 1e-6 of the largest field norm are identically
+    zero in the continuum (symmetry) and are reported but not ranked."""
+    import torch
+    a = a.double()
+    d = a - b
+    norms = [float(torch.linalg.vector_norm(b[i])) for i in range(b.shape[0])]
+    big = max(norms)
+    fields = {}
+    for i, n in enumerate(names):
+        nd = float(torch.linalg.vector_norm(d[i]))
+        nch = float(torch.linalg.vector_norm(b[i] - c0[i]))
+        fields[n] = {"rel_l2": nd / max(norms[i], 1e-300), "rel_l2_of_change": nd / max(nch, 1e-300),
+                     "rel_max": float(d[i].abs().max()) / max(float(b[i].abs().max()), 1e-300),
+                     "norm_fp64": norms[i], "significant": norms[i] >= 1e-6 * big}
+    sig = [f for f in fields.values() if f["significant"]]
+    return {"state_rel_l2": float(torch.linalg.vector_norm(d)) / float(torch.linalg.vector_norm(b)),
+            "max_rel_l2_significant_fields": max(f["rel_l2"] for f in sig),
+            "max_rel_max_significant_fields": max(f["rel_max"] for f in sig),
+            "max_rel_l2_of_change_significant_fields": max(f["rel_l2_of_change"] for f in sig),
+            "fields": fields}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -188,23 +215,32 @@ def run_gpu(args):
     finite = bool(torch.isfinite(y64).all().item())
     value = world * K * nint * 4 / t64
 
-    # ---- mixed precision (FP32 stage buffers and RHS, FP64 y_n/running total)
-    ev32 = Evolution("BSSN", G, precision="mixed", device=dev)
-    for _ in range(Wm):
-        ev32.y_n.copy_(y0)
-        ev32.step(dt)
-    ev32.y_n.copy_(y0)
-    torch.cuda.synchronize()
-    t32 = timed_steps(ev32, K)
+    # ---- FP32-arithmetic modes against the FP64 run over the same K steps
     g = W["ng"]
-    a = ev32.y_n[:, g:-g, g:-g, g:-g].double()
-    b = y64[:, g:-g, g:-g, g:-g]
-    rel_l2 = [float(torch.linalg.vector_norm(a[i] - b[i]) / torch.linalg.vector_norm(b[i]).clamp_min(1e-300))
-              for i in range(24)]
-    rel_max = [float((a[i] - b[i]).abs().max() / b[i].abs().max().clamp_min(1e-300)) for i in range(24)]
-    # Hamiltonian-constraint norms of both runs (FP64 diagnostics)
     H64 = ev.l2_norm(ev.hamiltonian(y64))
-    H32 = ev.l2_norm(ev.hamiltonian(ev32.y_n))
+    c0 = y0[:, g:-g, g:-g, g:-g]
+
+    def precision_run(prec):
+        e = Evolution("BSSN", G, precision=prec, device=dev)
+        for _ in range(Wm):
+            e.y_n.copy_(y0)
+            e.step(dt)
+        e.y_n.copy_(y0)
+        rep = e.capture(dt, n_steps=1)
+        e.y_n.copy_(y0)
+        torch.cuda.synchronize()
+        t = timed_replays(rep, K)
+        res = {"value": world * K * nint * 4 / t, "unit": UNIT, "ms_per_step": t / K * 1e3,
+               "speedup_vs_fp64": t64 / t, "after_steps": K}
+        res.update(state_errors(e.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names))
+        res["H_l2_fp64"] = H64
+        res["H_l2"] = e.l2_norm(ev.hamiltonian(e.y_n))
+        return e, res
+
+    ev32, mixed = precision_run("mixed")
+    del ev32
+    evc, comp = precision_run("compensated")
+    del evc
 
     # ---- dominant kernels alone: rhs_eval and Ricci_eval (plain stores)
     aux = torch.zeros((6,) + G.shape, dtype=torch.float64, device=dev)
@@ -232,6 +268,7 @@ def run_gpu(args):
     y32 = y0.float()
     aux32 = torch.zeros((6,) + G.shape, dtype=torch.float32, device=dev)
     rhs32 = torch.zeros_like(y32)
+    ev32 = Evolution("BSSN", G, precision="mixed", device=dev)
     ev32.ricci_eval(y32, aux32)
     t32k = []
     for r in range(R + 3):
@@ -282,10 +319,8 @@ def run_gpu(args):
         "kernels_ms": {"rhs_f64": t_rhs * 1e3, "ricci_f64": t_ric * 1e3, "rhs_f32": t_rhs32 * 1e3,
                        "ricci_f64_GBps": nint * RICCI_BYTES_F64 / t_ric / 1e9,
                        "rhs_f32_GBps": nint * RHS_BYTES_F64 / 2 / t_rhs32 / 1e9},
-        "mixed": {"value": world * K * nint * 4 / t32, "unit": UNIT, "ms_per_step": t32 / K * 1e3,
-                  "speedup_vs_fp64": t64 / t32,
-                  "rel_l2_vs_fp64_max_over_gfs": max(rel_l2), "rel_max_vs_fp64_max_over_gfs": max(rel_max),
-                  "after_steps": K, "H_l2_fp64": H64, "H_l2_mixed": H32},
+        "mixed": mixed,
+        "compensated": comp,
         "clocks": clocks,
     }
     if args.config3_steps > 0:
@@ -324,10 +359,12 @@ def run_config3(dev, K, flush):
     y0 = e64.y_n.clone()
     res = {"workload": "BSSN Cartesian 256^3 FD6 RK4 Brill-Lindquist m=(%.4f,%.4f) z=(%.4f,%.4f), seed 3"
                        % (m1, m2, z1, z2), "steps": K, "dt": dt}
-    times = {}
-    for prec, e in (("fp64", e64), ("mixed", None)):
-        if e is None:
-            e = Evolution("BSSN", G, precision="mixed", device=dev)
+    times, errs, H = {}, {}, {}
+    g = 4
+    B = e64.y_n[:, g:-g, g:-g, g:-g]
+    C0 = y0[:, g:-g, g:-g, g:-g]
+    for prec in ("fp64", "mixed", "compensated"):
+        e = e64 if prec == "fp64" else Evolution("BSSN", G, precision=prec, device=dev)
         e.y_n.copy_(y0)
         e.step(dt)  # warm-up
         e.y_n.copy_(y0)
@@ -342,30 +379,22 @@ def run_config3(dev, K, flush):
             torch.cuda.synchronize()
             tt += a.elapsed_time(b) / 1e3
         times[prec] = tt
-        if prec == "mixed":
-            emix = e
-    g = 4
-    A = emix.y_n[:, g:-g, g:-g, g:-g]
-    B = e64.y_n[:, g:-g, g:-g, g:-g]
-    C0 = y0[:, g:-g, g:-g, g:-g]
-    fields = {}
-    for i, name in enumerate(emix.gf_names):
-        d = A[i] - B[i]
-        nb = float(torch.linalg.vector_norm(B[i]))
-        nch = float(torch.linalg.vector_norm(B[i] - C0[i]))
-        fields[name] = {"rel_l2": float(torch.linalg.vector_norm(d)) / max(nb, 1e-300),
-                        "rel_l2_of_change": float(torch.linalg.vector_norm(d)) / max(nch, 1e-300),
-                        "rel_max": float(d.abs().max()) / max(float(B[i].abs().max()), 1e-300)}
-    res.update({
-        "fp64_gp_per_s": K * nint * 4 / times["fp64"], "mixed_gp_per_s": K * nint * 4 / times["mixed"],
-        "speedup": times["fp64"] / times["mixed"],
-        "ms_per_step_fp64": times["fp64"] / K * 1e3, "ms_per_step_mixed": times["mixed"] / K * 1e3,
-        "max_rel_l2_over_fields": max(f["rel_l2"] for f in fields.values()),
-        "max_rel_max_over_fields": max(f["rel_max"] for f in fields.values()),
-        "max_rel_l2_of_change_over_fields": max(f["rel_l2_of_change"] for f in fields.values()),
-        "H_l2_fp64": e64.l2_norm(e64.hamiltonian()), "H_l2_mixed": emix.l2_norm(emix.hamiltonian()),
-        "fields": fields,
-    })
+        H[prec] = e64.l2_norm(e64.hamiltonian(e.y_n))
+        if prec != "fp64":
+            errs[prec] = state_errors(e.y_n[:, g:-g, g:-g, g:-g], B, C0, e64.gf_names)
+            if prec == "mixed":
+                emix = e
+            else:
+                del e
+                torch.cuda.empty_cache()
+    res["fp64_gp_per_s"] = K * nint * 4 / times["fp64"]
+    res["ms_per_step_fp64"] = times["fp64"] / K * 1e3
+    res["H_l2_fp64"] = H["fp64"]
+    for prec in ("mixed", "compensated"):
+        r = {"gp_per_s": K * nint * 4 / times[prec], "ms_per_step": times[prec] / K * 1e3,
+             "speedup_vs_fp64": times["fp64"] / times[prec], "H_l2": H[prec]}
+        r.update(errs[prec])
+        res[prec] = r
     # FP32 rhs kernel alone at this size: algorithmic bytes 54 x 4 B per point
     y32 = emix.y_n.float()
     aux = torch.zeros((6,) + G.shape, dtype=torch.float32, device=dev)

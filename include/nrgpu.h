@@ -56,6 +56,8 @@ extern "C" {
 
 #define NRGPU_PREC_FP64   0       /* everything FP64                          */
 #define NRGPU_PREC_MIXED  1       /* FP32 stage buffers + FP32 RHS, FP64 y_n  */
+#define NRGPU_PREC_COMPENSATED 2  /* FP32 RHS on FP32 (hi, lo) pair stage
+                                     buffers, FP64 y_n and running total    */
 
 /*
  * paramstruct: the runtime parameters the generated kernels read through
@@ -119,8 +121,14 @@ typedef struct bc_struct {
  * MoL_gridfunctions: the four RK4 buffers of RK_Allocate_Memory.h
  * (MoLtimestepping/C_Code_Generation.py:97-103) plus auxevol storage.
  * y_n and the running total are always FP64; k_odd/k_even/auxevol are FP64
- * for NRGPU_PREC_FP64 and FP32 for NRGPU_PREC_MIXED.  All device pointers,
- * each NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot long (auxevol: 6 gfs for BSSN).
+ * for NRGPU_PREC_FP64 and FP32 otherwise.  All device pointers, each
+ * NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot values long (auxevol: 6 gfs for BSSN).
+ * NRGPU_PREC_COMPENSATED: k_odd/k_even hold interleaved FP32 pairs (float2:
+ * hi = FP32(v), lo = FP32(v - hi) of each FP64 stage value v), twice the
+ * floats of the MIXED buffers; each step starts by splitting y_n into
+ * k_even.  Stencils difference the hi parts (exact in FP32 for neighbouring
+ * values within a factor 2) and add the plain stencil of the lo parts, so
+ * the FP32 rounding of a value never enters a derivative.
  */
 typedef struct MoL_gridfunctions {
   int     precision;                     /* NRGPU_PREC_*                     */

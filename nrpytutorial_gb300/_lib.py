@@ -11,7 +11,7 @@ LIBPATH = os.path.join(HERE, "libnrgpu.so")
 
 COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2}
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
 
 

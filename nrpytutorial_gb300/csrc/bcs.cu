@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fd.cuh"
 #include "rfm.cuh"
 
 namespace nrgpu {
@@ -174,6 +175,32 @@ __global__ void bc_inner_kernel(const int *__restrict__ dest, const int *__restr
   f[dest[p]] = neg ? -v : v;
 }
 
+// FP32 pair gridfunctions (value = hi + lo): the outer rule evaluated in
+// FP64 on the values and re-split; the parity copy moves (or negates) both
+// parts, which is exact.
+__global__ void bc_outer_pair_kernel(const int *__restrict__ dest, const int *__restrict__ step, int npts,
+                                     int ngfs, long long ntot, float2 *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  float2 *f = gfs + (long long)gf * ntot;
+  const long long d = dest[p], s = step[p];
+  const double a = pair_value(f[d + s]), b = pair_value(f[d + 2 * s]), c = pair_value(f[d + 3 * s]);
+  f[d] = split_pair(__dadd_rn(__dsub_rn(__dmul_rn(3.0, a), __dmul_rn(3.0, b)), c));
+}
+
+__global__ void bc_inner_pair_kernel(const int *__restrict__ dest, const int *__restrict__ src,
+                                     const int *__restrict__ parity, int npts, int ngfs, long long ntot,
+                                     ParityTypes types, float2 *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  float2 *f = gfs + (long long)gf * ntot;
+  const bool neg = (parity[p] >> types.t[gf]) & 1;
+  const float2 v = f[src[p]];
+  f[dest[p]] = neg ? make_float2(-v.x, -v.y) : v;
+}
+
 template <typename T>
 int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
                           const int8_t *gfs_parity, T *gfs) {
@@ -207,6 +234,44 @@ int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
       dim3 grid((n + B - 1) / B, NUM_GFS);
       bc_inner_kernel<T><<<grid, B, 0, stream()>>>(bc->inner_dest + a, bc->inner_src + a,
                                                    bc->inner_parity + a, n, NUM_GFS, ntot, types, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+  }
+  return NRGPU_OK;
+}
+
+int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
+                        float2 *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL argument");
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64, "NUM_GFS %d out of range", NUM_GFS);
+  NRGPU_REQUIRE(bc->NGHOSTS == p->NGHOSTS, "bcstruct built for NGHOSTS=%d, params say %d", bc->NGHOSTS,
+                p->NGHOSTS);
+  ParityTypes types;
+  memset(&types, 0, sizeof(types));
+  for (int g = 0; g < NUM_GFS; g++) {
+    const int t = gfs_parity ? gfs_parity[g] : 0;
+    NRGPU_REQUIRE(t >= 0 && t <= 9, "parity type %d of gf %d not in 0..9", t, g);
+    types.t[g] = (int8_t)t;
+  }
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  const int B = 128;
+  for (int g = 0; g < bc->NGHOSTS; g++) {
+    for (int d = 0; d < 3; d++) {
+      const int a = bc->ob_dir_start[g][d], b = bc->ob_dir_start[g][d + 1];
+      const int n = b - a;
+      if (n <= 0) continue;
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_outer_pair_kernel<<<grid, B, 0, stream()>>>(bc->outer_dest + a, bc->outer_step + a, n, NUM_GFS, ntot, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+    const int n = bc->num_ib_gz_pts[g];
+    if (n > 0) {
+      const int a = bc->ib_start[g];
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_inner_pair_kernel<<<grid, B, 0, stream()>>>(bc->inner_dest + a, bc->inner_src + a, bc->inner_parity + a,
+                                                     n, NUM_GFS, ntot, types, gfs);
       NRGPU_LAUNCH_CHECK();
     }
   }

@@ -49,7 +49,9 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      h[i][j] = h[j][i] = (double)gfs[(long long)(HDD00 + S6(i, j)) * g.ntot + idx];
+      const long long k = (long long)(HDD00 + S6(i, j)) * g.ntot + idx;
+      if constexpr (std::is_same<T, float2>::value) h[i][j] = h[j][i] = pair_value(gfs[k]);
+      else h[i][j] = h[j][i] = (double)gfs[k];
       double v = RfmMask<CS>::trivial ? h[i][j] : h[i][j] * rf.ReDD(i, j);
       if (i == j) v += rf.ghatDD(i);
       gb[i][j] = gb[j][i] = v;
@@ -63,7 +65,10 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
 #pragma unroll
     for (int j = i; j < 3; j++) {
       const double d = (i == j) ? 1.0 : 0.0;
-      gfs[(long long)(HDD00 + S6(i, j)) * g.ntot + idx] = (T)(f * (d + h[i][j]) - d);
+      const long long k = (long long)(HDD00 + S6(i, j)) * g.ntot + idx;
+      const double v = f * (d + h[i][j]) - d;
+      if constexpr (std::is_same<T, float2>::value) gfs[k] = split_pair(v);
+      else gfs[k] = (T)v;
     }
 }
 
@@ -287,7 +292,7 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
   NRGPU_BSSN_SWITCH(RHS_CALL)
 }
 
-int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64) {
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair) {
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(gfs != nullptr, "NULL gridfunctions");
@@ -300,7 +305,8 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   else if (p->CoordSystem == NRGPU_COORD_SPHERICAL)                                                      \
     enforce_kernel<NRGPU_COORD_SPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
   else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
-  if (is_f64) { ENF(double) } else { ENF(float) }
+  NRGPU_REQUIRE(!(is_f64 && pair), "pair gridfunctions are FP32");
+  if (is_f64) { ENF(double) } else if (pair) { ENF(float2) } else { ENF(float) }
 #undef ENF
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;

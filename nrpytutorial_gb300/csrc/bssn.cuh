@@ -36,10 +36,10 @@ __host__ __device__ constexpr int S6(int i, int j) {
 
 // Stencil access to all gridfunctions at one point.
 template <typename Tin> struct Point {
-  const Tin *__restrict__ c;  // in_gfs + idx
+  typename InRef<Tin>::type c;  // in_gfs + idx (or hi + idx, lo + idx)
   long long ntot;
   long long st[3];
-  __device__ __forceinline__ const Tin *gf(int g) const { return c + (long long)g * ntot; }
+  __device__ __forceinline__ auto gf(int g) const { return c + (long long)g * ntot; }
 };
 
 template <int ORDER, typename R, typename Tin>
@@ -94,7 +94,7 @@ __device__ __forceinline__ void metric_point(const Point<Tin> &P, const Rfm<CS, 
 #pragma unroll
     for (int j = i; j < 3; j++) {
       const int g = HDD00 + S6(i, j);
-      const R hij = (R)__ldg(P.gf(g));
+      const R hij = val<R>(P.gf(g));
       m.h[i][j] = m.h[j][i] = hij;
       const R e = M::trivial ? hij : hij * rf.ReDD(i, j);
       m.eps[i][j] = m.eps[j][i] = e;
@@ -196,7 +196,7 @@ __device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R
   // lambda: \hat{D}_j Lambdabar^k (LambarU_dHatD)
   R lam[3], LdH[3][3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) lam[k] = (R)__ldg(P.gf(LAMBDAU0 + k));
+  for (int k = 0; k < 3; k++) lam[k] = val<R>(P.gf(LAMBDAU0 + k));
 #pragma unroll
   for (int k = 0; k < 3; k++)
 #pragma unroll
@@ -216,6 +216,12 @@ __device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R
 #pragma unroll
     for (int j = i; j < 3; j++) {
       const int gij = HDD00 + S6(i, j);
+      // the six distinct second derivatives of hDD_ij, each evaluated once
+      R hdd[6];
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int l = k; l < 3; l++) hdd[S6(k, l)] = D2<ORDER, R>(P, gij, k, l, inv);
       // Term 1: -1/2 gammabar^kl \hat{D}_k \hat{D}_l gammabar_ij (dHatDD[i][j][l][k])
       R t1 = (R)0;
 #pragma unroll
@@ -223,7 +229,7 @@ __device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R
 #pragma unroll
         for (int l = 0; l < 3; l++) {
           // eps_ij,lk
-          R edd = D2<ORDER, R>(P, gij, l, k, inv);
+          R edd = hdd[S6(l, k)];
           if constexpr (!M::trivial) {
             edd *= rf.ReDD(i, j);
             if (M::ReDDdD(i, j, k)) edd += D1<ORDER, R>(P, gij, l, inv) * rf.ReDDdD(i, j, k);
@@ -284,15 +290,15 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R> 
   Metric<CS, R> m;
   metric_point<ORDER, CS, R>(P, rf, inv, m);
 
-  const R alpha = (R)__ldg(P.gf(ALPHA));
-  const R cf = (R)__ldg(P.gf(CF));
-  const R trK = (R)__ldg(P.gf(TRK));
+  const R alpha = val<R>(P.gf(ALPHA));
+  const R cf = val<R>(P.gf(CF));
+  const R trK = val<R>(P.gf(TRK));
   R vet[3], bet[3], lam[3], betaU[3], BU[3], LambdabarU[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    vet[i] = (R)__ldg(P.gf(VETU0 + i));
-    bet[i] = (R)__ldg(P.gf(BETU0 + i));
-    lam[i] = (R)__ldg(P.gf(LAMBDAU0 + i));
+    vet[i] = val<R>(P.gf(VETU0 + i));
+    bet[i] = val<R>(P.gf(BETU0 + i));
+    lam[i] = val<R>(P.gf(LAMBDAU0 + i));
     betaU[i] = M::trivial ? vet[i] : vet[i] * rf.ReU(i);
     BU[i] = M::trivial ? bet[i] : bet[i] * rf.ReU(i);
     LambdabarU[i] = M::trivial ? lam[i] : lam[i] * rf.ReU(i);
@@ -337,7 +343,7 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R> 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      a[i][j] = a[j][i] = (R)__ldg(P.gf(ADD00 + S6(i, j)));
+      a[i][j] = a[j][i] = val<R>(P.gf(ADD00 + S6(i, j)));
       Abar[i][j] = Abar[j][i] = M::trivial ? a[i][j] : a[i][j] * rf.ReDD(i, j);
     }
   R AUD[3][3], AUU[3][3], trAbar = (R)0;

@@ -14,7 +14,7 @@ constexpr int kBlockX = 32, kBlockY = 4;
 
 template <typename R, typename Tin, int CS, int ORDER, typename TAux>
 __global__ void __launch_bounds__(kBlockX *kBlockY)
-    ricci_kernel(Grid g, const Tin *__restrict__ in, const R *__restrict__ tab, TAux *__restrict__ aux) {
+    ricci_kernel(Grid g, typename InRef<Tin>::type in, const R *__restrict__ tab, TAux *__restrict__ aux) {
   int i0, i1, i2;
   long long idx;
   if (!interior_point(g, i0, i1, i2, idx)) return;
@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY)
 
 template <typename R, typename Tin, int CS, int ORDER, typename TStage>
 __global__ void __launch_bounds__(kBlockX *kBlockY)
-    rhs_kernel(Grid g, const Tin *__restrict__ in, const TStage *__restrict__ aux, const R *__restrict__ tab,
+    rhs_kernel(Grid g, typename InRef<Tin>::type in, const R *__restrict__ aux, const R *__restrict__ tab,
                R eta, RKEpilogue<TStage> epi) {
   int i0, i1, i2;
   long long idx;
@@ -59,7 +59,10 @@ int ricci_launch_t(const rfm_struct *rfm, const paramstruct *p, const void *in, 
                    void *aux) {
   Grid g = make_grid(p);
   InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
-  if (prec == NRGPU_PREC_FP64) {
+  if (prec == NRGPU_PREC_COMPENSATED) {
+    ricci_kernel<float, Pair32, CS, ORDER, float><<<L.grid, L.block, 0, stream()>>>(
+        g, (const float2 *)in, table_of<float>(rfm), (float *)aux);
+  } else if (prec == NRGPU_PREC_FP64) {
     ricci_kernel<double, double, CS, ORDER, double>
         <<<L.grid, L.block, 0, stream()>>>(g, (const double *)in, table_of<double>(rfm), (double *)aux);
   } else if (in_is_f64) {
@@ -81,6 +84,10 @@ int rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
     rhs_kernel<double, double, CS, ORDER, double><<<L.grid, L.block, 0, stream()>>>(
         g, (const double *)a.in, (const double *)a.auxevol, table_of<double>(rfm), p->eta, epi);
+  } else if (a.prec == NRGPU_PREC_COMPENSATED) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    rhs_kernel<float, Pair32, CS, ORDER, float2><<<L.grid, L.block, 0, stream()>>>(
+        g, stage_input<Pair32>(a), (const float *)a.auxevol, table_of<float>(rfm), (float)p->eta, epi);
   } else {
     RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
     if (a.in_is_f64)

@@ -12,7 +12,10 @@
 // evaluated left to right in FP64 without FMA contraction, exactly as the
 // generated C writes it, so the fused update rounds like the reference's.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
+#include "fd.cuh"
 
 namespace nrgpu {
 
@@ -26,27 +29,35 @@ template <typename TStage> struct RKEpilogue {
   long long ntot;     // gridfunction stride
   double *y_n;        // FP64 state
   double *rt;         // FP64 running total
-  TStage *out;        // stage buffer (or rhs buffer for stage -1)
+  TStage *out;        // stage buffer (or rhs buffer for stage -1); float2:
+                      // FP32 (hi, lo) pairs of the FP64 stage value
+
+  // Stage value (computed in FP64) into the stage buffer.
+  __device__ __forceinline__ void put(long long i, double v) const {
+    if constexpr (std::is_same<TStage, float2>::value) out[i] = split_pair(v);
+    else out[i] = (TStage)v;
+  }
 
   template <typename R> __device__ __forceinline__ void operator()(int gf, long long idx, R value) const {
     const long long i = (long long)gf * ntot + idx;
     if (stage < 0) {
-      out[i] = (TStage)value;
+      if constexpr (std::is_same<TStage, float2>::value) out[i] = make_float2((float)value, 0.f);
+      else out[i] = (TStage)value;
       return;
     }
     const double kdt = dmul((double)value, dt);
     switch (stage) {
       case 0:
         rt[i] = dmul(kdt, 1.0 / 6.0);
-        out[i] = (TStage)dadd(y_n[i], dmul(kdt, 1.0 / 2.0));
+        put(i, dadd(y_n[i], dmul(kdt, 1.0 / 2.0)));
         break;
       case 1:
         rt[i] = dadd(rt[i], dmul(kdt, 1.0 / 3.0));
-        out[i] = (TStage)dadd(y_n[i], dmul(kdt, 1.0 / 2.0));
+        put(i, dadd(y_n[i], dmul(kdt, 1.0 / 2.0)));
         break;
       case 2:
         rt[i] = dadd(rt[i], dmul(kdt, 1.0 / 3.0));
-        out[i] = (TStage)dadd(y_n[i], kdt);
+        put(i, dadd(y_n[i], kdt));
         break;
       default:
         y_n[i] = dadd(dadd(y_n[i], rt[i]), dmul(kdt, 1.0 / 6.0));

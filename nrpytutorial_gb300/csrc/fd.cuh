@@ -101,6 +101,105 @@ __device__ __forceinline__ R fd_d11(const T *__restrict__ p, long long s, long l
   return acc;
 }
 
+// ------------------------------------------------ FP32 pair gridfunctions
+// A gridfunction stored as interleaved FP32 pairs (hi, lo) whose sum is the
+// FP64 value v: hi = FP32(v), lo = FP32(v - hi).  Stencils treat the two
+// parts separately: differences of neighbouring hi values are exact in
+// FP32 whenever the values are within a factor 2 of each other (Sterbenz)
+// and otherwise round relative to the difference, so a derivative loses
+// nothing to the FP32 storage of a large smooth field; lo is small and goes
+// through the plain stencil.  One 8-byte load fetches both parts.
+struct Pair32 {};  // stage-input tag: the input array is `const float2 *`
+
+// Input pointer type of a kernel whose stage input is `Tin`.
+template <typename Tin> struct InRef {
+  using type = const Tin *__restrict__;
+};
+template <> struct InRef<Pair32> {
+  using type = const float2 *__restrict__;
+};
+
+// Value at the stencil centre.
+template <typename R, typename T> __device__ __forceinline__ R val(const T *p) { return (R)__ldg(p); }
+template <typename R> __device__ __forceinline__ R val(const float2 *p) {
+  const float2 v = __ldg(p);
+  return (R)v.x + (R)v.y;
+}
+
+template <int ORDER, typename R> __device__ __forceinline__ R fd_d1(const float2 *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  R hi = (R)0, lo = (R)0;
+#pragma unroll
+  for (int k = 1; k <= C::R; k++) {
+    const float2 a = __ldg(p + k * s), b = __ldg(p - k * s);
+    hi += (R)C::c1(k) * ((R)a.x - (R)b.x);
+    lo += (R)C::c1(k) * ((R)a.y - (R)b.y);
+  }
+  return hi + lo;
+}
+// Second derivative over v[k] - v[0] (the weights sum to zero).
+template <int ORDER, typename R> __device__ __forceinline__ R fd_d2(const float2 *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  const float2 c = __ldg(p);
+  R hi = (R)0, lo = (R)C::c2(0) * (R)c.y;
+#pragma unroll
+  for (int k = 1; k <= C::R; k++) {
+    const float2 a = __ldg(p + k * s), b = __ldg(p - k * s);
+    hi += (R)C::c2(k) * (((R)a.x - (R)c.x) + ((R)b.x - (R)c.x));
+    lo += (R)C::c2(k) * ((R)a.y + (R)b.y);
+  }
+  return hi + lo;
+}
+template <int ORDER, typename R>
+__device__ __forceinline__ R fd_d11(const float2 *__restrict__ p, long long s, long long t) {
+  using C = FDCoef<ORDER>;
+  R hi = (R)0, lo = (R)0;
+#pragma unroll
+  for (int a = 1; a <= C::R; a++) {
+    R ih = (R)0, il = (R)0;
+#pragma unroll
+    for (int b = 1; b <= C::R; b++) {
+      const long long ps = a * s, qt = b * t;
+      const float2 pp = __ldg(p + ps + qt), pm = __ldg(p + ps - qt);
+      const float2 mp = __ldg(p - ps + qt), mm = __ldg(p - ps - qt);
+      ih += (R)C::c1(b) * (((R)pp.x - (R)pm.x) - ((R)mp.x - (R)mm.x));
+      il += (R)C::c1(b) * (((R)pp.y - (R)pm.y) - ((R)mp.y - (R)mm.y));
+    }
+    hi += (R)C::c1(a) * ih;
+    lo += (R)C::c1(a) * il;
+  }
+  return hi + lo;
+}
+// Upwinded derivative over v[k] - v[0] (the weights sum to zero).
+template <int ORDER, typename R>
+__device__ __forceinline__ R fd_dupwind(const float2 *__restrict__ p, long long s, bool positive) {
+  using C = FDCoef<ORDER>;
+  const long long ss = positive ? s : -s;
+  const float2 c = __ldg(p);
+  R hi = (R)0, lo = (R)0;
+#pragma unroll
+  for (int j = 0; j <= ORDER; j++) {
+    const int k = j + C::UPLO;
+    if (C::up(j) == 0.0) continue;
+    if (k == 0) {
+      lo += (R)C::up(j) * (R)c.y;
+    } else {
+      const float2 v = __ldg(p + k * ss);
+      hi += (R)C::up(j) * ((R)v.x - (R)c.x);
+      lo += (R)C::up(j) * (R)v.y;
+    }
+  }
+  const R acc = hi + lo;
+  return positive ? acc : -acc;
+}
+
+// FP64 value -> (hi, lo) pair.
+__device__ __forceinline__ float2 split_pair(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+}
+__device__ __forceinline__ double pair_value(float2 p) { return (double)p.x + (double)p.y; }
+
 // Upwinded first derivative (unscaled): dupD if positive, else ddnD.
 // ddnD weights are the negated mirror image of dupD's, so one loop with a
 // signed stride evaluates whichever one the control vector selects.

@@ -15,25 +15,25 @@ namespace nrgpu {
 
 template <typename R, typename Tin, int ORDER, typename TStage>
 __global__ void __launch_bounds__(256)
-    maxwell_kernel(Grid g, const Tin *__restrict__ in, RKEpilogue<TStage> epi) {
+    maxwell_kernel(Grid g, typename InRef<Tin>::type in, RKEpilogue<TStage> epi) {
   int i0, i1, i2;
   long long idx;
   if (!interior_point(g, i0, i1, i2, idx)) return;
   const long long st[3] = {1, g.n0, (long long)g.n0 * g.n1};
   const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
-  const Tin *A[3], *E[3];
+  decltype(in + idx) A[3], E[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     A[i] = in + (long long)i * g.ntot + idx;
     E[i] = in + (long long)(3 + i) * g.ntot + idx;
   }
-  const Tin *psi = in + 6LL * g.ntot + idx;
+  const auto psi = in + 6LL * g.ntot + idx;
   R divA = (R)0;
 #pragma unroll
   for (int i = 0; i < 3; i++) divA += fd_d1<ORDER, R>(A[i], st[i]) * inv[i];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    const R Ei = (R)__ldg(E[i]);
+    const R Ei = val<R>(E[i]);
     const R dpsi = fd_d1<ORDER, R>(psi, st[i]) * inv[i];
     epi(i, idx, -Ei - dpsi);
   }
@@ -65,13 +65,14 @@ __global__ void maxwell_constraint_kernel(Grid g, const double *__restrict__ in,
 }
 
 template <typename R, typename Tin, typename TStage>
-static int dispatch(const paramstruct *p, const Grid &g, const void *in, const RKEpilogue<TStage> &epi) {
+static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::type in,
+                    const RKEpilogue<TStage> &epi) {
   InteriorLaunch L = interior_launch(g, 64, 4);
   switch (p->FD_order) {
-    case 2: maxwell_kernel<R, Tin, 2, TStage><<<L.grid, L.block, 0, stream()>>>(g, (const Tin *)in, epi); break;
-    case 4: maxwell_kernel<R, Tin, 4, TStage><<<L.grid, L.block, 0, stream()>>>(g, (const Tin *)in, epi); break;
-    case 6: maxwell_kernel<R, Tin, 6, TStage><<<L.grid, L.block, 0, stream()>>>(g, (const Tin *)in, epi); break;
-    case 8: maxwell_kernel<R, Tin, 8, TStage><<<L.grid, L.block, 0, stream()>>>(g, (const Tin *)in, epi); break;
+    case 2: maxwell_kernel<R, Tin, 2, TStage><<<L.grid, L.block, 0, stream()>>>(g, in, epi); break;
+    case 4: maxwell_kernel<R, Tin, 4, TStage><<<L.grid, L.block, 0, stream()>>>(g, in, epi); break;
+    case 6: maxwell_kernel<R, Tin, 6, TStage><<<L.grid, L.block, 0, stream()>>>(g, in, epi); break;
+    case 8: maxwell_kernel<R, Tin, 8, TStage><<<L.grid, L.block, 0, stream()>>>(g, in, epi); break;
     default: set_error("Maxwell: FD_order %d not built", p->FD_order); return NRGPU_ERR_UNSUPPORTED;
   }
   NRGPU_LAUNCH_CHECK();
@@ -85,11 +86,15 @@ int maxwell_launch(const paramstruct *p, const StageArgs &a) {
   Grid g = make_grid(p);
   if (a.prec == NRGPU_PREC_FP64) {
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
-    return dispatch<double, double, double>(p, g, a.in, epi);
+    return dispatch<double, double, double>(p, g, stage_input<double>(a), epi);
+  }
+  if (a.prec == NRGPU_PREC_COMPENSATED) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), epi);
   }
   RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
-  if (a.in_is_f64) return dispatch<float, double, float>(p, g, a.in, epi);
-  return dispatch<float, float, float>(p, g, a.in, epi);
+  if (a.in_is_f64) return dispatch<float, double, float>(p, g, stage_input<double>(a), epi);
+  return dispatch<float, float, float>(p, g, stage_input<float>(a), epi);
 }
 
 }  // namespace nrgpu

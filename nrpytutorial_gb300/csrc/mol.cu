@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "epilogue.cuh"
 #include "systems.cuh"
@@ -49,30 +50,48 @@ int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const
 // ------------------------------------------------------- unfused update
 // LOOP_ALL_GFS_GPS RK update over all points of all gfs, reading the RHS the
 // RHS kernel stored in `k` (C_Code_Generation.py:159 and :277-329).
+// float2 stage buffers hold FP32 (hi, lo) pairs: the RHS is read as their
+// sum and the stage value is stored back as a pair.
+template <typename TStage> __device__ __forceinline__ double as_double(TStage v) {
+  if constexpr (std::is_same<TStage, float2>::value) return pair_value(v);
+  else return (double)v;
+}
+template <typename TStage> __device__ __forceinline__ TStage from_double(double v) {
+  if constexpr (std::is_same<TStage, float2>::value) return split_pair(v);
+  else return (TStage)v;
+}
+
 template <typename TStage>
 __global__ void rk4_update_kernel(int stage, double dt, long long n, double *__restrict__ y_n,
                                   double *__restrict__ rt, TStage *__restrict__ k) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const double kdt = __dmul_rn((double)k[i], dt);
+    const double kdt = __dmul_rn(as_double(k[i]), dt);
     switch (stage) {
       case 0:
         rt[i] = __dmul_rn(kdt, 1.0 / 6.0);
-        k[i] = (TStage)__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0));
+        k[i] = from_double<TStage>(__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0)));
         break;
       case 1:
         rt[i] = __dadd_rn(rt[i], __dmul_rn(kdt, 1.0 / 3.0));
-        k[i] = (TStage)__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0));
+        k[i] = from_double<TStage>(__dadd_rn(y_n[i], __dmul_rn(kdt, 1.0 / 2.0)));
         break;
       case 2:
         rt[i] = __dadd_rn(rt[i], __dmul_rn(kdt, 1.0 / 3.0));
-        k[i] = (TStage)__dadd_rn(y_n[i], kdt);
+        k[i] = from_double<TStage>(__dadd_rn(y_n[i], kdt));
         break;
       default:
         y_n[i] = __dadd_rn(__dadd_rn(y_n[i], rt[i]), __dmul_rn(kdt, 1.0 / 6.0));
         break;
     }
   }
+}
+
+// y_n -> FP32 (hi, lo) pairs over all points.
+__global__ void split_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = split_pair(y[i]);
 }
 
 static int sm_count() {
@@ -100,14 +119,32 @@ static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, co
   return NRGPU_ERR_ARG;
 }
 
-// Boundary conditions, then (BSSN) the det(gammabar) rescale, on `gfs`.
+// Boundary conditions, then (BSSN) the det(gammabar) rescale, on `gfs`
+// (double, float, or float2 pairs when `pair`).
 static int post_rhs(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc, void *gfs,
-                    bool is_f64) {
+                    bool is_f64, bool pair = false) {
   const int ngf = system_num_gfs(system);
-  int st = is_f64 ? apply_bcs_impl<double>(p, bc, ngf, system_parity(system), (double *)gfs)
-                  : apply_bcs_impl<float>(p, bc, ngf, system_parity(system), (float *)gfs);
+  int st;
+  if (pair) st = apply_bcs_pair_impl(p, bc, ngf, system_parity(system), (float2 *)gfs);
+  else if (is_f64) st = apply_bcs_impl<double>(p, bc, ngf, system_parity(system), (double *)gfs);
+  else st = apply_bcs_impl<float>(p, bc, ngf, system_parity(system), (float *)gfs);
   if (st) return st;
-  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64);
+  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64, pair);
+  return NRGPU_OK;
+}
+
+static long long state_len(int system, const paramstruct *p) {
+  return (long long)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 *
+         p->Nxx_plus_2NGHOSTS2;
+}
+
+// Start of a compensated step: y_n -> pairs in k_even_gfs (substep 0's input).
+static int split_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
+  const long long n = state_len(system, p);
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 8);
+  split_kernel<<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
+  NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
 
@@ -117,7 +154,8 @@ static int check_step_args(int system, const rfm_struct *rfm, const paramstruct 
   if (st) return st;
   NRGPU_REQUIRE(system_num_gfs(system) > 0, "unknown system %d", system);
   NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL bcstruct or gridfunctions");
-  NRGPU_REQUIRE(gfs->precision == NRGPU_PREC_FP64 || gfs->precision == NRGPU_PREC_MIXED,
+  NRGPU_REQUIRE(gfs->precision == NRGPU_PREC_FP64 || gfs->precision == NRGPU_PREC_MIXED ||
+                    gfs->precision == NRGPU_PREC_COMPENSATED,
                 "unknown precision %d", gfs->precision);
   NRGPU_REQUIRE(gfs->y_n_gfs && gfs->y_nplus1_running_total_gfs && gfs->k_odd_gfs && gfs->k_even_gfs,
                 "MoL gridfunction buffer is NULL");
@@ -137,23 +175,27 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
                              MoL_gridfunctions *gfs, double dt) {
   int st = check_step_args(system, rfm, p, bc, gfs);
   if (st) return st;
-  const bool mixed = gfs->precision == NRGPU_PREC_MIXED;
+  const bool f64 = gfs->precision == NRGPU_PREC_FP64;
+  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  if (pair && (st = split_state(system, p, gfs))) return st;
   for (int s = 0; s < 4; s++) {
     StageArgs a{};
     a.stage = s;
     a.dt = dt;
     a.prec = gfs->precision;
-    a.in = (s == 0) ? (const void *)gfs->y_n_gfs : (const void *)kbuf[(s + 1) % 2];
-    a.in_is_f64 = (s == 0) || !mixed;
+    // substep 0 reads y_n itself (as pairs in k_even when compensated)
+    a.in = (s == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
+                    : (const void *)kbuf[(s + 1) % 2];
+    a.in_is_f64 = !pair && ((s == 0) || f64);
     a.y_n = gfs->y_n_gfs;
     a.rt = gfs->y_nplus1_running_total_gfs;
     a.out = (s == 3) ? nullptr : kbuf[s % 2];
     a.auxevol = gfs->auxevol_gfs;
     if ((st = rhs_stage(system, rfm, p, a))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
-    const bool post_f64 = (s == 3) || !mixed;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64))) return st;
+    const bool post_f64 = (s == 3) || f64;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3))) return st;
   }
   return NRGPU_OK;
 }
@@ -162,23 +204,29 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
                                      const bc_struct *bc, MoL_gridfunctions *gfs, double dt) {
   int st = check_step_args(system, rfm, p, bc, gfs);
   if (st) return st;
-  const bool mixed = gfs->precision == NRGPU_PREC_MIXED;
+  const bool f64 = gfs->precision == NRGPU_PREC_FP64;
+  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
-  const long long n = (long long)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 *
-                      p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  const long long n = state_len(system, p);
   const int threads = 256;
   const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 16);
+  if (pair && (st = split_state(system, p, gfs))) return st;
   for (int s = 0; s < 4; s++) {
     StageArgs a{};
     a.stage = -1;
     a.dt = dt;
     a.prec = gfs->precision;
-    a.in = (s == 0) ? (const void *)gfs->y_n_gfs : (const void *)kbuf[(s + 1) % 2];
-    a.in_is_f64 = (s == 0) || !mixed;
+    a.in = (s == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
+                    : (const void *)kbuf[(s + 1) % 2];
+    a.in_is_f64 = !pair && ((s == 0) || f64);
     a.out = kbuf[s % 2];  // RHS_output: k_odd, k_even, k_odd, k_even
     a.auxevol = gfs->auxevol_gfs;
     if ((st = rhs_stage(system, rfm, p, a))) return st;
-    if (mixed)
+    if (pair)
+      rk4_update_kernel<float2><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+                                                                  gfs->y_nplus1_running_total_gfs,
+                                                                  (float2 *)kbuf[s % 2]);
+    else if (!f64)
       rk4_update_kernel<float><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
                                                                  gfs->y_nplus1_running_total_gfs,
                                                                  (float *)kbuf[s % 2]);
@@ -188,8 +236,8 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
                                                                   (double *)kbuf[s % 2]);
     NRGPU_LAUNCH_CHECK();
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
-    const bool post_f64 = (s == 3) || !mixed;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64))) return st;
+    const bool post_f64 = (s == 3) || f64;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3))) return st;
   }
   return NRGPU_OK;
 }

@@ -15,13 +15,13 @@ namespace nrgpu {
 
 template <typename R, typename Tin, int CS, int ORDER, typename TStage>
 __global__ void __launch_bounds__(256)
-    scalarwave_kernel(Grid g, const Tin *__restrict__ in, const R *__restrict__ rfmtab, R c2,
+    scalarwave_kernel(Grid g, typename InRef<Tin>::type in, const R *__restrict__ rfmtab, R c2,
                       RKEpilogue<TStage> epi) {
   int i0, i1, i2;
   long long idx;
   if (!interior_point(g, i0, i1, i2, idx)) return;
-  const Tin *uu = in + idx;
-  const R vv = (R)__ldg(in + g.ntot + idx);
+  const auto uu = in + idx;
+  const R vv = val<R>(in + g.ntot + idx);
   const long long st[3] = {1, g.n0, (long long)g.n0 * g.n1};
   const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
   R lap = (R)0;
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename R, typename Tin, typename TStage, int CS, int ORDER>
-static int launch_one(const Grid &g, const void *in, const rfm_struct *rfm, double c2,
+static int launch_one(const Grid &g, typename InRef<Tin>::type in, const rfm_struct *rfm, double c2,
                       const RKEpilogue<TStage> &epi) {
   const R *tab = nullptr;
   if constexpr (CS != NRGPU_COORD_CARTESIAN) {
@@ -64,13 +64,13 @@ static int launch_one(const Grid &g, const void *in, const rfm_struct *rfm, doub
   }
   InteriorLaunch L = interior_launch(g, 64, 4);
   scalarwave_kernel<R, Tin, CS, ORDER, TStage>
-      <<<L.grid, L.block, 0, stream()>>>(g, (const Tin *)in, tab, (R)c2, epi);
+      <<<L.grid, L.block, 0, stream()>>>(g, in, tab, (R)c2, epi);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
 
 template <typename R, typename Tin, typename TStage>
-static int dispatch(const paramstruct *p, const Grid &g, const void *in, const rfm_struct *rfm,
+static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::type in, const rfm_struct *rfm,
                     const RKEpilogue<TStage> &epi) {
   const double c2 = p->wavespeed * p->wavespeed;
 #define SW_CASE(CSV, ORD) \
@@ -90,11 +90,15 @@ int scalarwave_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
   Grid g = make_grid(p);
   if (a.prec == NRGPU_PREC_FP64) {
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
-    return dispatch<double, double, double>(p, g, a.in, rfm, epi);
+    return dispatch<double, double, double>(p, g, stage_input<double>(a), rfm, epi);
+  }
+  if (a.prec == NRGPU_PREC_COMPENSATED) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), rfm, epi);
   }
   RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
-  if (a.in_is_f64) return dispatch<float, double, float>(p, g, a.in, rfm, epi);
-  return dispatch<float, float, float>(p, g, a.in, rfm, epi);
+  if (a.in_is_f64) return dispatch<float, double, float>(p, g, stage_input<double>(a), rfm, epi);
+  return dispatch<float, float, float>(p, g, stage_input<float>(a), rfm, epi);
 }
 
 }  // namespace nrgpu

@@ -1,7 +1,10 @@
 // systems.cuh -- internal interface between the MoL driver and the per-system
 // RHS launchers.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
+#include "fd.cuh"
 
 namespace nrgpu {
 
@@ -10,7 +13,8 @@ namespace nrgpu {
 struct StageArgs {
   int stage;          // -1 plain rhs_eval, 0..3 RK4 substep
   double dt;
-  int prec;           // NRGPU_PREC_FP64 or NRGPU_PREC_MIXED (FP32 arithmetic)
+  int prec;           // NRGPU_PREC_FP64, or FP32 arithmetic (MIXED, COMPENSATED;
+                      // COMPENSATED: *in and *out are float2 pair arrays)
   const void *in;     // stage input gfs
   bool in_is_f64;     // type of *in
   double *y_n;        // FP64 state (fused stages)
@@ -19,16 +23,28 @@ struct StageArgs {
   void *auxevol;      // BSSN: RbarDD (same type as out)
 };
 
+// The kernel-side input of a stage (a float2 pair array for Pair32).
+template <typename Tin> inline typename InRef<Tin>::type stage_input(const StageArgs &a) {
+  if constexpr (std::is_same<Tin, Pair32>::value) return (const float2 *)a.in;
+  else return (const Tin *)a.in;
+}
+
 int scalarwave_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 int maxwell_launch(const paramstruct *p, const StageArgs &a);
 int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64,
                       int prec, void *auxevol);
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
-int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64);
+// is_f64: double array; otherwise float, or float2 pairs when pair is set
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair = false);
 
 // Evolved-gridfunction counts and parity types (alphabetical gf order;
 // parity types from CurviBoundaryConditions.py:122-213).
 int system_num_gfs(int system);
 const int8_t *system_parity(int system);
+
+// Boundary conditions on FP32 pair gridfunctions: ghost values computed in
+// FP64 from the pairs and stored back as pairs.
+int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
+                        float2 *gfs);
 
 }  // namespace nrgpu

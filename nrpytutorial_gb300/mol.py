@@ -21,7 +21,7 @@ class Evolution:
         if system not in SYSTEM_GFS:
             raise ValueError("unknown system %r" % system)
         if precision not in _lib.PREC:
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+            raise ValueError("precision must be one of %s" % sorted(_lib.PREC))
         self.system = system
         self.sys_id = _lib.SYSTEM[system]
         self.grid = grid
@@ -36,8 +36,10 @@ class Evolution:
         z = dict(device=self.device)
         self.y_n = torch.zeros(shape, dtype=torch.float64, **z)
         self.rt = torch.zeros(shape, dtype=torch.float64, **z)
-        self.k_odd = torch.zeros(shape, dtype=stage, **z)
-        self.k_even = torch.zeros(shape, dtype=stage, **z)
+        # compensated: stage buffers hold FP32 (hi, lo) pairs of the FP64 stage values
+        kshape = shape + (2,) if precision == "compensated" else shape
+        self.k_odd = torch.zeros(kshape, dtype=stage, **z)
+        self.k_even = torch.zeros(kshape, dtype=stage, **z)
         naux = len(AUXEVOL_GFS.get(system, []))
         self.auxevol = torch.zeros((max(naux, 1),) + grid.shape, dtype=stage, **z)
         self.gfs = _lib.MoL_gridfunctions(_lib.PREC[precision], self.y_n.data_ptr(), self.rt.data_ptr(),
@@ -91,11 +93,11 @@ class Evolution:
         buffer address are fixed at capture time."""
         g = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream(self.device)
+        snapshot = self.y_n.clone()
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
             self.step(dt, fused)  # warm-up launch outside the graph (module load, first-use costs)
         torch.cuda.current_stream(self.device).wait_stream(side)
-        snapshot = self.y_n.clone()
         with torch.cuda.graph(g):
             for _ in range(n_steps):
                 self.step(dt, fused)

@@ -147,7 +147,7 @@ def test_cuda_graph_replay_matches_eager_steps(cuda):
     eager = ev.y_n.clone()
     ev.y_n.copy_(y0)
     replay = ev.capture(dt, n_steps=3)
-    ev.y_n.copy_(y0)
+    assert torch.equal(ev.y_n, y0)  # capturing leaves the state as it was
     replay()
     torch.cuda.synchronize()
     assert torch.equal(ev.y_n, eager)

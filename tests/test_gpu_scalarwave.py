@@ -85,17 +85,18 @@ def test_rk4_step_matches_oracle(cuda, coord, fused):
     assert per_gf_rel(got, yo) < 1e-12
 
 
-def test_plane_wave_fourth_order_convergence(cuda):
-    """Config-1 physics at reduced size: u = sin(k.x - |k|t) on [-10,10]^3,
-    FD4, RK4, CFL 0.5, quadratic-extrapolation outer BCs.  The error at fixed
-    t must fall like N^-4 (Tutorial-Start_to_Finish-ScalarWave.ipynb's
-    48/64 convergence check)."""
+@pytest.mark.parametrize("prec", ["fp64", "compensated"])
+def test_plane_wave_fourth_order_convergence(cuda, prec):
+    """Plane wave u = sin(k.x - |k|t) on [-10,10]^3, FD4, RK4, CFL 0.5,
+    quadratic-extrapolation outer BCs.  The error at fixed t must fall like
+    N^-4 (Tutorial-Start_to_Finish-ScalarWave.ipynb's convergence check), in
+    FP64 and with FP32 RHS arithmetic on compensated stage buffers."""
     import torch
     errs = []
     T = 2.0
     for N in (24, 48):
         G, gp = grids("ScalarWave", "Cartesian", (N, N, N), 4)
-        ev = _evo(cuda, G)
+        ev = _evo(cuda, G, prec)
         ev.y_n.copy_(torch.tensor(ow.plane_wave(gp, 0.0), device=cuda))
         dt = 0.5 * min(gp.dxx)
         nsteps = int(round(T / dt))
