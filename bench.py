@@ -330,6 +330,9 @@ def run_gpu(args):
     if args.config4_steps > 0:
         torch.cuda.empty_cache()
         out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush)
+    if args.config5_steps > 0:
+        torch.cuda.empty_cache()
+        out["adjoint_maxwell_128"] = run_config5(dev, args.config5_steps)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -478,6 +481,47 @@ def run_config4(dev, K, flush):
     del runs, B64, B32
     torch.cuda.empty_cache()
     return res
+
+
+def run_config5(dev, K):
+    """Configuration 5: Maxwell System I, Cartesian [-10,10]^3 at 128^3, FD4,
+    FP64, K RK4 steps (CFL 0.5) from toroidal-dipole data with seeded
+    amplitude and width parameters; observable = L2 norm of E over the
+    sphere r = 8 (32 x 64 points) and the evolution; gradient with respect
+    to (amp, lam) by the discrete adjoint, checkpoints every 20 steps,
+    checked against central differences with h = 1e-6."""
+    import torch
+    from nrpytutorial_gb300 import Grid
+    from nrpytutorial_gb300.adjoint import ExtractionSphere, MaxwellExtraction
+    rng = np.random.default_rng(5)
+    amp, lam = rng.uniform(0.5, 1.5), rng.uniform(0.5, 1.5)
+    G = Grid("Cartesian", (128, 128, 128), FD_order=4, NGHOSTS=3, domain=(-10.0, 10.0))
+    m = MaxwellExtraction(G, ExtractionSphere(8.0, 32, 64), n_steps=K, checkpoint_every=20, device=dev)
+    m.forward(amp, lam)  # warm-up
+    m.gradient()
+
+    def timed(f):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        r = f()
+        b.record()
+        torch.cuda.synchronize()
+        return r, a.elapsed_time(b) / 1e3
+
+    J, t_fwd = timed(lambda: m.forward(amp, lam))
+    g, t_bwd = timed(m.gradient)
+    h = 1e-6
+    fd = [(m.forward(amp + h, lam) - m.forward(amp - h, lam)) / (2 * h),
+          (m.forward(amp, lam + h) - m.forward(amp, lam - h)) / (2 * h)]
+    rel = [abs(g[i] - fd[i]) / abs(fd[i]) for i in range(2)]
+    nint = 128 ** 3
+    return {"workload": "Maxwell System I Cartesian [-10,10]^3 128^3 FD4 FP64, %d RK4 steps, toroidal dipole "
+                        "amp=%.6f lam=%.6f (seed 5), |E| on sphere r=8 (32x64), checkpoints every 20" % (K, amp, lam),
+            "J": J, "grad": [float(v) for v in g], "grad_central_fd_h1e-6": [float(v) for v in fd],
+            "grad_rel_err_vs_fd": rel, "forward_s": t_fwd, "adjoint_s": t_bwd,
+            "adjoint_over_forward": t_bwd / t_fwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
+            "forward_gp_updates_per_s": K * nint / t_fwd, "checkpoints": len(m.checkpoints)}
 
 
 def _rhs_only(ev, y, aux, out):
@@ -637,6 +681,8 @@ def main():
     ap.add_argument("--ref-budget-s", type=float, default=90.0)
     ap.add_argument("--config3-steps", type=int, default=4,
                     help="RK4 steps of the 256^3 Cartesian mixed-vs-FP64 comparison (0 skips it)")
+    ap.add_argument("--config5-steps", type=int, default=300,
+                    help="RK4 steps of the Maxwell 128^3 adjoint-gradient run (0 skips it)")
     ap.add_argument("--config4-steps", type=int, default=400,
                     help="RK4 steps of the 512-instance batched ScalarWave run (0 skips it)")
     args = ap.parse_args()

@@ -309,6 +309,47 @@ int nrgpu_batch_autotune(nrgpu_batch *batch, const void *in_gfs, void *rhs_scrat
 int nrgpu_batch_set_tile(nrgpu_batch *batch, int tx, int ty, int grid);
 int nrgpu_batch_get_tile(const nrgpu_batch *batch, int *tx, int *ty, int *grid);
 
+/* ------------------------------------------------------------ adjoint */
+/* Discrete adjoint of the Maxwell System I evolution (FP64, Cartesian).  The
+ * reference has no adjoint; these are the transposes of the linear maps
+ * above, so that gradients of observables of an evolution with respect to
+ * its initial data are exact for the discretised problem.
+ *   Maxwell_rhs_eval_adjoint:  adj_in = L^T adj_rhs at every point, where L
+ *       is Maxwell_rhs_eval (interior rows only); adj_rhs is read at
+ *       interior points only.
+ *   apply_bcs_curvilinear_adjoint:  in place, the transpose of
+ *       apply_bcs_curvilinear: ghost adjoints are added onto the points they
+ *       were computed from (phases in reverse order) and zeroed.
+ *   MoL_adjoint_step_backward:  lam_out = (dy_{n+1}/dy_n)^T lam_in for one
+ *       MoL_step_forward_in_time step; lam_in is overwritten; scratch holds
+ *       4 * NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot doubles.  Maxwell only. */
+int Maxwell_rhs_eval_adjoint(const paramstruct *params, const double *adj_rhs_gfs, double *adj_in_gfs);
+int apply_bcs_curvilinear_adjoint(const paramstruct *params, const bc_struct *bcstruct, int NUM_GFS,
+                                  const int8_t *gfs_parity, double *adj_gfs);
+int MoL_adjoint_step_backward(int system, const paramstruct *params, const bc_struct *bcstruct,
+                              double *lam_in, double *lam_out, double *scratch, double dt);
+/* Toroidal-dipole initial data (Maxwell/InitialData.py:41-104) at all
+ * points, and its derivatives with respect to amp and lam (any of the three
+ * outputs may be NULL). */
+int Maxwell_initial_data_toroidal_dipole(const paramstruct *params, double amp, double lam, double time,
+                                         double *in_gfs, double *d_in_d_amp, double *d_in_d_lam);
+/* Extraction sphere: tricubic Lagrange interpolation of gridfunctions
+ * gf0..gf0+ngf-1 at npts Cartesian points (device array pts[3*npts]) into
+ * samples[npts*ngf], and accum[0] += scale * sum_p wts[p] |f(x_p)|^2 (device
+ * scalars).  Points whose 4x4x4 stencil leaves the grid set a flag that
+ * nrgpu_sphere_check reads (and that the next call clears).
+ * nrgpu_sphere_sample_adjoint adds the gradient of J = sqrt(accum[0]) with
+ * respect to the sampled gridfunctions for one sample set:
+ * adj_gfs += (scale/J) sum_p wts[p] samples[p] (x) interpolation weights. */
+int nrgpu_sphere_sample(const paramstruct *params, const double *gfs, int gf0, int ngf, const double *pts,
+                        const double *wts, int npts, double scale, double *samples, double *accum);
+int nrgpu_sphere_sample_adjoint(const paramstruct *params, const double *samples, int gf0, int ngf,
+                                const double *pts, const double *wts, int npts, double scale,
+                                const double *accum, double *adj_gfs);
+int nrgpu_sphere_check(const paramstruct *params, int *outside);
+/* result[0] = sum_i a[i] b[i] (device arrays, FP64, fixed summation order). */
+int nrgpu_dot(const double *a, const double *b, long long n, double *scratch, int scratch_len, double *result);
+
 /* --------------------------------------------------------- diagnostics */
 /* Sum over interior points of f^2 (and of 1) for gridfunction `gf` of an
  * FP64 array, FP64 accumulation; result[0] = sum f^2, result[1] = count.

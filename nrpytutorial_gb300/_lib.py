@@ -103,6 +103,17 @@ _PROTOS = {
                                   P(MoL_gridfunctions), C.c_double, C.c_int, P(C.c_double)]),
     "nrgpu_l2_norm_sq": (C.c_int, [P(paramstruct), vp, C.c_int, vp, C.c_int, vp]),
     "nrgpu_l2_norm_sq_static": (C.c_int, [P(paramstruct), vp, C.c_int, vp]),
+    "Maxwell_rhs_eval_adjoint": (C.c_int, [P(paramstruct), vp, vp]),
+    "apply_bcs_curvilinear_adjoint": (C.c_int, [P(paramstruct), P(bc_struct), C.c_int, P(C.c_int8), vp]),
+    "MoL_adjoint_step_backward": (C.c_int, [C.c_int, P(paramstruct), P(bc_struct), vp, vp, vp, C.c_double]),
+    "Maxwell_initial_data_toroidal_dipole": (C.c_int, [P(paramstruct), C.c_double, C.c_double, C.c_double,
+                                                       vp, vp, vp]),
+    "nrgpu_sphere_sample": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_double,
+                                      vp, vp]),
+    "nrgpu_sphere_sample_adjoint": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp, vp, C.c_int,
+                                              C.c_double, vp, vp]),
+    "nrgpu_sphere_check": (C.c_int, [P(paramstruct), P(C.c_int)]),
+    "nrgpu_dot": (C.c_int, [vp, vp, C.c_longlong, vp, C.c_int, vp]),
     "nrgpu_batch_create": (C.c_int, [C.c_int, P(C.c_int), C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                      C.c_double, C.c_double, C.c_double, C.c_int, P(vp)]),
     "nrgpu_batch_free": (C.c_int, [vp]),

@@ -278,6 +278,78 @@ int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, 
   return NRGPU_OK;
 }
 
+// ------------------------------------------------------------- adjoint
+// Transpose of apply_bcs_curvilinear (FP64): the phases in reverse order;
+// each ghost point hands its adjoint to the points it was computed from and
+// is zeroed.  Sources are updated with atomicAdd (several ghost points of a
+// parity phase can share a source; the outer faces of one phase never do,
+// so Cartesian grids give the same bits every run).
+__global__ void bc_outer_adjoint_kernel(const int *__restrict__ dest, const int *__restrict__ step, int npts,
+                                        int ngfs, long long ntot, double *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  double *f = gfs + (long long)gf * ntot;
+  const long long d = dest[p], s = step[p];
+  const double v = f[d];
+  f[d] = 0.0;
+  atomicAdd(f + d + s, 3.0 * v);
+  atomicAdd(f + d + 2 * s, -3.0 * v);
+  atomicAdd(f + d + 3 * s, v);
+}
+
+__global__ void bc_inner_adjoint_kernel(const int *__restrict__ dest, const int *__restrict__ src,
+                                        const int *__restrict__ parity, int npts, int ngfs, long long ntot,
+                                        ParityTypes types, double *gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  double *f = gfs + (long long)gf * ntot;
+  const bool neg = (parity[p] >> types.t[gf]) & 1;
+  const double v = f[dest[p]];
+  f[dest[p]] = 0.0;
+  atomicAdd(f + src[p], neg ? -v : v);
+}
+
+int apply_bcs_adjoint_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
+                           double *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL argument");
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64, "NUM_GFS %d out of range", NUM_GFS);
+  NRGPU_REQUIRE(bc->NGHOSTS == p->NGHOSTS, "bcstruct built for NGHOSTS=%d, params say %d", bc->NGHOSTS,
+                p->NGHOSTS);
+  ParityTypes types;
+  memset(&types, 0, sizeof(types));
+  for (int g = 0; g < NUM_GFS; g++) {
+    const int t = gfs_parity ? gfs_parity[g] : 0;
+    NRGPU_REQUIRE(t >= 0 && t <= 9, "parity type %d of gf %d not in 0..9", t, g);
+    types.t[g] = (int8_t)t;
+  }
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  const int B = 128;
+  for (int g = bc->NGHOSTS - 1; g >= 0; g--) {
+    const int n = bc->num_ib_gz_pts[g];
+    if (n > 0) {
+      const int a = bc->ib_start[g];
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_inner_adjoint_kernel<<<grid, B, 0, stream()>>>(bc->inner_dest + a, bc->inner_src + a,
+                                                        bc->inner_parity + a, n, NUM_GFS, ntot, types, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+    for (int d = 2; d >= 0; d--) {
+      const int a = bc->ob_dir_start[g][d], b = bc->ob_dir_start[g][d + 1];
+      const int m = b - a;
+      if (m <= 0) continue;
+      dim3 grid((m + B - 1) / B, NUM_GFS);
+      bc_outer_adjoint_kernel<<<grid, B, 0, stream()>>>(bc->outer_dest + a, bc->outer_step + a, m, NUM_GFS, ntot,
+                                                        gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+  }
+  return NRGPU_OK;
+}
+
 template int apply_bcs_impl<double>(const paramstruct *, const bc_struct *, int, const int8_t *, double *);
 template int apply_bcs_impl<float>(const paramstruct *, const bc_struct *, int, const int8_t *, float *);
 

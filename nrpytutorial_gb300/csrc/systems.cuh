@@ -46,5 +46,9 @@ const int8_t *system_parity(int system);
 // FP64 from the pairs and stored back as pairs.
 int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
                         float2 *gfs);
+// Transpose of the boundary conditions (FP64), in place: ghost adjoints are
+// moved onto their sources and zeroed.
+int apply_bcs_adjoint_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
+                           double *gfs);
 
 }  // namespace nrgpu
