@@ -9,9 +9,15 @@ CFL 0.5.  One step = one RK4 step = 4 RHS evaluations per interior point
 (the reference's gp/s definition, Nxx0*Nxx1*Nxx2*4 per step,
 Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:1165-1166).
 
-  python bench.py [--gpus N --steps K --warmup W]      GB300 arm (FP64 headline)
+  python bench.py [--gpus N --steps K --warmup W]      GB300 arm
   python bench.py --impl reference ...                 the reference's own
       generated C (OpenMP, host cores) on the same workload
+
+`value` is the compensated mixed-precision step (FP32 RHS on FP32 (hi, lo)
+stage pairs, FP64 RK state) with its error against the FP64 run stated in
+the line; the FP64 run, the plain FP32-stage run and the other
+configurations (Cartesian 256^3 FD6, 512 batched ScalarWave evolutions, the
+Maxwell adjoint gradient) are reported beside it.
 
 Prints one JSON line (rank 0).  For N > 1 (torchrun) every rank evolves an
 independent replica ("replicas only": one evolution does not shard here).
@@ -32,12 +38,16 @@ sys.path.insert(0, ROOT)
 W = dict(name="BSSN SinhSpherical 128x64x16 FD4 RK4 Brill-Lindquist", coord="SinhSpherical",
          Nxx=(128, 64, 16), fd=4, ng=3, AMPL=64.0, SINHW=0.2, eta=2.0, CFL=0.5,
          m1=0.5, pos1=(0.0, 0.0, 0.5), m2=0.5, pos2=(0.0, 0.0, -0.5))
-METRIC = "BSSN gridpoint-RHS/s (RK4 step, FP64)"
+METRIC = "BSSN gridpoint-RHS/s (RK4 step), mixed precision at stated error vs FP64"
 UNIT = "gridpoint-RHS/s"
-# Algorithmic bytes per interior point of one BSSN rhs_eval launch (FP64):
-# 24 evolved gfs + 6 RbarDD read once, 24 RHS written once.
+# Algorithmic bytes per interior point of the BSSN rhs kernel in a fused RK4
+# substep 1 (stage input read, RbarDD read, y_n read, running total read and
+# written, stage output written; 24 gfs):
+#   compensated: 24 x 8 (pairs) + 6 x 4 + 24 x 8 + 24 x 16 + 24 x 8 = 984 B
+#   FP64:        24 x 8 + 6 x 8 + 24 x 8 + 24 x 16 + 24 x 8 = 1008 B
+RHS_BYTES_COMP = 24 * 8 + 6 * 4 + 24 * 8 + 24 * 16 + 24 * 8
+RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
-RICCI_BYTES_F64 = (9 + 6) * 8
 
 
 def state_errors(a, b, c0, names):
@@ -166,173 +176,153 @@ def run_gpu(args):
     sampler = ClockSampler(local)
     sampler.start()
 
-    def timed_steps(e, n):
-        ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
-        ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
-        for k in range(n):
-            flush.zero_()                    # evict L2 between timed steps (untimed)
-            ev_s[k].record()
-            e.step(dt)
-            ev_e[k].record()
-        torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in zip(ev_s, ev_e)) / 1e3
-
     def timed_replays(replay, n):
         ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
         ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
         for k in range(n):
-            flush.zero_()
+            flush.zero_()                    # evict L2 between timed steps (untimed)
             ev_s[k].record()
             replay()
             ev_e[k].record()
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in zip(ev_s, ev_e)) / 1e3
 
-    # ---- FP64 headline: one RK4 step captured in a CUDA graph, replayed K times
-    for _ in range(Wm):
-        ev.step(dt)
-    ev.y_n.copy_(y0)
-    l0 = lib.nrgpu_kernel_launch_count()
-    ev.step(dt)
-    launches_per_step = lib.nrgpu_kernel_launch_count() - l0
-    ev.y_n.copy_(y0)
-    t_eager = timed_steps(ev, K)          # eager launches, for reference
-    ev.y_n.copy_(y0)
-    replay = ev.capture(dt, n_steps=1)
-    for _ in range(Wm):
-        replay()
-    ev.y_n.copy_(y0)
-    barrier()
-    t64 = timed_replays(replay, K)
-    launches = launches_per_step * K
-    barrier()
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t64], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t64 = float(tt.item())
-    y64 = ev.y_n.clone()
-    finite = bool(torch.isfinite(y64).all().item())
-    value = world * K * nint * 4 / t64
-
-    # ---- FP32-arithmetic modes against the FP64 run over the same K steps
-    g = W["ng"]
-    H64 = ev.l2_norm(ev.hamiltonian(y64))
-    c0 = y0[:, g:-g, g:-g, g:-g]
-
-    def precision_run(prec):
-        e = Evolution("BSSN", G, precision=prec, device=dev)
+    def run(e):
+        """K graph-replayed RK4 steps from y0 after Wm warm-up steps; returns
+        (seconds, kernel launches per step)."""
         for _ in range(Wm):
-            e.y_n.copy_(y0)
             e.step(dt)
         e.y_n.copy_(y0)
-        rep = e.capture(dt, n_steps=1)
+        l0 = lib.nrgpu_kernel_launch_count()
+        e.step(dt)
+        lps = lib.nrgpu_kernel_launch_count() - l0
+        replay = e.capture(dt, n_steps=1)
+        for _ in range(Wm):
+            replay()
         e.y_n.copy_(y0)
-        torch.cuda.synchronize()
-        t = timed_replays(rep, K)
-        res = {"value": world * K * nint * 4 / t, "unit": UNIT, "ms_per_step": t / K * 1e3,
-               "speedup_vs_fp64": t64 / t, "after_steps": K}
-        res.update(state_errors(e.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names))
-        res["H_l2_fp64"] = H64
-        res["H_l2"] = e.l2_norm(ev.hamiltonian(e.y_n))
-        return e, res
+        barrier()
+        t = timed_replays(replay, K)
+        barrier()
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([t], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        return t, lps
 
-    ev32, mixed = precision_run("mixed")
-    del ev32
-    evc, comp = precision_run("compensated")
-    del evc
+    def kernel_time(fn, reps=20):
+        ts = []
+        for r in range(reps + 3):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            if r >= 3:
+                ts.append(a.elapsed_time(b) / 1e3)
+        return float(np.mean(ts))
 
-    # ---- dominant kernels alone: rhs_eval and Ricci_eval (plain stores)
-    aux = torch.zeros((6,) + G.shape, dtype=torch.float64, device=dev)
-    rhs = torch.zeros_like(y0)
-    R = 20
-    times = {"rhs": [], "ricci": []}
-    for r in range(R + 3):
-        flush.zero_()
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        e0.record()
-        ev.ricci_eval(y0, aux)
-        e1.record()
-        flush.zero_()
-        e3 = torch.cuda.Event(enable_timing=True)
-        e3.record()
-        _rhs_only(ev, y0, aux, rhs)
-        e2.record()
-        torch.cuda.synchronize()
-        if r >= 3:
-            times["ricci"].append(e0.elapsed_time(e1) / 1e3)
-            times["rhs"].append(e3.elapsed_time(e2) / 1e3)
-    t_rhs = float(np.mean(times["rhs"]))
-    t_ric = float(np.mean(times["ricci"]))
-    # FP32 rhs kernel alone
-    y32 = y0.float()
-    aux32 = torch.zeros((6,) + G.shape, dtype=torch.float32, device=dev)
-    rhs32 = torch.zeros_like(y32)
-    ev32 = Evolution("BSSN", G, precision="mixed", device=dev)
-    ev32.ricci_eval(y32, aux32)
-    t32k = []
-    for r in range(R + 3):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        _rhs_only(ev32, y32, aux32, rhs32)
-        e1.record()
-        torch.cuda.synchronize()
-        if r >= 3:
-            t32k.append(e0.elapsed_time(e1) / 1e3)
-    t_rhs32 = float(np.mean(t32k))
+    # ---- FP64 (parity mode)
+    t64, lps64 = run(ev)
+    y64 = ev.y_n.clone()
+    H64 = ev.l2_norm(ev.hamiltonian(y64))
+    g = W["ng"]
+    c0 = y0[:, g:-g, g:-g, g:-g]
+
+    # ---- headline: compensated mixed precision
+    evc = Evolution("BSSN", G, precision="compensated", device=dev)
+    tc, lps = run(evc)
+    finite = bool(torch.isfinite(evc.y_n).all().item())
+    comp_err = state_errors(evc.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names)
+    Hc = ev.l2_norm(ev.hamiltonian(evc.y_n))
+    value = world * K * nint * 4 / tc
+    launches = lps * K
+
+    # ---- plain FP32 stage buffers, for comparison
+    evm = Evolution("BSSN", G, precision="mixed", device=dev)
+    tm, _ = run(evm)
+    mix_err = state_errors(evm.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names)
+    Hm = ev.l2_norm(ev.hamiltonian(evm.y_n))
+    del evm
+
+    # ---- the step's kernels alone (substep 1, fused RK update, after a step)
+    evc.y_n.copy_(y0)
+    evc.step(dt)
+    t_ric_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 1))
+    t_rhs_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 2))
+    ev.y_n.copy_(y0)
+    ev.step(dt)
+    t_ric_64 = kernel_time(lambda: ev.substep_rhs(dt, 1, 1))
+    t_rhs_64 = kernel_time(lambda: ev.substep_rhs(dt, 1, 2))
 
     # ---- end to end through the C ABI with host buffers (H2D + step + D2H per step)
     host = torch.empty(y0.shape, dtype=torch.float64, pin_memory=True)
     host.copy_(y0.cpu())
     hn = host.numpy()
-    ev.evolve_host(hn, dt, 1)  # warm
+    evc.evolve_host(hn, dt, 1)  # warm
     host.copy_(y0.cpu())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
-        ev.evolve_host(hn, dt, 1)
+        evc.evolve_host(hn, dt, 1)
     te2e = time.perf_counter() - t0
     clocks = sampler.stop()
 
     hbm, src = peaks()
-    achieved = nint * RHS_BYTES_F64 / t_rhs / 1e9
+    achieved = nint * RHS_BYTES_COMP / t_rhs_c / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
-        "ms_per_step": t64 / K * 1e3, "ms_per_step_eager": t_eager / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic: Brill-Lindquist initial data computed on the GPU",
+        "ms_per_step": tc / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 RHS on compensated f32 (hi,lo) stage pairs; f64 RK state",
+        "data": "synthetic: Brill-Lindquist initial data computed on the GPU",
         "config": {"workload": W["name"], "Nxx": list(W["Nxx"]), "NGHOSTS": W["ng"], "FD_order": W["fd"],
-                   "AMPL": W["AMPL"], "SINHW": W["SINHW"], "eta": W["eta"], "CFL": W["CFL"], "dt": dt,
                    "interior_points": nint, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed (256 MB write) before every timed step",
-                   "launch": "each step replays a CUDA graph of its %d kernel launches" % launches_per_step},
+                   "launch": "each step replays a CUDA graph of its %d kernel launches" % lps},
+        "error_vs_fp64": {"after_steps": K, "state_rel_l2": comp_err["state_rel_l2"],
+                          "max_rel_l2_significant_fields": comp_err["max_rel_l2_significant_fields"],
+                          "max_rel_max_significant_fields": comp_err["max_rel_max_significant_fields"],
+                          "H_l2_fp64": H64, "H_l2": Hc},
         "gpu_launches": int(launches),
         "state_finite": finite,
         "e2e": {"value": world * K * nint * 4 / te2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
-                "path": "MoL_evolve_host (C ABI), pinned host state, 1 step per call"},
-        "roofline": {"bound": "hbm", "kernel": "bssn rhs_kernel FP64 (plain rhs_eval)",
+                "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call"},
+        "roofline": {"bound": "hbm", "kernel": "bssn rhs_kernel, compensated (FP32 pairs in/out, fused RK4 "
+                                               "substep 1)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": None,
-                     "bytes_per_point": RHS_BYTES_F64, "launch_ms": t_rhs * 1e3,
-                     "note": "FP64 BSSN is FP64-ALU bound on GB300; the HBM fraction is reported as asked"},
-        "kernels_ms": {"rhs_f64": t_rhs * 1e3, "ricci_f64": t_ric * 1e3, "rhs_f32": t_rhs32 * 1e3,
-                       "ricci_f64_GBps": nint * RICCI_BYTES_F64 / t_ric / 1e9,
-                       "rhs_f32_GBps": nint * RHS_BYTES_F64 / 2 / t_rhs32 / 1e9},
-        "mixed": mixed,
-        "compensated": comp,
+                     "peak_source": src, "traffic": None, "bytes_per_point": RHS_BYTES_COMP,
+                     "launch_ms": t_rhs_c * 1e3,
+                     "note": "the kernel is FP32-issue/latency bound (255 registers, 12.5% occupancy); "
+                             "HBM fraction reported as asked"},
+        "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3},
+                       "fp64": {"ricci": t_ric_64 * 1e3, "rhs": t_rhs_64 * 1e3}},
+        "fp64": {"value": world * K * nint * 4 / t64, "unit": UNIT, "ms_per_step": t64 / K * 1e3,
+                 "launches_per_step": lps64, "H_l2": H64,
+                 "rhs_kernel_GBps": nint * RHS_BYTES_F64_FUSED / t_rhs_64 / 1e9,
+                 "note": "FP64 BSSN is FP64-pipe bound on GB300 (FP32:FP64 = 64:1)"},
+        "speedup_vs_fp64": t64 / tc,
+        "mixed_fp32_stages": {"value": world * K * nint * 4 / tm, "ms_per_step": tm / K * 1e3,
+                              "speedup_vs_fp64": t64 / tm, "state_rel_l2": mix_err["state_rel_l2"],
+                              "max_rel_l2_significant_fields": mix_err["max_rel_l2_significant_fields"],
+                              "H_l2": Hm},
+        "compensated_fields": {k: {"rel_l2": v["rel_l2"], "rel_max": v["rel_max"]}
+                               for k, v in comp_err["fields"].items() if v["significant"]},
         "clocks": clocks,
     }
+    del evc
+    torch.cuda.empty_cache()
     if args.config3_steps > 0:
-        del ev32, aux, rhs, y32, aux32, rhs32
-        torch.cuda.empty_cache()
         out["mixed_cartesian_256"] = run_config3(dev, args.config3_steps, flush)
+        torch.cuda.empty_cache()
     if args.config4_steps > 0:
-        torch.cuda.empty_cache()
         out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush)
-    if args.config5_steps > 0:
         torch.cuda.empty_cache()
-        out["adjoint_maxwell_128"] = run_config5(dev, args.config5_steps)
+    if args.config5_steps > 0:
+        a5 = run_config5(dev, args.config5_steps)
+        out["adjoint_maxwell_128"] = a5
+        out["adjoint_over_forward"] = a5["adjoint_over_forward"]
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:

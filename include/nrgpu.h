@@ -259,6 +259,13 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
  * kernel, LOOP_ALL_GFS_GPS update over all points, BCs, rescale. */
 int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *params,
                                      const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
+/* The RHS kernel(s) of one substep of MoL_step_forward_in_time alone, with
+ * the substep's fused RK update and no boundary conditions; for timing and
+ * profiling a step's dominant kernel.  which: 0 every RHS kernel of the
+ * substep, 1 BSSN Ricci_eval only, 2 BSSN rhs_eval only.  The buffers must
+ * hold a previous step's values (e.g. after one full step). */
+int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *params, MoL_gridfunctions *gfs,
+                    int stage, double dt, int which);
 /* Host-buffer form for callers whose state lives in host memory: copies
  * y_n_gfs (host, FP64, pinned or pageable) to gfs->y_n_gfs, runs n_steps
  * steps, copies the state back, and synchronises the stream. */

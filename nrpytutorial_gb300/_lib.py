@@ -99,6 +99,8 @@ _PROTOS = {
                                            P(MoL_gridfunctions), C.c_double]),
     "MoL_step_forward_in_time_unfused": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),
                                                    P(MoL_gridfunctions), C.c_double]),
+    "MoL_substep_rhs": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(MoL_gridfunctions), C.c_int,
+                                  C.c_double, C.c_int]),
     "MoL_evolve_host": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),
                                   P(MoL_gridfunctions), C.c_double, C.c_int, P(C.c_double)]),
     "nrgpu_l2_norm_sq": (C.c_int, [P(paramstruct), vp, C.c_int, vp, C.c_int, vp]),

@@ -200,6 +200,33 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
   return NRGPU_OK;
 }
 
+int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL_gridfunctions *gfs, int stage,
+                    double dt, int which) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(system_num_gfs(system) > 0 && gfs, "bad arguments");
+  NRGPU_REQUIRE(stage >= 0 && stage <= 3, "stage %d not in 0..3", stage);
+  NRGPU_REQUIRE(which >= 0 && which <= 2, "which %d not in 0..2", which);
+  NRGPU_REQUIRE(which == 0 || system == NRGPU_SYS_BSSN, "which = 1, 2 select BSSN's two kernels");
+  const bool f64 = gfs->precision == NRGPU_PREC_FP64;
+  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
+  void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  StageArgs a{};
+  a.stage = stage;
+  a.dt = dt;
+  a.prec = gfs->precision;
+  a.in = (stage == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
+                      : (const void *)kbuf[(stage + 1) % 2];
+  a.in_is_f64 = !pair && ((stage == 0) || f64);
+  a.y_n = gfs->y_n_gfs;
+  a.rt = gfs->y_nplus1_running_total_gfs;
+  a.out = (stage == 3) ? nullptr : kbuf[stage % 2];
+  a.auxevol = gfs->auxevol_gfs;
+  if (which == 1) return bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
+  if (which == 2) return bssn_rhs_launch(rfm, p, a);
+  return rhs_stage(system, rfm, p, a);
+}
+
 int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *p,
                                      const bc_struct *bc, MoL_gridfunctions *gfs, double dt) {
   int st = check_step_args(system, rfm, p, bc, gfs);

@@ -111,6 +111,14 @@ class Evolution:
         replay.graph = g
         return replay
 
+    def substep_rhs(self, dt, stage=1, which=0):
+        """One substep's RHS kernel(s) with the fused RK update, no BCs
+        (timing and profiling; run a full step first)."""
+        self._sync_stream()
+        _lib.check(self.lib.MoL_substep_rhs(self.sys_id, self._rfm(), C.byref(self.grid.params),
+                                            C.byref(self.gfs), int(stage), float(dt), int(which)),
+                   "MoL_substep_rhs")
+
     def evolve_host(self, y_host, dt, n_steps):
         """Host-buffer evolution: y_host (numpy float64, IDX4S) in, state out."""
         self._sync_stream()
