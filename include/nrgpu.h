@@ -301,11 +301,15 @@ int nrgpu_batch_set_timesteps(nrgpu_batch *batch, const double *dt);
 int nrgpu_batch_initial_data_gaussian(nrgpu_batch *batch, const double *A, const double *r0,
                                       const double *w, double *y_n_gfs);
 /* RHS of every instance at interior points (FP64: double in/out; MIXED:
- * float in/out, FP32 arithmetic). */
+ * float in/out; COMPENSATED: float2 (hi, lo) pairs in, (rhs, 0) pairs out;
+ * FP32 arithmetic unless FP64). */
 int nrgpu_batch_rhs_eval(nrgpu_batch *batch, const void *in_gfs, void *rhs_gfs);
-int nrgpu_batch_apply_bcs(nrgpu_batch *batch, void *gfs, int is_f64);
+/* Boundary conditions of every instance; kind 0: float, 1: double, 2: float2 pairs. */
+int nrgpu_batch_apply_bcs(nrgpu_batch *batch, void *gfs, int kind);
 /* One RK4 step of every instance; gfs->precision must equal the batch's.
- * MIXED: FP32 RHS and FP32 stage buffers, FP64 y_n and running total.
+ * MIXED: FP32 RHS and FP32 stage buffers, FP64 y_n and running total;
+ * COMPENSATED: stage buffers of FP32 pairs (2 floats per value), as in
+ * MoL_step_forward_in_time.
  * Neither allocates nor synchronises (graph-capturable). */
 int nrgpu_batch_step(nrgpu_batch *batch, MoL_gridfunctions *gfs);
 /* Tile autotuner: times the RHS launch for each built tile shape (TX along

@@ -21,7 +21,7 @@ class ScalarWaveBatch:
                  wavespeed=1.0, CFL_FACTOR=0.5, precision="mixed", device="cuda"):
         self.lib = _lib.load()
         if precision not in _lib.PREC:
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+            raise ValueError("precision must be one of %s" % sorted(_lib.PREC))
         self.Nr = [int(n) for n in Nr]
         self.ninst = len(self.Nr)
         self.precision = precision
@@ -49,8 +49,10 @@ class ScalarWaveBatch:
         z = dict(device=self.device)
         self.y_n = torch.zeros(self.total, dtype=torch.float64, **z)
         self.rt = torch.zeros(self.total, dtype=torch.float64, **z)
-        self.k_odd = torch.zeros(self.total, dtype=stage, **z)
-        self.k_even = torch.zeros(self.total, dtype=stage, **z)
+        # compensated: stage buffers of FP32 (hi, lo) pairs
+        kshape = (self.total, 2) if precision == "compensated" else (self.total,)
+        self.k_odd = torch.zeros(kshape, dtype=stage, **z)
+        self.k_even = torch.zeros(kshape, dtype=stage, **z)
         self.gfs = _lib.MoL_gridfunctions(_lib.PREC[precision], self.y_n.data_ptr(), self.rt.data_ptr(),
                                           self.k_odd.data_ptr(), self.k_even.data_ptr(), None)
         self.steps_taken = 0
@@ -75,7 +77,7 @@ class ScalarWaveBatch:
         buf = self.y_n if buf is None else buf
         n0, n1, n2 = (int(v) for v in self.dims[i])
         b, n = int(self.base[i]), int(self.ntot[i])
-        return buf[b:b + 2 * n].view(2, n2, n1, n0)
+        return buf[b:b + 2 * n].view((2, n2, n1, n0) + tuple(buf.shape[1:]))
 
     def interior_points(self):
         """Interior grid points summed over instances (one RK4 step updates each once)."""
@@ -101,7 +103,13 @@ class ScalarWaveBatch:
         """Chooses the RHS tile shape and persistent grid size by timing;
         returns (tx, ty, grid, ms)."""
         self._sync_stream()
-        src = self.y_n if self.precision == "fp64" else self.y_n.to(torch.float32)
+        if self.precision == "fp64":
+            src = self.y_n
+        elif self.precision == "compensated":
+            hi = self.y_n.to(torch.float32)
+            src = torch.stack([hi, (self.y_n - hi.double()).to(torch.float32)], dim=-1).contiguous()
+        else:
+            src = self.y_n.to(torch.float32)
         ms = C.c_float()
         _lib.check(self.lib.nrgpu_batch_autotune(self.handle, _lib.ptr(src), _lib.ptr(self.k_odd), int(reps),
                                                  C.byref(ms)), "nrgpu_batch_autotune")
@@ -124,8 +132,8 @@ class ScalarWaveBatch:
 
     def apply_bcs(self, gfs):
         self._sync_stream()
-        _lib.check(self.lib.nrgpu_batch_apply_bcs(self.handle, _lib.ptr(gfs), int(gfs.dtype == torch.float64)),
-                   "nrgpu_batch_apply_bcs")
+        kind = 1 if gfs.dtype == torch.float64 else (2 if gfs.dim() == 2 and gfs.shape[-1] == 2 else 0)
+        _lib.check(self.lib.nrgpu_batch_apply_bcs(self.handle, _lib.ptr(gfs), kind), "nrgpu_batch_apply_bcs")
 
     def step(self):
         """One RK4 step of every instance, each with its own time step."""

@@ -1,7 +1,7 @@
 // batch.cu -- many independent small ScalarWave evolutions (curvilinear,
 // ragged grid sizes) advanced together: one persistent launch per RK4
-// substep covers every instance, and one launch per boundary phase covers
-// every instance's ghost zones.
+// substep covers every instance, and one launch per boundary-condition
+// application covers every instance's ghost zones.
 //
 // Physics per instance is exactly the single-grid path: the curvilinear
 // ScalarWave RHS (ScalarWave/ScalarWaveCurvilinear_RHSs.py:43-98), FD4, the
@@ -13,10 +13,14 @@
 // list of (instance, i2, i1-block) items; a persistent grid walks the list
 // with a fixed stride, so instances of any size share one launch.  The item
 // shape (TX threads along i0, TY rows of i1) is chosen by a timing autotuner.
+// Boundary conditions: one launch per application, one block per instance,
+// which walks that instance's ghost-layer phases in the reference's order
+// with a block barrier between phases (instances do not depend on each other).
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "epilogue.cuh"
@@ -40,6 +44,7 @@ struct BatchInstance {
 };
 
 constexpr int kBatchNG = 2;     // FD4 ScalarWave ghost zones
+constexpr int kBatchPhases = 4 * kBatchNG;  // per layer: outer i0, i1, i2, inner
 constexpr int kBatchTab = 6;    // ghatUU0..2, contracted Gammahat^0..2
 
 struct BatchWork {
@@ -50,7 +55,7 @@ struct BatchWork {
 template <typename R, typename Tin, typename TStage, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY)
     sw_batch_rhs_kernel(const BatchInstance *__restrict__ insts, const BatchWork *__restrict__ work, int nwork,
-                        const Tin *__restrict__ in, const R *__restrict__ tab, R c2, RKEpilogue<TStage> epi) {
+                        typename InRef<Tin>::type in, const R *__restrict__ tab, R c2, RKEpilogue<TStage> epi) {
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const BatchWork it = work[w];
     const BatchInstance I = insts[it.inst];
@@ -62,8 +67,8 @@ __global__ void __launch_bounds__(TX *TY)
     const long long plane = (long long)I.n0 * I.n1;
     for (int i0 = kBatchNG + threadIdx.x; i0 < I.n0 - kBatchNG; i0 += TX) {
       const long long idx = i0 + I.n0 * ((long long)i1 + (long long)I.n1 * i2);
-      const Tin *uu = in + I.base + idx;
-      const R vv = (R)__ldg(in + I.base + I.ntot + idx);
+      const auto uu = in + I.base + idx;
+      const R vv = val<R>(in + I.base + I.ntot + idx);
       const R *t = tab + I.tab + (long long)i1 * I.n0 + i0;
       R lap = (R)0;
 #pragma unroll
@@ -133,31 +138,44 @@ __global__ void sw_batch_gaussian_kernel(const BatchInstance *__restrict__ insts
   }
 }
 
-// Batched boundary conditions: per ghost layer and phase, one launch over the
-// points of every instance (both gridfunctions per thread).
-template <typename T>
-__global__ void sw_batch_bc_outer(const long long *__restrict__ dest, const int *__restrict__ step,
-                                  const long long *__restrict__ gfstride, int n, T *gfs) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const long long s = step[p];
-#pragma unroll
-  for (int g = 0; g < 2; g++) {
-    T *f = gfs + dest[p] + g * gfstride[p];
-    T v;
-    if constexpr (sizeof(T) == 8) v = __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[s]), __dmul_rn(3.0, f[2 * s])), f[3 * s]);
-    else v = __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[s]), __fmul_rn(3.0f, f[2 * s])), f[3 * s]);
-    *f = v;
-  }
+// Batched boundary conditions: block `inst` applies instance inst's ghost
+// phases (per layer: outer faces along i0, i1, i2, then inner points) in
+// order.  Offsets a (dest) and b (outer: signed step; inner: src) are
+// relative to the instance's first point; both gridfunctions per thread.
+template <typename T> __device__ __forceinline__ T bc_extrapolate(const T *f, long long s) {
+  if constexpr (std::is_same<T, double>::value)
+    return __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[s]), __dmul_rn(3.0, f[2 * s])), f[3 * s]);
+  else if constexpr (std::is_same<T, float>::value)
+    return __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[s]), __fmul_rn(3.0f, f[2 * s])), f[3 * s]);
+  else  // FP32 pairs: the rule on the FP64 values, re-split
+    return split_pair(__dadd_rn(__dsub_rn(__dmul_rn(3.0, pair_value(f[s])), __dmul_rn(3.0, pair_value(f[2 * s]))),
+                                pair_value(f[3 * s])));
 }
 
 template <typename T>
-__global__ void sw_batch_bc_inner(const long long *__restrict__ dest, const long long *__restrict__ src,
-                                  const long long *__restrict__ gfstride, int n, T *gfs) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+__global__ void sw_batch_bc_kernel(const BatchInstance *__restrict__ insts, const int *__restrict__ phases,
+                                   const int *__restrict__ a, const int *__restrict__ b, T *gfs) {
+  const BatchInstance I = insts[blockIdx.x];
+  T *f = gfs + I.base;
+  const int *ph = phases + (long long)blockIdx.x * (kBatchPhases + 1);
+  for (int q = 0; q < kBatchPhases; q++) {
+    const bool inner = (q % 4) == 3;
+    for (int p = ph[q] + threadIdx.x; p < ph[q + 1]; p += blockDim.x) {
+      const long long d = a[p], e = b[p];
 #pragma unroll
-  for (int g = 0; g < 2; g++) gfs[dest[p] + g * gfstride[p]] = gfs[src[p] + g * gfstride[p]];  // scalars: parity +1
+      for (int g = 0; g < 2; g++) {
+        T *fg = f + g * I.ntot;
+        fg[d] = inner ? fg[e] : bc_extrapolate(fg + d, e);  // scalars: parity +1
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// y_n -> FP32 (hi, lo) pairs over all packed points.
+__global__ void sw_batch_split_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = split_pair(y[i]);
 }
 
 }  // namespace nrgpu
@@ -175,24 +193,20 @@ struct nrgpu_batch {
   int nwork[4] = {0, 0, 0, 0};
   double *d_tab64 = nullptr;
   float *d_tab32 = nullptr;
-  // boundary phases: per layer g (2) x {outer d0, d1, d2, inner}
-  long long *d_bc_dest[8] = {}, *d_bc_src[8] = {}, *d_bc_gfs[8] = {};
-  int *d_bc_step[8] = {};
-  int bc_n[8] = {};
+  // boundary phases: per instance, kBatchPhases+1 offsets into a/b
+  int *d_bc_phases = nullptr, *d_bc_a = nullptr, *d_bc_b = nullptr;
   // tuned launch shape
   int tx = 64, tyi = 1, grid = 0;
+  int bc_threads = 256;  // block size of the boundary-condition kernel
 };
 
 static void batch_destroy(nrgpu_batch *b) {
   if (!b) return;
   cudaFree(b->d_insts);
   for (int t = 0; t < 4; t++) cudaFree(b->d_work[t]);
-  for (int ph = 0; ph < 8; ph++) {
-    cudaFree(b->d_bc_dest[ph]);
-    cudaFree(b->d_bc_src[ph]);
-    cudaFree(b->d_bc_gfs[ph]);
-    cudaFree(b->d_bc_step[ph]);
-  }
+  cudaFree(b->d_bc_phases);
+  cudaFree(b->d_bc_a);
+  cudaFree(b->d_bc_b);
   cudaFree(b->d_tab64);
   cudaFree(b->d_tab32);
   delete b;
@@ -207,7 +221,8 @@ static int batch_launch_rhs(nrgpu_batch *b, const void *in, bool in_f64, int sta
   const int nwork = b->nwork[b->tyi];
 #define LAUNCH(R, Tin, TS, TX, TY)                                                                          \
   sw_batch_rhs_kernel<R, Tin, TS, TX, TY><<<grid, dim3(TX, TY), 0, stream()>>>(                            \
-      b->d_insts, work, nwork, (const Tin *)in, (const R *)(sizeof(R) == 8 ? (const void *)b->d_tab64      \
+      b->d_insts, work, nwork, (typename InRef<Tin>::type)in,                                               \
+      (const R *)(sizeof(R) == 8 ? (const void *)b->d_tab64                                                 \
                                                                             : (const void *)b->d_tab32),    \
       (R)b->c2, RKEpilogue<TS>{stage, 0.0, 0, y_n, rt, (TS *)out})
 #define SHAPES(R, Tin, TS)                                                   \
@@ -225,6 +240,8 @@ static int batch_launch_rhs(nrgpu_batch *b, const void *in, bool in_f64, int sta
   }
   if (b->prec == NRGPU_PREC_FP64) {
     SHAPES(double, double, double)
+  } else if (b->prec == NRGPU_PREC_COMPENSATED) {
+    SHAPES(float, Pair32, float2)
   } else if (in_f64) {
     SHAPES(float, double, float)
   } else {
@@ -237,16 +254,9 @@ static int batch_launch_rhs(nrgpu_batch *b, const void *in, bool in_f64, int sta
 }
 
 template <typename T> static int batch_bcs(nrgpu_batch *b, T *gfs) {
-  for (int ph = 0; ph < 8; ph++) {
-    const int n = b->bc_n[ph];
-    if (n == 0) continue;
-    const int B = 128;
-    if (ph % 4 < 3)
-      sw_batch_bc_outer<T><<<(n + B - 1) / B, B, 0, stream()>>>(b->d_bc_dest[ph], b->d_bc_step[ph], b->d_bc_gfs[ph], n, gfs);
-    else
-      sw_batch_bc_inner<T><<<(n + B - 1) / B, B, 0, stream()>>>(b->d_bc_dest[ph], b->d_bc_src[ph], b->d_bc_gfs[ph], n, gfs);
-    NRGPU_LAUNCH_CHECK();
-  }
+  sw_batch_bc_kernel<T><<<b->ninst, b->bc_threads, 0, stream()>>>(b->d_insts, b->d_bc_phases, b->d_bc_a, b->d_bc_b,
+                                                                  gfs);
+  NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
 
@@ -257,7 +267,9 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
   NRGPU_REQUIRE(out && Nr && ninst >= 1, "bad arguments");
   NRGPU_REQUIRE(CoordSystem == NRGPU_COORD_SPHERICAL || CoordSystem == NRGPU_COORD_SINHSPHERICAL,
                 "batched ScalarWave needs a Spherical-family CoordSystem");
-  NRGPU_REQUIRE(precision == NRGPU_PREC_FP64 || precision == NRGPU_PREC_MIXED, "bad precision");
+  NRGPU_REQUIRE(precision == NRGPU_PREC_FP64 || precision == NRGPU_PREC_MIXED ||
+                    precision == NRGPU_PREC_COMPENSATED,
+                "bad precision");
   NRGPU_REQUIRE(ninst <= 65535, "at most 65535 instances (grid y dimension)");
   nrgpu_batch *b = new nrgpu_batch();
   b->ninst = ninst;
@@ -272,8 +284,7 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
   long long base = 0, tab = 0;
   std::vector<BatchWork> work[4];
   const int TYs[4] = {1, 2, 4, 8};
-  std::vector<long long> bdest[8], bsrc[8], bgfs[8];
-  std::vector<int> bstep[8];
+  std::vector<int> bphase, ba, bb;  // per-instance phase offsets; dest; step or src
   for (int i = 0; i < ninst; i++) {
     paramstruct p{};
     p.CoordSystem = CoordSystem;
@@ -327,19 +338,26 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
       batch_destroy(b);
       return st;
     }
+    if (I.ntot > 0x7fffffffLL) {
+      batch_destroy(b);
+      set_error("instance %d has more than 2^31 points", i);
+      return NRGPU_ERR_SIZE;
+    }
     for (int g = 0; g < kBatchNG; g++) {
-      for (int d = 0; d < 3; d++)
+      for (int d = 0; d < 3; d++) {
+        bphase.push_back((int)ba.size());
         for (int k = bc.ob_dir_start[g][d]; k < bc.ob_dir_start[g][d + 1]; k++) {
-          bdest[g * 4 + d].push_back(I.base + od[k]);
-          bstep[g * 4 + d].push_back(os[k]);
-          bgfs[g * 4 + d].push_back(I.ntot);
+          ba.push_back(od[k]);
+          bb.push_back(os[k]);
         }
+      }
+      bphase.push_back((int)ba.size());
       for (int k = bc.ib_start[g]; k < bc.ib_start[g] + bc.num_ib_gz_pts[g]; k++) {
-        bdest[g * 4 + 3].push_back(I.base + id_[k]);
-        bsrc[g * 4 + 3].push_back(I.base + is[k]);
-        bgfs[g * 4 + 3].push_back(I.ntot);
+        ba.push_back(id_[k]);
+        bb.push_back(is[k]);
       }
     }
+    bphase.push_back((int)ba.size());  // end of this instance's last phase
   }
   b->total_points = base;
   auto up = [&](void **dst, const void *src, size_t bytes) -> int {
@@ -360,13 +378,9 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
     b->nwork[t] = (int)work[t].size();
     NRGPU_BATCH_TRY(up((void **)&b->d_work[t], work[t].data(), work[t].size() * sizeof(BatchWork)))
   }
-  for (int ph = 0; ph < 8; ph++) {
-    b->bc_n[ph] = (int)bdest[ph].size();
-    NRGPU_BATCH_TRY(up((void **)&b->d_bc_dest[ph], bdest[ph].data(), bdest[ph].size() * 8))
-    NRGPU_BATCH_TRY(up((void **)&b->d_bc_src[ph], bsrc[ph].data(), bsrc[ph].size() * 8))
-    NRGPU_BATCH_TRY(up((void **)&b->d_bc_gfs[ph], bgfs[ph].data(), bgfs[ph].size() * 8))
-    NRGPU_BATCH_TRY(up((void **)&b->d_bc_step[ph], bstep[ph].data(), bstep[ph].size() * 4))
-  }
+  NRGPU_BATCH_TRY(up((void **)&b->d_bc_phases, bphase.data(), bphase.size() * sizeof(int)))
+  NRGPU_BATCH_TRY(up((void **)&b->d_bc_a, ba.data(), ba.size() * sizeof(int)))
+  NRGPU_BATCH_TRY(up((void **)&b->d_bc_b, bb.data(), bb.size() * sizeof(int)))
   NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab64, tab * sizeof(double)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
   NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab32, tab * sizeof(float)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
 #undef NRGPU_BATCH_TRY
@@ -478,6 +492,31 @@ int nrgpu_batch_autotune(nrgpu_batch *b, const void *in, void *rhs_scratch, int 
     }
     if (st) break;
   }
+  // boundary-condition block size, timed on the scratch buffer's ghost points
+  float best_bc = 1e30f;
+  int bthreads = b->bc_threads;
+  for (int threads : {128, 256, 512, 1024}) {
+    if (st) break;
+    b->bc_threads = threads;
+    auto bcs = [&]() {
+      if (b->prec == NRGPU_PREC_FP64) return batch_bcs<double>(b, (double *)rhs_scratch);
+      if (b->prec == NRGPU_PREC_COMPENSATED) return batch_bcs<float2>(b, (float2 *)rhs_scratch);
+      return batch_bcs<float>(b, (float *)rhs_scratch);
+    };
+    if ((st = bcs())) break;
+    cudaEventRecord(e0, stream());
+    for (int r = 0; r < reps && st == NRGPU_OK; r++) st = bcs();
+    cudaEventRecord(e1, stream());
+    if (st) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) { st = NRGPU_ERR_CUDA; break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms / reps < best_bc) {
+      best_bc = ms / reps;
+      bthreads = threads;
+    }
+  }
+  b->bc_threads = bthreads;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->tx = btx;
@@ -512,28 +551,39 @@ int nrgpu_batch_initial_data_gaussian(nrgpu_batch *b, const double *A, const dou
 
 int nrgpu_batch_rhs_eval(nrgpu_batch *b, const void *in, void *rhs) {
   NRGPU_REQUIRE(b && in && rhs, "NULL argument");
-  return batch_launch_rhs(b, in, b->prec == NRGPU_PREC_FP64, -1, nullptr, nullptr, rhs);
+  return batch_launch_rhs(b, in, b->prec == NRGPU_PREC_FP64, -1, nullptr, nullptr, rhs);  // compensated: pairs
 }
 
-int nrgpu_batch_apply_bcs(nrgpu_batch *b, void *gfs, int is_f64) {
+int nrgpu_batch_apply_bcs(nrgpu_batch *b, void *gfs, int kind) {
   NRGPU_REQUIRE(b && gfs, "NULL argument");
-  return is_f64 ? batch_bcs<double>(b, (double *)gfs) : batch_bcs<float>(b, (float *)gfs);
+  NRGPU_REQUIRE(kind >= 0 && kind <= 2, "kind must be 0 (float), 1 (double) or 2 (float2 pairs)");
+  if (kind == 1) return batch_bcs<double>(b, (double *)gfs);
+  if (kind == 2) return batch_bcs<float2>(b, (float2 *)gfs);
+  return batch_bcs<float>(b, (float *)gfs);
 }
 
 int nrgpu_batch_step(nrgpu_batch *b, MoL_gridfunctions *gfs) {
   NRGPU_REQUIRE(b && gfs && gfs->y_n_gfs && gfs->y_nplus1_running_total_gfs && gfs->k_odd_gfs && gfs->k_even_gfs,
                 "NULL argument");
   NRGPU_REQUIRE(gfs->precision == b->prec, "buffers' precision differs from the batch's");
-  const bool mixed = b->prec == NRGPU_PREC_MIXED;
+  const bool f64 = b->prec == NRGPU_PREC_FP64, pair = b->prec == NRGPU_PREC_COMPENSATED;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   int st;
+  if (pair) {  // substep 0 reads y_n as FP32 pairs from k_even
+    const int blocks = (int)std::min<long long>((b->total_points + 255) / 256, 152LL * 16);
+    sw_batch_split_kernel<<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
+    NRGPU_LAUNCH_CHECK();
+  }
   for (int s = 0; s < 4; s++) {
-    const void *in = (s == 0) ? (const void *)gfs->y_n_gfs : kbuf[(s + 1) % 2];
-    const bool in_f64 = (s == 0) || !mixed;
+    const void *in = (s == 0) ? (pair ? gfs->k_even_gfs : (const void *)gfs->y_n_gfs) : kbuf[(s + 1) % 2];
+    const bool in_f64 = !pair && ((s == 0) || f64);
     void *out = (s == 3) ? nullptr : kbuf[s % 2];
     if ((st = batch_launch_rhs(b, in, in_f64, s, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, out))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
-    if ((st = (s == 3 || !mixed) ? batch_bcs<double>(b, (double *)post) : batch_bcs<float>(b, (float *)post))) return st;
+    if (s == 3 || f64) st = batch_bcs<double>(b, (double *)post);
+    else if (pair) st = batch_bcs<float2>(b, (float2 *)post);
+    else st = batch_bcs<float>(b, (float *)post);
+    if (st) return st;
   }
   return NRGPU_OK;
 }

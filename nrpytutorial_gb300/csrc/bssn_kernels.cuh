@@ -11,9 +11,18 @@ namespace nrgpu {
 namespace bssn {
 
 constexpr int kBlockX = 32, kBlockY = 4;
+// Resident blocks per SM the compiler must allow (caps registers per thread):
+// measured on GB300, the rhs kernel runs fastest at 4 blocks of 128 threads
+// (128 registers, spilling to L1), the Ricci kernel at 1 (255 registers).
+#ifndef NRGPU_BSSN_RICCI_MIN_BLOCKS
+#define NRGPU_BSSN_RICCI_MIN_BLOCKS 1
+#endif
+#ifndef NRGPU_BSSN_RHS_MIN_BLOCKS
+#define NRGPU_BSSN_RHS_MIN_BLOCKS 4
+#endif
 
 template <typename R, typename Tin, int CS, int ORDER, typename TAux>
-__global__ void __launch_bounds__(kBlockX *kBlockY)
+__global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
     ricci_kernel(Grid g, typename InRef<Tin>::type in, const R *__restrict__ tab, TAux *__restrict__ aux) {
   int i0, i1, i2;
   long long idx;
@@ -30,7 +39,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY)
 }
 
 template <typename R, typename Tin, int CS, int ORDER, typename TStage>
-__global__ void __launch_bounds__(kBlockX *kBlockY)
+__global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
     rhs_kernel(Grid g, typename InRef<Tin>::type in, const R *__restrict__ aux, const R *__restrict__ tab,
                R eta, RKEpilogue<TStage> epi) {
   int i0, i1, i2;
