@@ -319,6 +319,7 @@ def run_gpu(args):
     if args.config4_steps > 0:
         out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush)
         torch.cuda.empty_cache()
+    out["convergence_order_H"] = convergence_orders(dev)
     if args.config5_steps > 0:
         a5 = run_config5(dev, args.config5_steps)
         out["adjoint_maxwell_128"] = a5
@@ -472,6 +473,33 @@ def run_config4(dev, K, flush):
     del runs, B64
     torch.cuda.empty_cache()
     return res
+
+
+def convergence_orders(dev):
+    """|H| in 2 < r < 5 after t = 0.2 of Brill-Lindquist data (m = 0.5 at
+    z = +-0.5) on Spherical grids 48x24x4 and 96x48x4 (RMAX 8, FD4): the
+    convergence order log2(|H|_coarse / |H|_fine), FP64 and compensated."""
+    from nrpytutorial_gb300 import Evolution, Grid
+    T, out = 0.2, {}
+    for prec in ("fp64", "compensated"):
+        norms = []
+        for Nr, Nth in ((48, 24), (96, 48)):
+            G = Grid("Spherical", (Nr, Nth, 4), FD_order=4, NGHOSTS=3, RMAX=8.0, eta=2.0)
+            ev = Evolution("BSSN", G, precision=prec, device=dev)
+            ev.initial_data_brill_lindquist(0.5, (0, 0, 0.5), 0.5, (0, 0, -0.5))
+            ev.apply_bcs(ev.y_n)
+            ev.enforce_detgammabar(ev.y_n)
+            n = int(np.ceil(T / G.find_timestep(0.5)))
+            for _ in range(n):
+                ev.step(T / n)
+            H = ev.hamiltonian()[0].cpu().numpy()
+            r = np.asarray(G.xx[0])[None, None, :] * np.ones_like(H)
+            m = np.zeros_like(H, dtype=bool)
+            m[3:-3, 3:-3, 3:-3] = True
+            m &= (r > 2.0) & (r < 5.0)
+            norms.append(float(np.sqrt(np.mean(H[m] ** 2))))
+        out[prec] = {"H_rms_coarse": norms[0], "H_rms_fine": norms[1], "order": float(np.log2(norms[0] / norms[1]))}
+    return out
 
 
 def run_config5(dev, K):

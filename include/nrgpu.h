@@ -234,6 +234,10 @@ int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const paramst
  * (BSSN_constraints.py:19-74; Ricci evaluated inline). */
 int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *params,
                                 const double *in_gfs, double *aux_gfs);
+/* Momentum constraint M^i (rescaled by ReU) at interior points into
+ * aux_gfs[0..2] (BSSN_constraints.py:76-126). */
+int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
+                             const double *in_gfs, double *aux_gfs);
 
 /* --------------------------------------------------------- initial data */
 /* Brill-Lindquist two-puncture data converted to rescaled BSSN variables in

@@ -93,6 +93,7 @@ _PROTOS = {
     "BSSN_enforce_detgammabar_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp]),
     "BSSN_enforce_detgammabar_constraint_f32": (C.c_int, [P(rfm_struct), P(paramstruct), vp]),
     "BSSN_Hamiltonian_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "BSSN_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double),
                                                    C.c_double, P(C.c_double), vp]),
     "MoL_step_forward_in_time": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),

@@ -72,6 +72,22 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
     }
 }
 
+// ------------------------------------------------------ momentum constraint
+template <int CS, int ORDER>
+__global__ void __launch_bounds__(kBlockX *kBlockY)
+    momentum_kernel(Grid g, const double *__restrict__ in, const double *__restrict__ tab, double *__restrict__ aux) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  double MU[3];
+  momentum_point<ORDER, CS, double>(P, rf, inv, MU);
+#pragma unroll
+  for (int k = 0; k < 3; k++) aux[(long long)k * g.ntot + idx] = MU[k];
+}
+
 // --------------------------------------------------- Hamiltonian constraint
 template <int CS, int ORDER>
 __global__ void __launch_bounds__(kBlockX *kBlockY)
@@ -368,6 +384,27 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
       set_error("Hamiltonian: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
       return NRGPU_ERR_UNSUPPORTED;
   }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const double *in, double *aux) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(in && aux, "NULL argument");
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  const double *tab = rfm ? rfm->table64 : nullptr;
+#define MOM(CS, ORD) momentum_kernel<CS, ORD><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux)
+  switch (p->CoordSystem * 16 + p->FD_order) {
+    case NRGPU_COORD_CARTESIAN * 16 + 4: MOM(NRGPU_COORD_CARTESIAN, 4); break;
+    case NRGPU_COORD_CARTESIAN * 16 + 6: MOM(NRGPU_COORD_CARTESIAN, 6); break;
+    case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MOM(NRGPU_COORD_SINHSPHERICAL, 4); break;
+    case NRGPU_COORD_SPHERICAL * 16 + 4: MOM(NRGPU_COORD_SPHERICAL, 4); break;
+    default:
+      set_error("momentum constraint: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
+      return NRGPU_ERR_UNSUPPORTED;
+  }
+#undef MOM
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }

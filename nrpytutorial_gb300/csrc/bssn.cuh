@@ -281,6 +281,80 @@ __device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R
     }
 }
 
+// --------------------------------------------------- momentum constraint
+// M^i = e^{-4 phi}/ReU^i [gammabar^ik gammabar^jl Dbar_j Abar_kl
+//       + 6 Abar^ij d_j phi - 2/3 gammabar^ij d_j K]  (BSSN_constraints.py:76-126;
+// AbarDD_dD from BSSN_quantities.py:247-255; W = e^{-2 phi}).
+template <int ORDER, int CS, typename R, typename Tin>
+__device__ __forceinline__ void momentum_point(const Point<Tin> &P, const Rfm<CS, R> &rf, const R *inv, R MU[3]) {
+  using M = RfmMask<CS>;
+  Metric<CS, R> m;
+  metric_point<ORDER, CS, R>(P, rf, inv, m);
+  const R cf = val<R>(P.gf(CF));
+  R a[3][3], Abar[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      a[i][j] = a[j][i] = val<R>(P.gf(ADD00 + S6(i, j)));
+      Abar[i][j] = Abar[j][i] = M::trivial ? a[i][j] : a[i][j] * rf.ReDD(i, j);
+    }
+  R AUD[3][3], AUU[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R s = (R)0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) s += m.gUU[i][k] * Abar[k][j];
+      AUD[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R s = (R)0;
+#pragma unroll
+      for (int l = 0; l < 3; l++) s += AUD[i][l] * m.gUU[j][l];
+      AUU[i][j] = s;
+    }
+  R phid[3], trKd[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    phid[j] = -D1<ORDER, R>(P, CF, j, inv) / ((R)2 * cf);
+    trKd[j] = D1<ORDER, R>(P, TRK, j, inv);
+  }
+  // Dbar_k Abar_ij (symmetric in ij)
+  R AdBar[3][3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const R ad = D1<ORDER, R>(P, ADD00 + S6(i, j), k, inv);
+        R v = M::trivial ? ad : ad * rf.ReDD(i, j);
+        if (M::ReDDdD(i, j, k)) v += rf.ReDDdD(i, j, k) * a[i][j];
+#pragma unroll
+        for (int l = 0; l < 3; l++) v -= m.Gbar[l][k][i] * Abar[l][j] + m.Gbar[l][k][j] * Abar[i][l];
+        AdBar[i][j][k] = AdBar[j][i][k] = v;
+      }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    R r = (R)0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) r += (R)6 * AUU[i][j] * phid[j] - (R)(2.0 / 3.0) * m.gUU[i][j] * trKd[j];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+      for (int l = 0; l < 3; l++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) r += m.gUU[i][k] * m.gUU[j][l] * AdBar[k][l][j];
+    r *= cf * cf;
+    MU[i] = M::trivial ? r : r / rf.ReU(i);
+  }
+}
+
 // -------------------------------------------------------------------- RHS
 // All 24 right-hand sides at one interior point, in gridfunction order.
 template <int ORDER, int CS, typename R, typename Tin>

@@ -177,6 +177,15 @@ class Evolution:
                                                         _lib.ptr(H)), "BSSN_Hamiltonian_constraint")
         return H
 
+    def momentum(self, gfs=None):
+        """Momentum constraint M^i (3 gfs) at interior points (FP64)."""
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        M = torch.zeros((3,) + self.grid.shape, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.BSSN_momentum_constraint(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs),
+                                                     _lib.ptr(M)), "BSSN_momentum_constraint")
+        return M
+
     def maxwell_constraint(self, gfs=None):
         self._sync_stream()
         gfs = self.y_n if gfs is None else gfs

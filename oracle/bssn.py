@@ -301,6 +301,24 @@ def hamiltonian(v, q):
     return H + cf * cf * (Rtr - 8 * (pp + pdd))
 
 
+def momentum(v, q):
+    """BSSN_constraints.py:76-126: M^i = e^{-4 phi}/ReU^i [gammabar^ik gammabar^jl
+    Dbar_j Abar_kl + 6 Abar^ij d_j phi - 2/3 gammabar^ij d_j K], with
+    AbarDD_dD from BSSN_quantities.py:247-255 and d_j phi = -d_j W/(2 W)."""
+    Q = _Q(v, q)
+    gUU, Abar, G = Q.gammabarUU, Q.AbarDD, Q.GammabarUDD
+    cf = v["cf"]
+    AUU = np.einsum("ik...,jl...,kl...->ij...", gUU, gUU, Abar)
+    phid = -v["cf_dD"] / (2 * cf)
+    AdD = q["ReDDdD"] * v["aDD"][:, :, None] + q["ReDD"][:, :, None] * v["aDD_dD"]
+    AdBar = (AdD - np.einsum("lki...,lj...->ijk...", G, Abar)
+             - np.einsum("lkj...,il...->ijk...", G, Abar))
+    MU = (6 * np.einsum("ij...,j...->i...", AUU, phid)
+          - 2.0 / 3.0 * np.einsum("ij...,j...->i...", gUU, v["trK_dD"])
+          + np.einsum("ik...,jl...,klj...->i...", gUU, gUU, AdBar))
+    return MU * cf * cf / q["ReU"]
+
+
 # ------------------------------------------------------------------ grids
 def grid_symbols(gp, gfs, need_ricci=True):
     """Symbol values at interior points from FD of a (24, n2, n1, n0) array."""
@@ -395,6 +413,23 @@ def hamiltonian_grid(gp, gfs):
     v, q = grid_symbols(gp, gfs)
     out = np.zeros(gp.shape)
     gp.interior(out)[...] = hamiltonian(v, q)
+    return out
+
+
+def momentum_grid(gp, gfs):
+    """M^i (3, n2, n1, n0) at interior points, zero elsewhere."""
+    v, q = grid_symbols(gp, gfs, need_ricci=False)
+    S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+    f = {n: gfs[GF[n]] for n in EVOL}
+    a = np.empty((3, 3, 3) + v["cf"].shape)
+    for (i, j) in SYM:
+        for k in R3:
+            a[i, j, k] = a[j, i, k] = S.d1(f["aDD%d%d" % (i, j)], k)
+    v["aDD_dD"] = a
+    M = momentum(v, q)
+    out = np.zeros((3,) + gp.shape)
+    for i in R3:
+        gp.interior(out[i])[...] = M[i]
     return out
 
 

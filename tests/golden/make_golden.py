@@ -100,7 +100,7 @@ TRUSTED = [
      "import BSSN.BSSN_quantities as M", "M.RicciBar__gammabarDD_dHatD__DGammaUDD__DGammaU()",
      ["RbarDD", "DGammaU"]),
     ("constraints", "BSSN", "BSSN_constraints__BSSN_constraints__globals",
-     "import BSSN.BSSN_constraints as M", "M.BSSN_constraints()", ["H"]),
+     "import BSSN.BSSN_constraints as M", "M.BSSN_constraints()", ["H", "MU"]),
     ("ScalarWave_RHSs", "ScalarWave", "ScalarWave_RHSs__ScalarWave_RHSs__globals",
      "import ScalarWave.ScalarWave_RHSs as M", "M.ScalarWave_RHSs()", ["uu_rhs", "vv_rhs"]),
     ("ScalarWaveCurvilinear_RHSs", "ScalarWave", "ScalarWaveCurvilinear_RHSs__ScalarWaveCurvilinear_RHSs__globals",

@@ -120,6 +120,15 @@ def test_trusted_hamiltonian():
     assert close(H, want, 1e-11), (H, want)
 
 
+def test_trusted_momentum_constraint():
+    inp, v, q = _bssn_case("constraints")
+    M = obs.momentum(v, q)
+    ex = expect("constraints")
+    for i in range(3):
+        want = ex["MU[%d]" % i]
+        assert close(M[i, 0], want, 1e-11), (i, M[i, 0], want)
+
+
 @pytest.mark.parametrize("case,cart", [("ScalarWave_RHSs", True), ("ScalarWaveCurvilinear_RHSs", False)])
 def test_trusted_scalarwave(case, cart):
     inp = TV[case]["inputs"]

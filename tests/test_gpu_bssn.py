@@ -109,6 +109,16 @@ def test_hamiltonian_matches_oracle(cuda, coord, Nxx, order):
     assert per_gf_rel(H[None, g:-g, g:-g, g:-g], ref[None, g:-g, g:-g, g:-g]) < FP64_TOL
 
 
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_momentum_constraint_matches_oracle(cuda, coord, Nxx, order):
+    import torch
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    f = bssn_random_state(gp.shape, seed=19)
+    M = ev.momentum(torch.tensor(f, device=cuda)).cpu().numpy()
+    ref = obs.momentum_grid(gp, f)
+    assert per_gf_rel(M, ref, gp.NGHOSTS) < FP64_TOL
+
+
 @pytest.mark.parametrize("coord,Nxx,order", [CASES[0], CASES[2]])
 @pytest.mark.parametrize("fused", [True, False])
 def test_rk4_step_matches_oracle(cuda, coord, Nxx, order, fused):

@@ -109,3 +109,38 @@ def test_compensated_stage_buffers_are_pairs(cuda):
     hi, lo = k[..., 0].astype(np.float64), k[..., 1].astype(np.float64)
     assert np.array_equal((hi + lo).astype(np.float32).astype(np.float64), hi)
     assert np.all(np.abs(lo) <= np.spacing(np.abs(k[..., 0])).astype(np.float64) / 2)
+
+
+def test_bssn_constraint_convergence_order_unchanged(cuda):
+    """|H| in 2 < r < 5 after a short evolution of Brill-Lindquist data
+    (m = 0.5 at z = +-0.5) on Spherical grids at two resolutions: the
+    convergence order is FD4's, and the same in compensated precision as in
+    FP64 (the reference's |H| resolution-scaling check,
+    Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:1637-1673)."""
+    import torch
+    from nrpytutorial_gb300 import Evolution, Grid
+    T = 0.2
+    orders = {}
+    for prec in ("fp64", "compensated"):
+        norms = []
+        for Nr, Nth in ((48, 24), (96, 48)):
+            G = Grid("Spherical", (Nr, Nth, 4), FD_order=4, NGHOSTS=3, RMAX=8.0, eta=2.0)
+            ev = Evolution("BSSN", G, precision=prec, device=cuda)
+            ev.initial_data_brill_lindquist(0.5, (0, 0, 0.5), 0.5, (0, 0, -0.5))
+            ev.apply_bcs(ev.y_n)
+            ev.enforce_detgammabar(ev.y_n)
+            dt0 = G.find_timestep(0.5)
+            n = int(np.ceil(T / dt0))
+            for _ in range(n):
+                ev.step(T / n)
+            H = ev.hamiltonian()[0].cpu().numpy()
+            g = 3
+            r = np.asarray(G.xx[0])[None, None, :] * np.ones_like(H)
+            m = np.zeros_like(H, dtype=bool)
+            m[g:-g, g:-g, g:-g] = True
+            m &= (r > 2.0) & (r < 5.0)
+            norms.append(float(np.sqrt(np.mean(H[m] ** 2))))
+        orders[prec] = float(np.log2(norms[0] / norms[1]))
+    print("convergence orders", orders)
+    assert 3.0 < orders["fp64"] < 5.0, orders
+    assert abs(orders["compensated"] - orders["fp64"]) < 0.05, orders
