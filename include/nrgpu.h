@@ -224,6 +224,14 @@ int BSSN_rhs_eval(const rfm_struct *rfm, const paramstruct *params,
                   const double *auxevol_gfs, const double *in_gfs, double *rhs_gfs);
 int BSSN_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params,
                       const float *auxevol_gfs, const float *in_gfs, float *rhs_gfs);
+/* The same two functions in the reference's no-precompute form
+ * rhs_eval(params, xx, auxevol_gfs, in_gfs, rhs_gfs)
+ * (...Two_BHs_Collide-no_rfm_precompute.ipynb:477): the reference metric is
+ * evaluated at each point from the caller's coordinate arrays xx[0][i0],
+ * xx[1][i1] (device pointers; xx[2] is not read).  FP64. */
+int BSSN_Ricci_eval_xx(const paramstruct *params, double *xx[3], const double *in_gfs, double *auxevol_gfs);
+int BSSN_rhs_eval_xx(const paramstruct *params, double *xx[3], const double *auxevol_gfs,
+                     const double *in_gfs, double *rhs_gfs);
 /* enforce_detgammabar_constraint(rfmstruct, params, in_gfs) at ALL points
  * (Enforce_Detgammabar_Constraint.py:16-75).  Arithmetic is FP64 in both. */
 int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const paramstruct *params,

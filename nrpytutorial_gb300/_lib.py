@@ -93,6 +93,8 @@ _PROTOS = {
     "BSSN_enforce_detgammabar_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp]),
     "BSSN_enforce_detgammabar_constraint_f32": (C.c_int, [P(rfm_struct), P(paramstruct), vp]),
     "BSSN_Hamiltonian_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "BSSN_Ricci_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp]),
+    "BSSN_rhs_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp, vp]),
     "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "BSSN_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double),
                                                    C.c_double, P(C.c_double), vp]),

@@ -387,6 +387,28 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
+int BSSN_Ricci_eval_xx(const paramstruct *p, double *xx[3], const double *in, double *aux) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(xx && xx[0] && xx[1] && in && aux, "NULL argument");
+  NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
+  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
+#define RXX(CS, ORD) ricci_xx_launch_t<CS, ORD>(p, xa, in, aux)
+  NRGPU_BSSN_SWITCH(RXX)
+#undef RXX
+}
+
+int BSSN_rhs_eval_xx(const paramstruct *p, double *xx[3], const double *aux, const double *in, double *rhs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(xx && xx[0] && xx[1] && aux && in && rhs, "NULL argument");
+  NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
+  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
+#define HXX(CS, ORD) rhs_xx_launch_t<CS, ORD>(p, xa, aux, in, rhs)
+  NRGPU_BSSN_SWITCH(HXX)
+#undef HXX
+}
+
 int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const double *in, double *aux) {
   int st = check_bssn(rfm, p);
   if (st) return st;

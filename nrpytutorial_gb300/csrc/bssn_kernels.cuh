@@ -57,6 +57,81 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
   for (int gf = 0; gf < NUM_EVOL_GFS; gf++) epi(gf, idx, out[gf]);
 }
 
+// The same kernels with the reference metric evaluated at each point from the
+// caller's coordinate arrays xx0[i0], xx1[i1] (FP64), as the reference's
+// no-precompute rhs_eval(params, xx, auxevol_gfs, in_gfs, rhs_gfs) does.
+struct XXArgs {
+  const double *xx0, *xx1;
+  double AMPL, SINHW;
+};
+
+template <int CS>
+__device__ __forceinline__ void hatted_at_point(const XXArgs &xa, int i0, int i1, double *q) {
+  if constexpr (CS != NRGPU_COORD_CARTESIAN) {
+    ScaleFactors S;
+    scale_factors(CS, xa.AMPL, xa.SINHW, xa.xx0[i0], xa.xx1[i1], &S);
+    hatted_quantities(S, q);
+  }
+}
+
+template <int CS, int ORDER>
+__global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
+    ricci_xx_kernel(Grid g, const double *__restrict__ in, XXArgs xa, double *__restrict__ aux) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  double q[rq::NQ];
+  hatted_at_point<CS>(xa, i0, i1, q);
+  const Rfm<CS, double, true> rf{q, 1};
+  Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
+  Metric<CS, double> m;
+  metric_point<ORDER, CS, double>(P, rf, inv, m);
+  double Rbar[6];
+  ricci_point<ORDER, CS, double>(P, rf, inv, m, Rbar);
+#pragma unroll
+  for (int k = 0; k < 6; k++) aux[(long long)k * g.ntot + idx] = Rbar[k];
+}
+
+template <int CS, int ORDER>
+__global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
+    rhs_xx_kernel(Grid g, const double *__restrict__ in, const double *__restrict__ aux, XXArgs xa, double eta,
+                  double *__restrict__ out) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  double q[rq::NQ];
+  hatted_at_point<CS>(xa, i0, i1, q);
+  const Rfm<CS, double, true> rf{q, 1};
+  Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
+  double Rbar[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) Rbar[k] = __ldg(aux + (long long)k * g.ntot + idx);
+  double r[NUM_EVOL_GFS];
+  rhs_point<ORDER, CS, double>(P, rf, inv, Rbar, eta, r);
+#pragma unroll
+  for (int gf = 0; gf < NUM_EVOL_GFS; gf++) out[(long long)gf * g.ntot + idx] = r[gf];
+}
+
+template <int CS, int ORDER>
+int ricci_xx_launch_t(const paramstruct *p, const XXArgs &xa, const double *in, double *aux) {
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  ricci_xx_kernel<CS, ORDER><<<L.grid, L.block, 0, stream()>>>(g, in, xa, aux);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+template <int CS, int ORDER>
+int rhs_xx_launch_t(const paramstruct *p, const XXArgs &xa, const double *aux, const double *in, double *out) {
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  rhs_xx_kernel<CS, ORDER><<<L.grid, L.block, 0, stream()>>>(g, in, aux, xa, p->eta, out);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
 template <typename R> inline const R *table_of(const rfm_struct *rfm) {
   if (!rfm) return nullptr;
   if constexpr (sizeof(R) == 8) return (const R *)rfm->table64;
@@ -113,11 +188,18 @@ int rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a
 #define NRGPU_BSSN_DECLARE(CS, ORDER)                                                                 \
   extern template int ricci_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const void *, \
                                                 bool, int, void *);                                    \
-  extern template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &);
+  extern template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &); \
+  extern template int ricci_xx_launch_t<CS, ORDER>(const paramstruct *, const XXArgs &, const double *,   \
+                                                   double *);                                              \
+  extern template int rhs_xx_launch_t<CS, ORDER>(const paramstruct *, const XXArgs &, const double *,     \
+                                                 const double *, double *);
 #define NRGPU_BSSN_INSTANTIATE(CS, ORDER)                                                         \
   template int ricci_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const void *, \
                                          bool, int, void *);                                    \
-  template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &);
+  template int rhs_launch_t<CS, ORDER>(const rfm_struct *, const paramstruct *, const StageArgs &); \
+  template int ricci_xx_launch_t<CS, ORDER>(const paramstruct *, const XXArgs &, const double *, double *); \
+  template int rhs_xx_launch_t<CS, ORDER>(const paramstruct *, const XXArgs &, const double *, const double *, \
+                                          double *);
 
 }  // namespace bssn
 }  // namespace nrgpu

@@ -79,12 +79,17 @@ template <int CS> struct RfmMask {
 // ------------------------------------------------------- point accessor
 // Reads hatted quantities at one (i0,i1) column.  R is the arithmetic type
 // of the caller; tables are FP64 (tab64) with an FP32 copy (tab32).
-template <int CS, typename R> struct Rfm {
+// LOCAL: base points at this thread's own NQ values (plane 1), computed from
+// the caller's coordinates instead of read from the precomputed table.
+template <int CS, typename R, bool LOCAL = false> struct Rfm {
   using M = RfmMask<CS>;
   const R *__restrict__ base;  // table + i1*N0 + i0
   long long plane;             // N0*N1
 
-  __device__ __forceinline__ R q(int slot) const { return __ldg(base + slot * plane); }
+  __device__ __forceinline__ R q(int slot) const {
+    if constexpr (LOCAL) return base[slot];
+    else return __ldg(base + slot * plane);
+  }
 
   __device__ __forceinline__ R ReU(int i) const { return M::trivial ? (R)1 : q(rq::ReU + i); }
   __device__ __forceinline__ R ReUdD(int i, int j) const { return q(rq::ReUdD + 3 * i + j); }

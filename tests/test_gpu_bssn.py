@@ -110,6 +110,32 @@ def test_hamiltonian_matches_oracle(cuda, coord, Nxx, order):
 
 
 @pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_no_precompute_signature_matches_table_path(cuda, coord, Nxx, order):
+    """BSSN_Ricci_eval_xx / BSSN_rhs_eval_xx (reference metric evaluated
+    from the caller's xx arrays) agree with the precomputed-table path and
+    with the oracle."""
+    import ctypes as C
+    import torch
+    from nrpytutorial_gb300 import _lib
+    ev, gp = _setup(cuda, coord, Nxx, order)
+    f = bssn_random_state(gp.shape, seed=23)
+    t = torch.tensor(f, device=cuda)
+    xx = [torch.tensor(np.asarray(ev.grid.xx[d]), dtype=torch.float64, device=cuda) for d in range(3)]
+    xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
+    p = C.byref(ev.grid.params)
+    aux_a = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+    aux_b = torch.zeros_like(aux_a)
+    out_a = torch.zeros_like(t)
+    out_b = torch.zeros_like(t)
+    ev.rhs_eval(t, out_a, auxevol=aux_a)
+    _lib.check(ev.lib.BSSN_Ricci_eval_xx(p, xxp, _lib.ptr(t), _lib.ptr(aux_b)), "Ricci_eval_xx")
+    _lib.check(ev.lib.BSSN_rhs_eval_xx(p, xxp, _lib.ptr(aux_b), _lib.ptr(t), _lib.ptr(out_b)), "rhs_eval_xx")
+    assert per_gf_rel(aux_b.cpu().numpy(), aux_a.cpu().numpy(), gp.NGHOSTS) < 1e-14
+    assert per_gf_rel(out_b.cpu().numpy(), out_a.cpu().numpy(), gp.NGHOSTS) < 1e-14
+    assert per_gf_rel(out_b.cpu().numpy(), obs.rhs_grid(gp, f), gp.NGHOSTS) < FP64_TOL
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
 def test_momentum_constraint_matches_oracle(cuda, coord, Nxx, order):
     import torch
     ev, gp = _setup(cuda, coord, Nxx, order)
