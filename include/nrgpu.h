@@ -194,6 +194,21 @@ int apply_bcs_curvilinear(const paramstruct *params, const bc_struct *bcstruct,
 int apply_bcs_curvilinear_f32(const paramstruct *params, const bc_struct *bcstruct,
                               int NUM_GFS, const int8_t *gfs_parity, float *gfs);
 
+/* Sommerfeld radiation boundary condition (CurviBoundaryConditions.py:259-658,
+ * apply_bcs_sommerfeld): sets rhs_gfs at every ghost point from the state
+ * gfs: outer points rhs = -c (d_r f + (f - f_inf)/r) plus the radial-falloff
+ * correction from the point one step inward; inner points copy the RHS with
+ * parity.  xx: device coordinate arrays (or NULL for the cell-centred
+ * coordinates of params).  FP64.  The per-gridfunction speed c, f_inf and
+ * falloff power, and the FD order (2, 4, 6) of d_r, are those of
+ * sommerfeld_boundary_condition_class (defaults 1, 0, 3 and 2; the
+ * reference writes them into sommerfeld_params.h) and are set by
+ * nrgpu_sommerfeld_params (NULL arrays leave values unchanged). */
+int nrgpu_sommerfeld_params(int fd_order, int NUM_GFS, const double *speed, const double *f_inf,
+                            const double *radial_falloff_power);
+int apply_bcs_sommerfeld(const paramstruct *params, double *xx[3], const bc_struct *bcstruct, int NUM_GFS,
+                         const int8_t *gfs_parity, const double *gfs, double *rhs_gfs);
+
 /* -------------------------------------------------------- RHS kernels */
 /* ScalarWave Cartesian: rhs_eval(params, in_gfs, rhs_gfs)
  * (Tutorial-Start_to_Finish-ScalarWave.ipynb, rhs_eval; ScalarWave_RHSs.py:46-71) */
@@ -278,6 +293,11 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
  * hold a previous step's values (e.g. after one full step). */
 int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *params, MoL_gridfunctions *gfs,
                     int stage, double dt, int which);
+/* The RK4 step of the reference's Sommerfeld drivers: RHS_string = rhs_eval +
+ * apply_bcs_sommerfeld (on the stage's RHS), empty post_RHS_string, the
+ * update over every point (C_Code_Generation.py:266-329).  FP64. */
+int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const paramstruct *params,
+                                        const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* Host-buffer form for callers whose state lives in host memory: copies
  * y_n_gfs (host, FP64, pinned or pageable) to gfs->y_n_gfs, runs n_steps
  * steps, copies the state back, and synchronises the stream. */

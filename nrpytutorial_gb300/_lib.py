@@ -104,6 +104,11 @@ _PROTOS = {
                                                    P(MoL_gridfunctions), C.c_double]),
     "MoL_substep_rhs": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(MoL_gridfunctions), C.c_int,
                                   C.c_double, C.c_int]),
+    "MoL_step_forward_in_time_sommerfeld": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),
+                                                      P(MoL_gridfunctions), C.c_double]),
+    "nrgpu_sommerfeld_params": (C.c_int, [C.c_int, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double)]),
+    "apply_bcs_sommerfeld": (C.c_int, [P(paramstruct), P(C.c_void_p), P(bc_struct), C.c_int, P(C.c_int8),
+                                       vp, vp]),
     "MoL_evolve_host": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),
                                   P(MoL_gridfunctions), C.c_double, C.c_int, P(C.c_double)]),
     "nrgpu_l2_norm_sq": (C.c_int, [P(paramstruct), vp, C.c_int, vp, C.c_int, vp]),

@@ -353,6 +353,182 @@ int apply_bcs_adjoint_impl(const paramstruct *p, const bc_struct *bc, int NUM_GF
 template int apply_bcs_impl<double>(const paramstruct *, const bc_struct *, int, const int8_t *, double *);
 template int apply_bcs_impl<float>(const paramstruct *, const bc_struct *, int, const int8_t *, float *);
 
+// ----------------------------------------------------------- Sommerfeld
+// CurviBoundaryConditions.py:259-658 (apply_bcs_sommerfeld): on the RHS at
+// every outer ghost point, rhs = -c (d_r f + (f - f_inf)/r), plus for a radial
+// falloff power n > 0 the correction (rhs(o) + c (d_r f(o) + (f(o) -
+// f_inf)/r(o))) (r(o)/r)^n from the point o one step inward along the face
+// normal.  d_r f = sum_i d_i f dx^i/dr with d_i f one-sided (shifted into the
+// grid along the face normal, or away from the array edge) or centred, at the
+// FD order of the Sommerfeld parameters (2, 4 or 6).  Inner ghost points copy
+// the RHS with parity.  FP64.
+struct SommerfeldParams {
+  int fd_order;
+  double speed[64], f_inf[64], falloff[64];
+};
+static SommerfeldParams g_somm = [] {
+  SommerfeldParams s{};
+  s.fd_order = 2;
+  for (int g = 0; g < 64; g++) {
+    s.speed[g] = 1.0;
+    s.f_inf[g] = 0.0;
+    s.falloff[g] = 3.0;
+  }
+  return s;
+}();
+
+struct SommerfeldGeom {
+  int cs, n[3], ng;
+  double xxmin[3], dxx[3], invdx[3], AMPL, SINHW;
+  const double *xx[3];  // caller's coordinates, or NULL: cell-centred from xxmin/dxx
+};
+
+__device__ __forceinline__ double somm_xx(const SommerfeldGeom &G, int d, int i) {
+  return G.xx[d] ? G.xx[d][i] : xx_of(G.xxmin[d], G.dxx[d], i, G.ng);
+}
+
+template <int FD>
+__device__ __forceinline__ void somm_contraction(const SommerfeldGeom &G, const double *f, long long ntot_unused,
+                                                 const int idx3[3], const int face[3], double &r, double &pif) {
+  double J[3];
+  const double x0 = somm_xx(G, 0, idx3[0]);
+  if (G.cs == NRGPU_COORD_CARTESIAN) {
+    const double x1 = somm_xx(G, 1, idx3[1]), x2 = somm_xx(G, 2, idx3[2]);
+    r = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
+    J[0] = x0 / r;
+    J[1] = x1 / r;
+    J[2] = x2 / r;
+  } else if (G.cs == NRGPU_COORD_SPHERICAL) {
+    r = x0;
+    J[0] = 1.0;
+    J[1] = J[2] = 0.0;
+  } else {
+    const double sw = sinh(1.0 / G.SINHW);
+    r = G.AMPL * sinh(x0 / G.SINHW) / sw;
+    J[0] = 1.0 / (G.AMPL * cosh(x0 / G.SINHW) / (G.SINHW * sw));
+    J[1] = J[2] = 0.0;
+  }
+  constexpr int NU = FD + 1;
+  const double up2[3] = {-1.5, 2.0, -0.5}, cen2[1] = {0.5};
+  const double up4[5] = {-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0}, cen4[2] = {2.0 / 3.0, -1.0 / 12.0};
+  const double up6[7] = {-49.0 / 20.0, 6.0, -15.0 / 2.0, 20.0 / 3.0, -15.0 / 4.0, 6.0 / 5.0, -1.0 / 6.0},
+               cen6[3] = {3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0};
+  const double *up = FD == 2 ? up2 : (FD == 4 ? up4 : up6);
+  const double *cen = FD == 2 ? cen2 : (FD == 4 ? cen4 : cen6);
+  const long long st[3] = {1, G.n[0], (long long)G.n[0] * G.n[1]};
+  const long long c = idx3[0] + st[1] * idx3[1] + st[2] * idx3[2];
+  pif = 0.0;
+  for (int d = 0; d < 3; d++) {
+    if (J[d] == 0.0) continue;
+    const int i = idx3[d];
+    double fd;
+    if (face[d] != 0 || i + G.ng >= G.n[d] || i - G.ng <= 0) {
+      int shift = face[d];
+      if (i + G.ng >= G.n[d]) shift = -1;
+      if (i - G.ng <= 0) shift = 1;
+      double s = 0.0;
+      for (int k = 0; k < NU; k++) s += up[k] * f[c + (long long)k * shift * st[d]];
+      fd = shift * s * G.invdx[d];
+    } else {
+      double s = 0.0;
+      for (int k = 1; k <= FD / 2; k++) s += cen[k - 1] * (f[c + k * st[d]] - f[c - k * st[d]]);
+      fd = s * G.invdx[d];
+    }
+    pif += fd * J[d];
+  }
+}
+
+template <int FD>
+__global__ void sommerfeld_outer_kernel(SommerfeldGeom G, SommerfeldParams P, const int *__restrict__ dest,
+                                        const int *__restrict__ step, int npts, int dir, int ngfs, long long ntot,
+                                        const double *__restrict__ gfs, double *rhs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  const double *f = gfs + (long long)gf * ntot;
+  double *R = rhs + (long long)gf * ntot;
+  const long long d = dest[p];
+  const int idx3[3] = {(int)(d % G.n[0]), (int)((d / G.n[0]) % G.n[1]), (int)(d / ((long long)G.n[0] * G.n[1]))};
+  int face[3] = {0, 0, 0};
+  face[dir] = step[p] > 0 ? 1 : -1;
+  const double c = P.speed[gf], finf = P.f_inf[gf], n = P.falloff[gf];
+  double r, pif;
+  somm_contraction<FD>(G, f, ntot, idx3, face, r, pif);
+  double val = -c * (pif + (f[d] - finf) / r);
+  if (n > 0) {
+    int o3[3] = {idx3[0], idx3[1], idx3[2]};
+    o3[dir] += face[dir];
+    const long long o = d + step[p];
+    double ro, pifo;
+    somm_contraction<FD>(G, f, ntot, o3, face, ro, pifo);
+    const double extrap = c * (pifo + (f[o] - finf) / ro);
+    val += (R[o] + extrap) * pow(ro / r, n);
+  }
+  R[d] = val;
+}
+
+int apply_sommerfeld_impl(const paramstruct *p, double *const xx[3], const bc_struct *bc, int NUM_GFS,
+                          const int8_t *gfs_parity, const double *gfs, double *rhs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(bc != nullptr && gfs != nullptr && rhs != nullptr, "NULL argument");
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64, "NUM_GFS %d out of range", NUM_GFS);
+  NRGPU_REQUIRE(bc->NGHOSTS == p->NGHOSTS, "bcstruct built for NGHOSTS=%d, params say %d", bc->NGHOSTS,
+                p->NGHOSTS);
+  const int FD = g_somm.fd_order;
+  // centred stencils stay inside the array when NGHOSTS >= FD/2, one-sided
+  // ones when every extent is at least NGHOSTS + FD + 1
+  NRGPU_REQUIRE(p->NGHOSTS >= FD / 2, "Sommerfeld FD%d needs NGHOSTS >= %d", FD, FD / 2);
+  NRGPU_REQUIRE(p->Nxx_plus_2NGHOSTS0 >= p->NGHOSTS + FD + 1 && p->Nxx_plus_2NGHOSTS1 >= p->NGHOSTS + FD + 1 &&
+                    p->Nxx_plus_2NGHOSTS2 >= p->NGHOSTS + FD + 1,
+                "grid too small for the Sommerfeld FD%d stencils", FD);
+  ParityTypes types;
+  memset(&types, 0, sizeof(types));
+  for (int g = 0; g < NUM_GFS; g++) {
+    const int t = gfs_parity ? gfs_parity[g] : 0;
+    NRGPU_REQUIRE(t >= 0 && t <= 9, "parity type %d of gf %d not in 0..9", t, g);
+    types.t[g] = (int8_t)t;
+  }
+  SommerfeldGeom G;
+  G.cs = p->CoordSystem;
+  G.n[0] = p->Nxx_plus_2NGHOSTS0;
+  G.n[1] = p->Nxx_plus_2NGHOSTS1;
+  G.n[2] = p->Nxx_plus_2NGHOSTS2;
+  G.ng = p->NGHOSTS;
+  G.xxmin[0] = p->xxmin0; G.xxmin[1] = p->xxmin1; G.xxmin[2] = p->xxmin2;
+  G.dxx[0] = p->dxx0; G.dxx[1] = p->dxx1; G.dxx[2] = p->dxx2;
+  G.invdx[0] = p->invdx0; G.invdx[1] = p->invdx1; G.invdx[2] = p->invdx2;
+  G.AMPL = p->AMPL;
+  G.SINHW = p->SINHW;
+  for (int d = 0; d < 3; d++) G.xx[d] = xx ? xx[d] : nullptr;
+  const long long ntot = (long long)G.n[0] * G.n[1] * G.n[2];
+  const int B = 128;
+  for (int g = 0; g < bc->NGHOSTS; g++) {
+    for (int d = 0; d < 3; d++) {
+      const int a = bc->ob_dir_start[g][d], b = bc->ob_dir_start[g][d + 1];
+      const int n = b - a;
+      if (n <= 0) continue;
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+#define SOMM(F) sommerfeld_outer_kernel<F><<<grid, B, 0, stream()>>>(G, g_somm, bc->outer_dest + a, \
+                                                                    bc->outer_step + a, n, d, NUM_GFS, ntot, gfs, rhs)
+      if (FD == 2) SOMM(2);
+      else if (FD == 4) SOMM(4);
+      else SOMM(6);
+#undef SOMM
+      NRGPU_LAUNCH_CHECK();
+    }
+    const int n = bc->num_ib_gz_pts[g];
+    if (n > 0) {
+      const int a = bc->ib_start[g];
+      dim3 grid((n + B - 1) / B, NUM_GFS);
+      bc_inner_kernel<double><<<grid, B, 0, stream()>>>(bc->inner_dest + a, bc->inner_src + a,
+                                                        bc->inner_parity + a, n, NUM_GFS, ntot, types, rhs);
+      NRGPU_LAUNCH_CHECK();
+    }
+  }
+  return NRGPU_OK;
+}
+
 }  // namespace nrgpu
 
 using namespace nrgpu;
@@ -487,3 +663,21 @@ int apply_bcs_curvilinear_f32(const paramstruct *p, const bc_struct *bc, int NUM
 }
 
 }  // extern "C"
+
+extern "C" int nrgpu_sommerfeld_params(int fd_order, int NUM_GFS, const double *speed, const double *f_inf,
+                                       const double *radial_falloff_power) {
+  NRGPU_REQUIRE(fd_order == 2 || fd_order == 4 || fd_order == 6, "Sommerfeld fd_order must be 2, 4 or 6");
+  NRGPU_REQUIRE(NUM_GFS >= 0 && NUM_GFS <= 64, "NUM_GFS %d out of range", NUM_GFS);
+  g_somm.fd_order = fd_order;
+  for (int g = 0; g < NUM_GFS; g++) {
+    if (speed) g_somm.speed[g] = speed[g];
+    if (f_inf) g_somm.f_inf[g] = f_inf[g];
+    if (radial_falloff_power) g_somm.falloff[g] = radial_falloff_power[g];
+  }
+  return NRGPU_OK;
+}
+
+extern "C" int apply_bcs_sommerfeld(const paramstruct *p, double *xx[3], const bc_struct *bc, int NUM_GFS,
+                                    const int8_t *gfs_parity, const double *gfs, double *rhs_gfs) {
+  return apply_sommerfeld_impl(p, xx, bc, NUM_GFS, gfs_parity, gfs, rhs_gfs);
+}

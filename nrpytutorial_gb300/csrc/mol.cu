@@ -227,6 +227,42 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   return rhs_stage(system, rfm, p, a);
 }
 
+int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const paramstruct *p,
+                                        const bc_struct *bc, MoL_gridfunctions *gfs, double dt) {
+  int st = check_step_args(system, rfm, p, bc, gfs);
+  if (st) return st;
+  NRGPU_REQUIRE(gfs->precision == NRGPU_PREC_FP64, "the Sommerfeld step is FP64");
+  void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  const int ngf = system_num_gfs(system);
+  const long long n = state_len(system, p);
+  const int threads = 256;
+  const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 16);
+  for (int s = 0; s < 4; s++) {
+    StageArgs a{};
+    a.stage = -1;
+    a.dt = dt;
+    a.prec = gfs->precision;
+    a.in = (s == 0) ? (const void *)gfs->y_n_gfs : (const void *)kbuf[(s + 1) % 2];
+    a.in_is_f64 = true;
+    a.out = kbuf[s % 2];  // RHS_output: k_odd, k_even, k_odd, k_even
+    a.auxevol = gfs->auxevol_gfs;
+    if ((st = rhs_stage(system, rfm, p, a))) return st;
+    // radiation condition on the RHS at the ghost points (RHS_string), then the
+    // update over every point; no post-RHS boundary step
+    if ((st = apply_sommerfeld_impl(p, nullptr, bc, ngf, system_parity(system), (const double *)a.in,
+                                    (double *)kbuf[s % 2])))
+      return st;
+    rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+                                                                gfs->y_nplus1_running_total_gfs,
+                                                                (double *)kbuf[s % 2]);
+    NRGPU_LAUNCH_CHECK();
+    if (system == NRGPU_SYS_BSSN &&
+        (st = bssn_enforce_launch(rfm, p, s == 3 ? (void *)gfs->y_n_gfs : kbuf[s % 2], true)))
+      return st;
+  }
+  return NRGPU_OK;
+}
+
 int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *p,
                                      const bc_struct *bc, MoL_gridfunctions *gfs, double dt) {
   int st = check_step_args(system, rfm, p, bc, gfs);

@@ -46,6 +46,10 @@ const int8_t *system_parity(int system);
 // FP64 from the pairs and stored back as pairs.
 int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,
                         float2 *gfs);
+// Sommerfeld radiation condition on rhs from the state gfs (FP64); xx may be
+// NULL (cell-centred coordinates from params).
+int apply_sommerfeld_impl(const paramstruct *p, double *const xx[3], const bc_struct *bc, int NUM_GFS,
+                          const int8_t *gfs_parity, const double *gfs, double *rhs);
 // Transpose of the boundary conditions (FP64), in place: ghost adjoints are
 // moved onto their sources and zeroed.
 int apply_bcs_adjoint_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, const int8_t *gfs_parity,

@@ -16,8 +16,13 @@ from .grid import AUXEVOL_GFS, SYSTEM_GFS, Grid
 
 
 class Evolution:
-    def __init__(self, system, grid: Grid, precision="fp64", device="cuda"):
+    def __init__(self, system, grid: Grid, precision="fp64", device="cuda", boundary="extrapolation"):
         self.lib = _lib.load()
+        if boundary not in ("extrapolation", "sommerfeld"):
+            raise ValueError("boundary must be 'extrapolation' or 'sommerfeld'")
+        if boundary == "sommerfeld" and precision != "fp64":
+            raise ValueError("the Sommerfeld step is FP64")
+        self.boundary = boundary
         if system not in SYSTEM_GFS:
             raise ValueError("unknown system %r" % system)
         if precision not in _lib.PREC:
@@ -78,9 +83,14 @@ class Evolution:
 
     # -- the hot path
     def step(self, dt, fused=True):
-        """One RK4 step (MoLtimestepping/RK_MoL.h)."""
+        """One RK4 step (MoLtimestepping/RK_MoL.h).  With boundary="sommerfeld"
+        the radiation condition acts on each stage's RHS instead
+        (MoL_step_forward_in_time_sommerfeld; FP64)."""
         self._sync_stream()
-        f = self.lib.MoL_step_forward_in_time if fused else self.lib.MoL_step_forward_in_time_unfused
+        if self.boundary == "sommerfeld":
+            f = self.lib.MoL_step_forward_in_time_sommerfeld
+        else:
+            f = self.lib.MoL_step_forward_in_time if fused else self.lib.MoL_step_forward_in_time_unfused
         _lib.check(f(self.sys_id, self._rfm(), C.byref(self.grid.params), C.byref(self.bc),
                      C.byref(self.gfs), float(dt)), "MoL_step_forward_in_time")
         self.time += dt
@@ -161,6 +171,16 @@ class Evolution:
         f = self.lib.apply_bcs_curvilinear_f32 if gfs.dtype == torch.float32 else self.lib.apply_bcs_curvilinear
         _lib.check(f(C.byref(self.grid.params), C.byref(self.bc), gfs.shape[0],
                      C.cast(self.parity, C.POINTER(C.c_int8)), _lib.ptr(gfs)), "apply_bcs_curvilinear")
+
+    def apply_sommerfeld(self, gfs, rhs, xx=None):
+        """Sommerfeld radiation condition on rhs (FP64) from the state gfs."""
+        self._sync_stream()
+        xxp = None
+        if xx is not None:
+            xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
+        _lib.check(self.lib.apply_bcs_sommerfeld(C.byref(self.grid.params), xxp, C.byref(self.bc), gfs.shape[0],
+                                                 C.cast(self.parity, C.POINTER(C.c_int8)), _lib.ptr(gfs),
+                                                 _lib.ptr(rhs)), "apply_bcs_sommerfeld")
 
     def enforce_detgammabar(self, gfs):
         self._sync_stream()

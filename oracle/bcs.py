@@ -152,3 +152,118 @@ def rk4_step(y_n, dt, rhs_fn, post_fn, ng, k_odd=None, k_even=None):
     y_new = y_n + rt + k_even * dt * (1.0 / 6.0)
     post_fn(y_new)
     return y_new, k_odd, k_even
+
+
+# ------------------------------------------------------------ Sommerfeld
+# CurviBoundaryConditions.py:259-658 (sommerfeld_boundary_condition_class):
+# at every outer ghost point the RHS becomes the radiation condition
+#   rhs = -c (d_r f + (f - f_inf)/r)
+# plus, for a radial falloff power n > 0, the correction
+#   (rhs(o) + c (d_r f(o) + (f(o) - f_inf)/r(o))) (r(o)/r)^n
+# from the point o one step inward along the face normal; d_r f =
+# sum_i d_i f dx^i/dr, with d_i f one-sided (stencil shifted into the grid
+# along the face normal, or near an edge of the array) or centred.  Inner
+# points copy the RHS with parity.  Per gridfunction, per ghost layer: outer
+# points in list order, then inner points.
+SOMMERFELD_FD = {
+    2: ((-1.5, 2.0, -0.5), (0.5,)),
+    4: ((-25.0 / 12.0, 4.0, -3.0, 4.0 / 3.0, -1.0 / 4.0), (2.0 / 3.0, -1.0 / 12.0)),
+    6: ((-49.0 / 20.0, 6.0, -15.0 / 2.0, 20.0 / 3.0, -15.0 / 4.0, 6.0 / 5.0, -1.0 / 6.0),
+        (3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0)),
+}
+
+
+def _radial_geometry(gp, i0, i1, i2):
+    """(r, dx^i/dr) at a grid point (CoordSystem's xxSph[0] and Jacobian)."""
+    x0, x1, x2 = gp.xx[0][i0], gp.xx[1][i1], gp.xx[2][i2]
+    if gp.CoordSystem == CART:
+        r = np.sqrt(x0 * x0 + x1 * x1 + x2 * x2)
+        return r, (x0 / r, x1 / r, x2 / r)
+    if gp.CoordSystem == 1:  # Spherical: xx0 = r
+        return x0, (1.0, 0.0, 0.0)
+    w, A = gp.SINHW, gp.AMPL
+    r = A * np.sinh(x0 / w) / np.sinh(1.0 / w)
+    drdx = A * np.cosh(x0 / w) / (w * np.sinh(1.0 / w))
+    return r, (1.0 / drdx, 0.0, 0.0)
+
+
+def _sommerfeld_dr(gp, f, idx3, face, fd_order):
+    n = gp.np
+    ng = gp.NGHOSTS
+    up, cen = SOMMERFELD_FD[fd_order]
+    r, J = _radial_geometry(gp, *idx3)
+    acc = 0.0
+    for d in range(3):
+        if J[d] == 0.0:
+            continue
+        i = idx3[d]
+        if abs(face[d]) == 1 or i + ng >= n[d] or i - ng <= 0:
+            shift = face[d]
+            if i + ng >= n[d]:
+                shift = -1
+            if i - ng <= 0:
+                shift = 1
+            s = 0.0
+            for k, c in enumerate(up):
+                j = list(idx3)
+                j[d] += k * shift
+                s += c * f[j[2], j[1], j[0]]
+            fd = shift * s * gp.invdx[d]
+        else:
+            s = 0.0
+            for k, c in enumerate(cen, start=1):
+                jp, jm = list(idx3), list(idx3)
+                jp[d] += k
+                jm[d] -= k
+                s += c * (f[jp[2], jp[1], jp[0]] - f[jm[2], jm[1], jm[0]])
+            fd = s * gp.invdx[d]
+        acc += fd * J[d]
+    return r, acc
+
+
+def apply_sommerfeld(gp, layers, gfs, rhs, parity_types, fd_order=2, speed=None, f_inf=None, falloff=None):
+    """In place on rhs (ngf, n2, n1, n0), from the state gfs."""
+    ngf = gfs.shape[0]
+    speed = [1.0] * ngf if speed is None else speed
+    f_inf = [0.0] * ngf if f_inf is None else f_inf
+    falloff = [3.0] * ngf if falloff is None else falloff
+    n0, n1, _ = gp.np
+    stride = [1, n0, n0 * n1]
+    for g in range(ngf):
+        f, R = gfs[g], rhs[g]
+        Rf = R.reshape(-1)
+        for outer_dirs, (idst, isrc, ipar) in layers:
+            for d, arr in enumerate(outer_dirs):
+                for idx, st in arr:
+                    i0, i1, i2 = idx % n0, (idx // n0) % n1, idx // (n0 * n1)
+                    face = [0, 0, 0]
+                    face[d] = 1 if st > 0 else -1
+                    r, pif = _sommerfeld_dr(gp, f, (i0, i1, i2), face, fd_order)
+                    val = -speed[g] * (pif + (f[i2, i1, i0] - f_inf[g]) / r)
+                    if falloff[g] > 0:
+                        o = [i0, i1, i2]
+                        o[d] += face[d]
+                        ro, pifo = _sommerfeld_dr(gp, f, tuple(o), face, fd_order)
+                        extrap = speed[g] * (pifo + (f[o[2], o[1], o[0]] - f_inf[g]) / ro)
+                        val += (R[o[2], o[1], o[0]] + extrap) * (ro / r) ** falloff[g]
+                    Rf[idx] = val
+            if len(idst):
+                Rf[idst] = ipar[:, parity_types[g]] * Rf[isrc]
+    return rhs
+
+
+def rk4_step_sommerfeld(y_n, dt, rhs_fn, ng):
+    """RK4 step whose RHS function returns the full array (interior RHS plus
+    the Sommerfeld ghost RHS); the update runs over every point, with no
+    post-RHS boundary step (the reference's Sommerfeld driver)."""
+    k1 = rhs_fn(y_n)
+    rt = k1 * dt * (1.0 / 6.0)
+    y1 = y_n + k1 * dt * (1.0 / 2.0)
+    k2 = rhs_fn(y1)
+    rt = rt + k2 * dt * (1.0 / 3.0)
+    y2 = y_n + k2 * dt * (1.0 / 2.0)
+    k3 = rhs_fn(y2)
+    rt = rt + k3 * dt * (1.0 / 3.0)
+    y3 = y_n + k3 * dt
+    k4 = rhs_fn(y3)
+    return y_n + rt + k4 * dt * (1.0 / 6.0)
