@@ -59,7 +59,15 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
   const double det = -gb[0][2] * gb[0][2] * gb[1][1] + 2.0 * gb[0][1] * gb[0][2] * gb[1][2] -
                      gb[0][0] * gb[1][2] * gb[1][2] - gb[0][1] * gb[0][1] * gb[2][2] +
                      gb[0][0] * gb[1][1] * gb[2][2];
-  const double f = cbrt(fabs(rf.detg()) / det);
+  // f = (|det ghat| / det gammabar)^{1/3} = s^{-1/3}, s = det gammabar / |det ghat|:
+  // Newton-Raphson on w^{-3} = s (w <- w (4 - s w^3) / 3, quadratic
+  // convergence) from the FP32 reciprocal cube root, two steps to FP64
+  // accuracy, in place of the FP64 cube root (several times the FP64
+  // instructions on this FP64-light GPU).
+  const double sdet = det / fabs(rf.detg());
+  double f = (double)rcbrtf((float)sdet);
+#pragma unroll
+  for (int it = 0; it < 2; it++) f = f * (4.0 - sdet * f * f * f) * (1.0 / 3.0);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
