@@ -77,6 +77,9 @@ def state_errors(a, b, c0, names):
             "fields": fields}
 
 
+PROFILE_N3 = PROFILE_N4 = PROFILE_N5 = None  # --profile-sizes: smaller configurations 3-5
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -314,14 +317,15 @@ def run_gpu(args):
     del evc
     torch.cuda.empty_cache()
     if args.config3_steps > 0:
-        out["mixed_cartesian_256"] = run_config3(dev, args.config3_steps, flush)
+        out["mixed_cartesian_256"] = run_config3(dev, args.config3_steps, flush, N=PROFILE_N3 or 256)
         torch.cuda.empty_cache()
     if args.config4_steps > 0:
-        out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush)
+        out["batched_scalarwave_512"] = run_config4(dev, args.config4_steps, flush, n=PROFILE_N4 or 512)
         torch.cuda.empty_cache()
-    out["convergence_order_H"] = convergence_orders(dev)
+    if not args.profile_sizes:
+        out["convergence_order_H"] = convergence_orders(dev)
     if args.config5_steps > 0:
-        a5 = run_config5(dev, args.config5_steps)
+        a5 = run_config5(dev, args.config5_steps, N=PROFILE_N5 or 128)
         out["adjoint_maxwell_128"] = a5
         out["adjoint_over_forward"] = a5["adjoint_over_forward"]
     if rank == 0 and not args.no_cpu:
@@ -333,7 +337,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def run_config3(dev, K, flush):
+def run_config3(dev, K, flush, N=256):
     """Configuration 3: BSSN Cartesian [-10,10]^3, 256^3 interior, FD6 (4 ghosts),
     RK4, Brill-Lindquist with masses ~U[0.3,0.7] at z = +-U[0.3,1.0] (seeded);
     FP32 storage and RHS with FP64 RK accumulation, det(gammabar) rescale and
@@ -343,7 +347,7 @@ def run_config3(dev, K, flush):
     rng = np.random.default_rng(3)
     m1, m2 = rng.uniform(0.3, 0.7, 2)
     z1, z2 = rng.uniform(0.3, 1.0), -rng.uniform(0.3, 1.0)
-    G = Grid("Cartesian", (256, 256, 256), FD_order=6, NGHOSTS=4, domain=(-10.0, 10.0), eta=2.0)
+    G = Grid("Cartesian", (N, N, N), FD_order=6, NGHOSTS=4, domain=(-10.0, 10.0), eta=2.0)
     nint = G.n_interior()
     dt = G.find_timestep(0.5)
     e64 = Evolution("BSSN", G, precision="fp64", device=dev)
@@ -351,8 +355,8 @@ def run_config3(dev, K, flush):
     e64.apply_bcs(e64.y_n)
     e64.enforce_detgammabar(e64.y_n)
     y0 = e64.y_n.clone()
-    res = {"workload": "BSSN Cartesian 256^3 FD6 RK4 Brill-Lindquist m=(%.4f,%.4f) z=(%.4f,%.4f), seed 3"
-                       % (m1, m2, z1, z2), "steps": K, "dt": dt}
+    res = {"workload": "BSSN Cartesian %d^3 FD6 RK4 Brill-Lindquist m=(%.4f,%.4f) z=(%.4f,%.4f), seed 3"
+                       % (N, m1, m2, z1, z2), "steps": K, "dt": dt}
     times, errs, H = {}, {}, {}
     g = 4
     B = e64.y_n[:, g:-g, g:-g, g:-g]
@@ -412,7 +416,7 @@ def run_config3(dev, K, flush):
     return res
 
 
-def run_config4(dev, K, flush):
+def run_config4(dev, K, flush, n=512):
     """Configuration 4: 512 independent ScalarWave evolutions on Spherical
     grids (RMAX 10), Nr ~ U{32..160} (seeded), Ntheta 32, Nphi 8, FD4, RK4 with
     each instance's own CFL-0.5 time step, Gaussian pulses
@@ -424,10 +428,9 @@ def run_config4(dev, K, flush):
     from nrpytutorial_gb300 import _lib
     from nrpytutorial_gb300.batch import ScalarWaveBatch
     rng = np.random.default_rng(4)
-    n = 512
     Nr = rng.integers(32, 161, n)
     A, r0, w = rng.uniform(0.1, 1.0, n), rng.uniform(1.0, 4.0, n), rng.uniform(0.5, 2.0, n)
-    res = {"workload": "512 x ScalarWave Spherical Nr~U{32..160} x 32 x 8 FD4 RK4, seed 4", "steps": K}
+    res = {"workload": "%d x ScalarWave Spherical Nr~U{32..160} x 32 x 8 FD4 RK4, seed 4" % n, "steps": K}
     runs = {}
     lib = _lib.load()
     for prec in ("fp64", "mixed", "compensated"):
@@ -502,7 +505,7 @@ def convergence_orders(dev):
     return out
 
 
-def run_config5(dev, K):
+def run_config5(dev, K, N=128):
     """Configuration 5: Maxwell System I, Cartesian [-10,10]^3 at 128^3, FD4,
     FP64, K RK4 steps (CFL 0.5) from toroidal-dipole data with seeded
     amplitude and width parameters; observable = L2 norm of E over the
@@ -514,7 +517,7 @@ def run_config5(dev, K):
     from nrpytutorial_gb300.adjoint import ExtractionSphere, MaxwellExtraction
     rng = np.random.default_rng(5)
     amp, lam = rng.uniform(0.5, 1.5), rng.uniform(0.5, 1.5)
-    G = Grid("Cartesian", (128, 128, 128), FD_order=4, NGHOSTS=3, domain=(-10.0, 10.0))
+    G = Grid("Cartesian", (N, N, N), FD_order=4, NGHOSTS=3, domain=(-10.0, 10.0))
     m = MaxwellExtraction(G, ExtractionSphere(8.0, 32, 64), n_steps=K, checkpoint_every=20, device=dev)
     m.forward(amp, lam)  # warm-up
     m.gradient()
@@ -534,9 +537,9 @@ def run_config5(dev, K):
     fd = [(m.forward(amp + h, lam) - m.forward(amp - h, lam)) / (2 * h),
           (m.forward(amp, lam + h) - m.forward(amp, lam - h)) / (2 * h)]
     rel = [abs(g[i] - fd[i]) / abs(fd[i]) for i in range(2)]
-    nint = 128 ** 3
-    return {"workload": "Maxwell System I Cartesian [-10,10]^3 128^3 FD4 FP64, %d RK4 steps, toroidal dipole "
-                        "amp=%.6f lam=%.6f (seed 5), |E| on sphere r=8 (32x64), checkpoints every 20" % (K, amp, lam),
+    nint = N ** 3
+    return {"workload": "Maxwell System I Cartesian [-10,10]^3 %d^3 FD4 FP64, %d RK4 steps, toroidal dipole "
+                        "amp=%.6f lam=%.6f (seed 5), |E| on sphere r=8 (32x64), checkpoints every 20" % (N, K, amp, lam),
             "J": J, "grad": [float(v) for v in g], "grad_central_fd_h1e-6": [float(v) for v in fd],
             "grad_rel_err_vs_fd": rel, "forward_s": t_fwd, "adjoint_s": t_bwd,
             "adjoint_over_forward": t_bwd / t_fwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
@@ -700,11 +703,16 @@ def main():
     ap.add_argument("--ref-budget-s", type=float, default=90.0)
     ap.add_argument("--config3-steps", type=int, default=4,
                     help="RK4 steps of the 256^3 Cartesian mixed-vs-FP64 comparison (0 skips it)")
+    ap.add_argument("--profile-sizes", action="store_true",
+                    help="small configurations 3-5 (96^3, 64 instances, 48^3) for profiler captures")
     ap.add_argument("--config5-steps", type=int, default=300,
                     help="RK4 steps of the Maxwell 128^3 adjoint-gradient run (0 skips it)")
     ap.add_argument("--config4-steps", type=int, default=400,
                     help="RK4 steps of the 512-instance batched ScalarWave run (0 skips it)")
     args = ap.parse_args()
+    global PROFILE_N3, PROFILE_N4, PROFILE_N5
+    if args.profile_sizes:
+        PROFILE_N3, PROFILE_N4, PROFILE_N5 = 96, 64, 48
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

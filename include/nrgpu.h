@@ -263,6 +263,12 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
                              const double *in_gfs, double *aux_gfs);
 
 /* --------------------------------------------------------- initial data */
+/* ScalarWave initial data at ALL points (ScalarWave/InitialData.py:27-88):
+ * kind 0 PlaneWave (uu = sin(khat.x - c t) + 2, vv = d uu/dt, khat = kk/|kk|),
+ * kind 1 SphericalGaussian (width sigma), at Cartesian positions of the grid's
+ * CoordSystem, time `time`, c = params->wavespeed. */
+int ScalarWave_initial_data(const paramstruct *params, int kind, double time, const double kk[3],
+                            double sigma, double *in_gfs);
 /* Brill-Lindquist two-puncture data converted to rescaled BSSN variables in
  * the grid's coordinates at ALL points (BrillLindquist.py:48-82,
  * ADM_Exact_Spherical_or_Cartesian_to_BSSNCurvilinear.py:16-135,

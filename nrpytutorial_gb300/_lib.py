@@ -96,6 +96,7 @@ _PROTOS = {
     "BSSN_Ricci_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp]),
     "BSSN_rhs_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp, vp]),
     "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "ScalarWave_initial_data": (C.c_int, [P(paramstruct), C.c_int, C.c_double, P(C.c_double), C.c_double, vp]),
     "BSSN_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double),
                                                    C.c_double, P(C.c_double), vp]),
     "MoL_step_forward_in_time": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct),

@@ -101,6 +101,49 @@ int scalarwave_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
   return dispatch<float, float, float>(p, g, stage_input<float>(a), rfm, epi);
 }
 
+// Initial data of ScalarWave/InitialData.py:27-88 at every point, at
+// Cartesian positions xx_to_Cart(xx) of the grid's CoordSystem:
+//   PlaneWave          uu = sin(khat.x - c t) + 2, vv = -c cos(khat.x - c t)
+//   SphericalGaussian  uu = (r-ct)/r e^{-(r-ct)^2/(2s^2)} + (r+ct)/r e^{-(r+ct)^2/(2s^2)} + 1,
+//                      vv = c/r [e_a ((r-ct)^2/s^2 - 1) + e_b (1 - (r+ct)^2/s^2)]
+__global__ void sw_initial_data_kernel(paramstruct p, int kind, double t, double k0, double k1, double k2,
+                                       double sigma, double *__restrict__ gfs) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
+  const int n0 = p.Nxx_plus_2NGHOSTS0, n1 = p.Nxx_plus_2NGHOSTS1;
+  if (i0 >= n0) return;
+  const long long ntot = (long long)n0 * n1 * p.Nxx_plus_2NGHOSTS2;
+  const long long idx = i0 + (long long)n0 * (i1 + (long long)n1 * i2);
+  const double x0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS), x1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS),
+               x2 = xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS);
+  double x, y, z;
+  if (p.CoordSystem == NRGPU_COORD_CARTESIAN) {
+    x = x0;
+    y = x1;
+    z = x2;
+  } else {
+    double r, r1, r2, r3;
+    radial_map(p.CoordSystem, p.AMPL, p.SINHW, x0, &r, &r1, &r2, &r3);
+    x = r * sin(x1) * cos(x2);
+    y = r * sin(x1) * sin(x2);
+    z = r * cos(x1);
+  }
+  const double c = p.wavespeed;
+  double uu, vv;
+  if (kind == 0) {
+    const double ph = (k0 * x + k1 * y + k2 * z) / sqrt(k0 * k0 + k1 * k1 + k2 * k2) - c * t;
+    uu = sin(ph) + 2.0;
+    vv = -c * cos(ph);
+  } else {
+    const double r = sqrt(x * x + y * y + z * z);
+    const double a = r - c * t, b = r + c * t, s2 = sigma * sigma;
+    const double ea = exp(-a * a / (2.0 * s2)), eb = exp(-b * b / (2.0 * s2));
+    uu = a / r * ea + b / r * eb + 1.0;
+    vv = c / r * (ea * (a * a / s2 - 1.0) + eb * (1.0 - b * b / s2));
+  }
+  gfs[idx] = uu;
+  gfs[ntot + idx] = vv;
+}
+
 }  // namespace nrgpu
 
 using namespace nrgpu;
@@ -134,5 +177,19 @@ int ScalarWaveCurvilinear_rhs_eval(const rfm_struct *rfm, const paramstruct *p, 
 int ScalarWaveCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *p, const float *in,
                                        float *rhs) {
   return sw_plain(rfm, p, in, rhs, NRGPU_PREC_MIXED, true);
+}
+int ScalarWave_initial_data(const paramstruct *p, int kind, double time, const double kk[3], double sigma,
+                            double *in_gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(in_gfs, "NULL argument");
+  NRGPU_REQUIRE(kind == 0 || kind == 1, "kind must be 0 (PlaneWave) or 1 (SphericalGaussian)");
+  NRGPU_REQUIRE(kind == 1 || (kk && (kk[0] != 0.0 || kk[1] != 0.0 || kk[2] != 0.0)), "PlaneWave needs k != 0");
+  NRGPU_REQUIRE(kind == 0 || sigma > 0.0, "SphericalGaussian needs sigma > 0");
+  dim3 block(64), grid((p->Nxx_plus_2NGHOSTS0 + 63) / 64, p->Nxx_plus_2NGHOSTS1, p->Nxx_plus_2NGHOSTS2);
+  sw_initial_data_kernel<<<grid, block, 0, stream()>>>(*p, kind, time, kk ? kk[0] : 0.0, kk ? kk[1] : 0.0,
+                                                       kk ? kk[2] : 0.0, sigma, in_gfs);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
 }
 }

@@ -172,6 +172,15 @@ class Evolution:
         _lib.check(f(C.byref(self.grid.params), C.byref(self.bc), gfs.shape[0],
                      C.cast(self.parity, C.POINTER(C.c_int8)), _lib.ptr(gfs)), "apply_bcs_curvilinear")
 
+    def initial_data_scalarwave(self, kind="PlaneWave", time=0.0, k=(1.0, 1.0, 1.0), sigma=3.0, out=None):
+        """ScalarWave/InitialData.py data ("PlaneWave" or "SphericalGaussian") at all points."""
+        self._sync_stream()
+        out = self.y_n if out is None else out
+        kk = (C.c_double * 3)(*[float(v) for v in k])
+        _lib.check(self.lib.ScalarWave_initial_data(C.byref(self.grid.params), {"PlaneWave": 0,
+                                                    "SphericalGaussian": 1}[kind], float(time), kk, float(sigma),
+                                                    _lib.ptr(out)), "ScalarWave_initial_data")
+
     def apply_sommerfeld(self, gfs, rhs, xx=None):
         """Sommerfeld radiation condition on rhs (FP64) from the state gfs."""
         self._sync_stream()

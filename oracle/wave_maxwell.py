@@ -124,3 +124,33 @@ def toroidal_dipole(gp, t, amp=1.0, lam=1.0):
     out[0], out[1] = -y * F, x * F
     out[3], out[4] = y * dF, -x * dF
     return out
+
+
+def scalarwave_id_pointwise(kind, x, y, z, t, c, k=(1.0, 1.0, 1.0), sigma=3.0):
+    """ScalarWave/InitialData.py:27-88 at Cartesian points.
+    PlaneWave: uu = sin(khat.x - c t) + 2, vv = -c cos(khat.x - c t), khat = k/|k|.
+    SphericalGaussian: uu = (r-ct)/r e^{-(r-ct)^2/(2 s^2)} + (r+ct)/r e^{-(r+ct)^2/(2 s^2)} + 1,
+    vv = d uu/dt = c/r [e_a ((r-ct)^2/s^2 - 1) + e_b (1 - (r+ct)^2/s^2)]."""
+    if kind == "PlaneWave":
+        kn = np.sqrt(k[0] ** 2 + k[1] ** 2 + k[2] ** 2)
+        ph = (k[0] * x + k[1] * y + k[2] * z) / kn - c * t
+        return np.sin(ph) + 2.0, -c * np.cos(ph)
+    r = np.sqrt(x * x + y * y + z * z)
+    a, b = r - c * t, r + c * t
+    ea, eb = np.exp(-a * a / (2 * sigma ** 2)), np.exp(-b * b / (2 * sigma ** 2))
+    uu = a / r * ea + b / r * eb + 1.0
+    vv = c / r * (ea * (a * a / sigma ** 2 - 1.0) + eb * (1.0 - b * b / sigma ** 2))
+    return uu, vv
+
+
+def scalarwave_id_grid(gp, kind, t=0.0, k=(1.0, 1.0, 1.0), sigma=3.0):
+    """(2, n2, n1, n0) initial data at every point of a grid (Cartesian
+    coordinates from xx_to_Cart of the grid's CoordSystem)."""
+    X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
+    if gp.CoordSystem == 0:
+        x, y, z = X0, X1, X2
+    else:
+        r = X0 if gp.CoordSystem == 1 else gp.AMPL * np.sinh(X0 / gp.SINHW) / np.sinh(1.0 / gp.SINHW)
+        x, y, z = r * np.sin(X1) * np.cos(X2), r * np.sin(X1) * np.sin(X2), r * np.cos(X1)
+    uu, vv = scalarwave_id_pointwise(kind, x, y, z, t, gp.wavespeed, k, sigma)
+    return np.stack([uu, vv])

@@ -101,6 +101,10 @@ TRUSTED = [
      ["RbarDD", "DGammaU"]),
     ("constraints", "BSSN", "BSSN_constraints__BSSN_constraints__globals",
      "import BSSN.BSSN_constraints as M", "M.BSSN_constraints()", ["H", "MU"]),
+    ("SW_ID_PlaneWave", "ScalarWave", "InitialData__InitialData__Type__PlaneWave___globals",
+     "import ScalarWave.InitialData as M", 'M.InitialData(Type="PlaneWave")', ["uu_ID", "vv_ID"]),
+    ("SW_ID_SphericalGaussian", "ScalarWave", "InitialData__InitialData__Type__SphericalGaussian___globals",
+     "import ScalarWave.InitialData as M", 'M.InitialData(Type="SphericalGaussian")', ["uu_ID", "vv_ID"]),
     ("ScalarWave_RHSs", "ScalarWave", "ScalarWave_RHSs__ScalarWave_RHSs__globals",
      "import ScalarWave.ScalarWave_RHSs as M", "M.ScalarWave_RHSs()", ["uu_rhs", "vv_rhs"]),
     ("ScalarWaveCurvilinear_RHSs", "ScalarWave", "ScalarWaveCurvilinear_RHSs__ScalarWaveCurvilinear_RHSs__globals",

@@ -120,6 +120,16 @@ def test_trusted_hamiltonian():
     assert close(H, want, 1e-11), (H, want)
 
 
+@pytest.mark.parametrize("kind", ["PlaneWave", "SphericalGaussian"])
+def test_trusted_scalarwave_initial_data(kind):
+    inp = TV["SW_ID_" + kind]["inputs"]
+    ex = expect("SW_ID_" + kind)
+    uu, vv = ow.scalarwave_id_pointwise(kind, inp["xx0"], inp["xx1"], inp["xx2"], inp["time"], inp["wavespeed"],
+                                        (inp.get("kk0"), inp.get("kk1"), inp.get("kk2")), inp.get("sigma"))
+    assert close(uu, ex["uu_ID"], 1e-13), (uu, ex)
+    assert close(vv, ex["vv_ID"], 1e-13), (vv, ex)
+
+
 def test_trusted_momentum_constraint():
     inp, v, q = _bssn_case("constraints")
     M = obs.momentum(v, q)

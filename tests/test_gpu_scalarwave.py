@@ -108,3 +108,13 @@ def test_plane_wave_fourth_order_convergence(cuda, prec):
         errs.append(np.abs(num - exact[0][g:-g, g:-g, g:-g]).max())
     order = np.log2(errs[0] / errs[1])
     assert 3.5 < order < 4.6, (errs, order)
+
+
+@pytest.mark.parametrize("coord", ["Cartesian", "Spherical", "SinhSpherical"])
+@pytest.mark.parametrize("kind", ["PlaneWave", "SphericalGaussian"])
+def test_initial_data_matches_oracle(cuda, coord, kind):
+    G, gp = grids("ScalarWave", coord, (10, 8, 6), 4, AMPL=5.0, SINHW=0.3, RMAX=5.0, wavespeed=0.7)
+    ev = _evo(cuda, G)
+    ev.initial_data_scalarwave(kind, time=0.4, k=(0.3, -1.0, 0.5), sigma=1.5)
+    ref = ow.scalarwave_id_grid(gp, kind, 0.4, (0.3, -1.0, 0.5), 1.5)
+    assert np.allclose(ev.y_n.cpu().numpy(), ref, rtol=1e-13, atol=1e-13)
