@@ -80,6 +80,9 @@ typedef struct paramstruct {
   double eta;                         /* Gamma-driver damping (BSSN_gauge_RHSs.py:233) */
   double wavespeed;                   /* ScalarWave/CommonParams.py:24          */
   double time;
+  double diss_strength;               /* Kreiss-Oliger dissipation added to every BSSN
+                                         RHS (KO_Dissipation::diss_strength,
+                                         BaikalETK_C_kernels_codegen.py:147-171); 0 = off */
 } paramstruct;
 
 /*
@@ -149,8 +152,9 @@ const char *nrgpu_last_error(void);
 /* Number of kernels this library has launched in this process. */
 long long   nrgpu_kernel_launch_count(void);
 /* FD coefficients the kernels use: kind 0 = centred 1st, 1 = centred 2nd,
- * 2 = upwind (+1 shifted) 1st.  Writes order+1 doubles (offsets -order/2
- * ... +order/2, shifted by +1 for kind 2).  Host only, no GPU needed.
+ * 2 = upwind (+1 shifted) 1st, 3 = Kreiss-Oliger.  Writes order+1 doubles
+ * (offsets -order/2 ... +order/2, shifted by +1 for kind 2), order+3 for
+ * kind 3 (offsets -order/2-1 ... order/2+1).  Host only, no GPU needed.
  * finite_difference.py:252-369 computes the reference's. */
 int         nrgpu_fd_coeffs(int order, int kind, double *out);
 

@@ -32,6 +32,7 @@ class paramstruct(C.Structure):
         ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
         ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
         ("eta", C.c_double), ("wavespeed", C.c_double), ("time", C.c_double),
+        ("diss_strength", C.c_double),
     ]
 
 

@@ -308,7 +308,8 @@ int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *i
   NRGPU_REQUIRE(in && auxevol, "NULL gridfunctions");
   NRGPU_BSSN_SWITCH(RICCI_CALL)
 }
-#define RHS_CALL(CS, ORD) rhs_launch_t<CS, ORD>(rfm, p, a)
+#define RHS_CALL(CS, ORD) \
+  (p->diss_strength != 0.0 ? rhs_launch_t<CS, ORD, true>(rfm, p, a) : rhs_launch_t<CS, ORD, false>(rfm, p, a))
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
   int st = check_bssn(rfm, p);
   if (st) return st;
@@ -412,7 +413,9 @@ int BSSN_rhs_eval_xx(const paramstruct *p, double *xx[3], const double *aux, con
   NRGPU_REQUIRE(xx && xx[0] && xx[1] && aux && in && rhs, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
   const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
-#define HXX(CS, ORD) rhs_xx_launch_t<CS, ORD>(p, xa, aux, in, rhs)
+#define HXX(CS, ORD)                                                 \
+  (p->diss_strength != 0.0 ? rhs_xx_launch_t<CS, ORD, true>(p, xa, aux, in, rhs) \
+                           : rhs_xx_launch_t<CS, ORD, false>(p, xa, aux, in, rhs))
   NRGPU_BSSN_SWITCH(HXX)
 #undef HXX
 }

@@ -18,7 +18,10 @@ namespace nrgpu {
 template <int ORDER> struct FDCoef;
 
 // Coefficients as constexpr functions of the (unrolled, hence constant)
-// offset, usable from both host and device code.
+// offset, usable from both host and device code.  ko(k), k = 0..R+1, are the
+// Kreiss-Oliger weights of the symmetric (ORDER+3)-point stencil: the
+// (ORDER+2)-th derivative times (-1)^((ORDER+4)/2) / 2^(ORDER+2)
+// (finite_difference.py:252-258, 310-313, 331-334).
 #define NRGPU_FD_TABLE(NAME, ...)                                              \
   __host__ __device__ static constexpr double NAME(int k) {                    \
     constexpr double t[] = {__VA_ARGS__};                                      \
@@ -31,6 +34,7 @@ template <> struct FDCoef<2> {
   NRGPU_FD_TABLE(c1, 0.0, 1.0 / 2.0)
   NRGPU_FD_TABLE(c2, -2.0, 1.0)
   NRGPU_FD_TABLE(up, -3.0 / 2.0, 2.0, -1.0 / 2.0)
+  NRGPU_FD_TABLE(ko, -3.0 / 8.0, 1.0 / 4.0, -1.0 / 16.0)
 };
 template <> struct FDCoef<4> {
   static constexpr int R = 2;
@@ -38,6 +42,7 @@ template <> struct FDCoef<4> {
   NRGPU_FD_TABLE(c1, 0.0, 2.0 / 3.0, -1.0 / 12.0)
   NRGPU_FD_TABLE(c2, -5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0)
   NRGPU_FD_TABLE(up, -1.0 / 4.0, -5.0 / 6.0, 3.0 / 2.0, -1.0 / 2.0, 1.0 / 12.0)
+  NRGPU_FD_TABLE(ko, -5.0 / 16.0, 15.0 / 64.0, -3.0 / 32.0, 1.0 / 64.0)
 };
 template <> struct FDCoef<6> {
   static constexpr int R = 3;
@@ -45,6 +50,7 @@ template <> struct FDCoef<6> {
   NRGPU_FD_TABLE(c1, 0.0, 3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0)
   NRGPU_FD_TABLE(c2, -49.0 / 18.0, 3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0)
   NRGPU_FD_TABLE(up, 1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0)
+  NRGPU_FD_TABLE(ko, -35.0 / 128.0, 7.0 / 32.0, -7.0 / 64.0, 1.0 / 32.0, -1.0 / 256.0)
 };
 template <> struct FDCoef<8> {
   static constexpr int R = 4;
@@ -53,6 +59,7 @@ template <> struct FDCoef<8> {
   NRGPU_FD_TABLE(c2, -205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0)
   NRGPU_FD_TABLE(up, -1.0 / 168.0, 1.0 / 14.0, -1.0 / 2.0, -9.0 / 20.0, 5.0 / 4.0, -1.0 / 2.0, 1.0 / 6.0,
                  -1.0 / 28.0, 1.0 / 280.0)
+  NRGPU_FD_TABLE(ko, -63.0 / 256.0, 105.0 / 512.0, -15.0 / 128.0, 45.0 / 1024.0, -5.0 / 512.0, 1.0 / 1024.0)
 };
 #undef NRGPU_FD_TABLE
 
@@ -98,6 +105,16 @@ __device__ __forceinline__ R fd_d11(const T *__restrict__ p, long long s, long l
     }
     acc += (R)C::c1(a) * inner;
   }
+  return acc;
+}
+
+// Kreiss-Oliger derivative along stride s (unscaled by invdx).
+template <int ORDER, typename R, typename T>
+__device__ __forceinline__ R fd_ko(const T *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  R acc = (R)C::ko(0) * ld<T, R>(p, 0);
+#pragma unroll
+  for (int k = 1; k <= C::R + 1; k++) acc += (R)C::ko(k) * (ld<T, R>(p, k * s) + ld<T, R>(p, -k * s));
   return acc;
 }
 
@@ -147,6 +164,19 @@ template <int ORDER, typename R> __device__ __forceinline__ R fd_d2(const float2
     const float2 a = __ldg(p + k * s), b = __ldg(p - k * s);
     hi += (R)C::c2(k) * (((R)a.x - (R)c.x) + ((R)b.x - (R)c.x));
     lo += (R)C::c2(k) * ((R)a.y + (R)b.y);
+  }
+  return hi + lo;
+}
+// Kreiss-Oliger derivative over v[k] - v[0] (the weights sum to zero).
+template <int ORDER, typename R> __device__ __forceinline__ R fd_ko(const float2 *__restrict__ p, long long s) {
+  using C = FDCoef<ORDER>;
+  const float2 c = __ldg(p);
+  R hi = (R)0, lo = (R)C::ko(0) * (R)c.y;
+#pragma unroll
+  for (int k = 1; k <= C::R + 1; k++) {
+    const float2 a = __ldg(p + k * s), b = __ldg(p - k * s);
+    hi += (R)C::ko(k) * (((R)a.x - (R)c.x) + ((R)b.x - (R)c.x));
+    lo += (R)C::ko(k) * ((R)a.y + (R)b.y);
   }
   return hi + lo;
 }

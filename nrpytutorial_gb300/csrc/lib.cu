@@ -1,5 +1,6 @@
 // lib.cu -- library state (status messages, stream, launch counter), grid
 // set-up, CFL timestep and the reference-metric precompute tables.
+#include <cmath>
 #include <math.h>
 #include <stdarg.h>
 #include <string.h>
@@ -41,6 +42,7 @@ int check_params(const paramstruct *p) {
   const long long ntot =
       (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
   NRGPU_REQUIRE(ntot < (1LL << 31) / 32, "grid of %lld points too large for 32-bit gf indexing", ntot);
+  NRGPU_REQUIRE(std::isfinite(p->diss_strength), "diss_strength is not finite");
   return NRGPU_OK;
 }
 
@@ -81,10 +83,14 @@ long long nrgpu_kernel_launch_count(void) { return g_launches.load(); }
 
 int nrgpu_fd_coeffs(int order, int kind, double *out) {
   NRGPU_REQUIRE(out != nullptr, "out is NULL");
-  NRGPU_REQUIRE(kind >= 0 && kind <= 2, "kind must be 0, 1 or 2");
+  NRGPU_REQUIRE(kind >= 0 && kind <= 3, "kind must be 0, 1, 2 or 3");
   auto fill = [&](auto C) {
     using CC = decltype(C);
     const int R = CC::R;
+    if (kind == 3) {
+      for (int j = 0; j <= 2 * R + 2; j++) out[j] = CC::ko(j >= R + 1 ? j - R - 1 : R + 1 - j);
+      return;
+    }
     for (int j = 0; j <= 2 * R; j++) {
       const int k = j - R;
       if (kind == 0) out[j] = (k == 0) ? 0.0 : (k > 0 ? CC::c1(k) : -CC::c1(-k));

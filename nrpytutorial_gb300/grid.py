@@ -36,7 +36,7 @@ class Grid:
     """Numerical grid: paramstruct + cell-centred xx arrays (host, FP64)."""
 
     def __init__(self, CoordSystem, Nxx, FD_order=4, NGHOSTS=2, *, AMPL=10.0, SINHW=0.2,
-                 RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0):
+                 RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, diss_strength=0.0):
         lib = _lib.load()
         p = _lib.paramstruct()
         p.CoordSystem = _lib.COORD[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
@@ -47,6 +47,7 @@ class Grid:
         p.xmin = p.ymin = p.zmin = lo
         p.xmax = p.ymax = p.zmax = hi
         p.eta, p.wavespeed, p.time = eta, wavespeed, 0.0
+        p.diss_strength = diss_strength  # Kreiss-Oliger dissipation of the BSSN RHSs (0 = off)
         n = [int(v) for v in Nxx]
         np_ = [v + 2 * NGHOSTS for v in n]
         self.xx = [np.zeros(np_[d]) for d in range(3)]

@@ -393,9 +393,12 @@ def ricci_grid(gp, gfs):
     return out
 
 
-def rhs_grid(gp, gfs, RbarDD6=None):
+def rhs_grid(gp, gfs, RbarDD6=None, diss_strength=0.0):
     """rhs_eval: 24 RHSs at interior points (zero elsewhere).  RbarDD6, if
-    given, is the (6, n2, n1, n0) auxevol array (LeaveRicciSymbolic form)."""
+    given, is the (6, n2, n1, n0) auxevol array (LeaveRicciSymbolic form).
+    diss_strength != 0 adds Kreiss-Oliger dissipation to every RHS,
+    diss_strength * sum_k f_dKOD[k] * ReU[k]
+    (BaikalETK/BaikalETK_C_kernels_codegen.py:147-171)."""
     v, q = grid_symbols(gp, gfs, need_ricci=RbarDD6 is None)
     Rbar = None
     if RbarDD6 is not None:
@@ -404,8 +407,15 @@ def rhs_grid(gp, gfs, RbarDD6=None):
             Rbar[i, j] = Rbar[j, i] = gp.interior(RbarDD6[n])
     r = rhs(v, q, gp.eta, Rbar)
     out = np.zeros((24,) + gp.shape)
+    if diss_strength != 0.0:
+        S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+        ReU = q["ReU"]
     for n, name in enumerate(EVOL):
-        gp.interior(out[n])[...] = r[name]
+        val = r[name]
+        if diss_strength != 0.0:
+            ko = sum(S.dko(gfs[GF[name]], k) * ReU[k] for k in R3)
+            val = val + diss_strength * ko
+        gp.interior(out[n])[...] = val
     return out
 
 

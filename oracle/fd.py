@@ -54,6 +54,18 @@ def fd_weights(order, deriv, shift=0):
     return offs, w
 
 
+def ko_weights(order):
+    """Kreiss-Oliger dissipation weights for FD order `order`
+    (finite_difference.py:252-258, 310-313, 331-334): the (order+2)-th
+    derivative on order+3 points (FD_KO_ORDER__CENTDERIVS_PLUS = 2) times
+    (-1)**((order+4)/2) / 2**(order+2).  Offsets -(order/2+1) .. order/2+1;
+    the stencil is multiplied by invdx once (finite_difference_helpers.py:486)."""
+    n = order + 2
+    offs, w = fd_weights(n, n)
+    sign = -1 if ((n + 2) // 2) % 2 else 1
+    return offs, [sign * x / Fraction(2) ** n for x in w]
+
+
 def coeff_table(order):
     """Float coefficient table used by both the oracle and the C-ABI check."""
     c1 = fd_weights(order, 1)[1]
@@ -141,6 +153,13 @@ class Stencils:
             k = j - self.r - 1
             if w != 0.0:
                 acc = acc + w * self._shift(f, self._off(d, k))
+        return acc * self.invdx[d]
+
+    def dko(self, f, d):
+        """Kreiss-Oliger derivative ("_dKOD" symbols) along direction d."""
+        acc = 0.0
+        for k, w in zip(*ko_weights(self.order)):
+            acc = acc + float(w) * self._shift(f, self._off(d, k))
         return acc * self.invdx[d]
 
     def dupwind(self, f, d, control):

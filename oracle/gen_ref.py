@@ -13,7 +13,9 @@ start-to-finish drivers do, and writes the C that its code generator emits:
   rhs_eval / Ricci_eval / enforce_detgammabar_constraint /
   Hamiltonian_constraint / initial_data (BSSN; the no-rfm-precompute,
   Read_xxs forms of Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide-
-  no_rfm_precompute.ipynb), rhs_eval (ScalarWave, Maxwell System I),
+  no_rfm_precompute.ipynb), rhs_eval with Kreiss-Oliger dissipation
+  (BSSN_KO: the BSSN RHSs plus BaikalETK's diss_strength * f_dKOD * ReU
+  terms), rhs_eval (ScalarWave, Maxwell System I),
   plus its declare_Cparameters_struct.h / set_Cparameters*.h /
   gridfunction_defines.h.
 Nothing of the reference's source is copied: only what its generator prints.
@@ -38,6 +40,8 @@ CONFIGS = {
     "bssn_sph_fd4": ("BSSN", "Spherical", 4, 3),
     "bssn_cart_fd4": ("BSSN", "Cartesian", 4, 3),
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
+    "bssn_ko_sinhsph_fd4": ("BSSN_KO", "SinhSpherical", 4, 3),
+    "bssn_ko_cart_fd6": ("BSSN_KO", "Cartesian", 6, 4),
     "sw_cart_fd4": ("ScalarWave", "Cartesian", 4, 2),
     "sw_sinhsph_fd4": ("ScalarWave", "SinhSpherical", 4, 2),
     "maxwell_cart_fd4": ("Maxwell", "Cartesian", 4, 3),
@@ -68,11 +72,13 @@ def emit(name, params, body, loopopts):
     with open(os.path.join(OUTDIR, name + ".h"), "w") as f:
         f.write(txt)
 
-if SYSTEM == "BSSN":
-    import BSSN.BrillLindquist as bl
-    bl.BrillLindquist()
-    with open(os.path.join(OUTDIR, "initial_data.h"), "w") as f:
-        f.write(outC_function_dict["initial_data"])
+if SYSTEM in ("BSSN", "BSSN_KO"):
+    KO = SYSTEM == "BSSN_KO"
+    if not KO:
+        import BSSN.BrillLindquist as bl
+        bl.BrillLindquist()
+        with open(os.path.join(OUTDIR, "initial_data.h"), "w") as f:
+            f.write(outC_function_dict["initial_data"])
     import BSSN.BSSN_RHSs as rhs
     import BSSN.BSSN_gauge_RHSs as gaugerhs
     import BSSN.BSSN_quantities as Bq
@@ -99,6 +105,25 @@ if SYSTEM == "BSSN":
         for j in range(i, 3):
             lhs_names.append("aDD" + str(i) + str(j)); rhs_exprs.append(rhs.a_rhsDD[i][j])
             lhs_names.append("hDD" + str(i) + str(j)); rhs_exprs.append(rhs.h_rhsDD[i][j])
+    if KO:
+        # Kreiss-Oliger dissipation added to every evolved gridfunction's RHS
+        # the way BaikalETK/BaikalETK_C_kernels_codegen.py:147-171 adds it
+        # (diss_strength * sum_k f_dKOD[k] * ReU[k]; the 2nd-order shift
+        # condition, so betU is dissipated too).
+        import indexedexp as ixp
+        diss = par.Cparameters("REAL", "KO_Dissipation", "diss_strength", 0.1)
+        ko = {"alpha": ixp.declarerank1("alpha_dKOD"), "cf": ixp.declarerank1("cf_dKOD"),
+              "trK": ixp.declarerank1("trK_dKOD")}
+        for b in ("betU", "vetU", "lambdaU"):
+            t = ixp.declarerank2(b + "_dKOD", "nosym")
+            for i in range(3):
+                ko[b + str(i)] = t[i]
+        for b in ("aDD", "hDD"):
+            t = ixp.declarerank3(b + "_dKOD", "sym01")
+            for i in range(3):
+                for j in range(i, 3):
+                    ko[b + str(i) + str(j)] = t[i][j]
+        rhs_exprs = [e + sum(diss * ko[n][k] * rfm.ReU[k] for k in range(3)) for n, e in zip(lhs_names, rhs_exprs)]
     lhs_names, rhs_exprs = [list(x) for x in zip(*sorted(zip(lhs_names, rhs_exprs), key=lambda p: p[0]))]
     ev = [lhrh(lhs=gri.gfaccess("rhs_gfs", n), rhs=e) for n, e in zip(lhs_names, rhs_exprs)]
     emit("rhs_eval",
@@ -106,6 +131,11 @@ if SYSTEM == "BSSN":
          "const REAL *restrict in_gfs, REAL *restrict rhs_gfs",
          fin.FD_outputC("returnstring", ev, params="outCverbose=False", upwindcontrolvec=betaU).replace("IDX4", "IDX4S"),
          "InteriorPoints,Read_xxs")
+    if KO:
+        par.generate_Cparameters_Ccodes(OUTDIR)
+        gri.output__gridfunction_defines_h__return_gf_lists(OUTDIR)
+        print("generated", SYSTEM, COORD, FD)
+        sys.exit(0)
     R = Bq.RbarDD
     emit("Ricci_eval",
          "const paramstruct *restrict params, REAL *restrict xx[3], const REAL *restrict in_gfs, REAL *restrict auxevol_gfs",
@@ -160,7 +190,7 @@ def shim_source(system, ng, fields, funcs):
                         for t, n in fields)
     wr = []
     if "rhs_eval" in funcs:
-        if system == "BSSN":
+        if system.startswith("BSSN"):
             wr.append("void ref_rhs_eval(REAL *x0, REAL *x1, REAL *x2, const REAL *aux, const REAL *in, REAL *rhs)"
                       " { REAL *xx[3] = {x0, x1, x2}; rhs_eval(&params_, xx, aux, in, rhs); }")
         else:

@@ -14,7 +14,11 @@ Writes:
       on seeded inputs (tests/helpers.py bssn_random_state / numpy
       default_rng): Ricci, rhs_eval, Hamiltonian at interior points,
       enforce_detgammabar_constraint (hDD at all points), Brill-Lindquist
-      initial_data (interior points); rhs_eval for ScalarWave / Maxwell.
+      initial_data (interior points); rhs_eval for ScalarWave / Maxwell;
+      for bssn_ko_*: rhs_eval with Kreiss-Oliger dissipation on seeded
+      state and auxevol inputs.
+  fd_coefficients.json  exact FD coefficients of
+      finite_difference.compute_fdcoeffs_fdstencl (incl. Kreiss-Oliger).
   trusted_values.json  the reference's trusted-value unit tests for the
       hot-path expressions: md5-seeded symbol values (exactly as
       UnitTesting/cse_simplify_and_evaluate_sympy_expressions.py:53-67
@@ -46,7 +50,10 @@ FIXTURE_GRIDS = {
     "sw_cart_fd4": ("Cartesian", (6, 6, 6), 4, 2, 15),
     "sw_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 2, 16),
     "maxwell_cart_fd4": ("Cartesian", (6, 6, 6), 4, 3, 17),
+    "bssn_ko_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 18),
+    "bssn_ko_cart_fd6": ("Cartesian", (6, 6, 6), 6, 4, 19),
 }
+KO_DISS_STRENGTH = 0.3
 
 
 def senr_bc():
@@ -71,7 +78,16 @@ def ref_outputs():
         g = ng
         I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
         out = dict(seed=seed, Nxx=np.array(N), fd=fd, ng=ng)
-        if cfg.startswith("bssn"):
+        if cfg.startswith("bssn_ko"):
+            # rhs_eval with Kreiss-Oliger dissipation; RbarDD is an input
+            # (auxevol) of the generated rhs_eval, so any seeded values do.
+            R = RefKernels(cfg, gp, "strict", extra=dict(cart, diss_strength=KO_DISS_STRENGTH))
+            f = bssn_random_state(gp.shape, seed=seed)
+            aux = 0.1 * np.random.default_rng(seed + 100).standard_normal((6,) + gp.shape)
+            out["aux"] = aux
+            out["diss_strength"] = KO_DISS_STRENGTH
+            out["rhs"] = R.rhs_eval(f, aux=aux)[I]
+        elif cfg.startswith("bssn"):
             f = bssn_random_state(gp.shape, seed=seed)
             ric = R.ricci(f)
             out["ricci"] = ric[I]
@@ -85,6 +101,36 @@ def ref_outputs():
             out["rhs"] = R.rhs_eval(f)[I]
         np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % cfg), **out)
         print(cfg, {k: getattr(v, "shape", v) for k, v in out.items()})
+
+
+FD_WORKER = r'''
+import sys, json
+sys.dont_write_bytecode = True
+sys.path.insert(0, sys.argv[1])
+import NRPy_param_funcs as par
+import finite_difference as fin
+out = {}
+for order in (2, 4, 6, 8):
+    par.set_parval_from_str("finite_difference::FD_CENTDERIVS_ORDER", order)
+    for op in ("dD0", "dDD00", "dupD0", "ddnD0", "dKOD0"):
+        c, st = fin.compute_fdcoeffs_fdstencl(op)
+        out["%d_%s" % (order, op.rstrip("0"))] = {"offsets": [s[0] for s in st], "coeffs": [str(x) for x in c]}
+print(json.dumps(out))
+'''
+
+
+def fd_coeffs():
+    """fd_coefficients.json: finite_difference.compute_fdcoeffs_fdstencl's
+    exact coefficients and offsets (first, second, up/downwinded and
+    Kreiss-Oliger derivatives along x0) at FD orders 2, 4, 6, 8."""
+    r = subprocess.run([sys.executable, "-c", FD_WORKER, REF], capture_output=True, text=True,
+                       env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"), cwd="/tmp")
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-3000:])
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    with open(os.path.join(HERE, "fd_coefficients.json"), "w") as f:
+        json.dump(res, f, indent=0, sort_keys=True)
+    print("fd coefficients", len(res))
 
 
 # ------------------------------------------------------------ trusted values
@@ -181,6 +227,12 @@ def trusted():
 
 
 if __name__ == "__main__":
-    senr_bc()
-    ref_outputs()
-    trusted()
+    what = sys.argv[1:] or ["senr", "ref", "fd", "trusted"]
+    if "senr" in what:
+        senr_bc()
+    if "ref" in what:
+        ref_outputs()
+    if "fd" in what:
+        fd_coeffs()
+    if "trusted" in what:
+        trusted()

@@ -49,6 +49,17 @@ def test_fd_coefficients_match_vandermonde(order):
         assert np.array_equal(np.array(list(out)), np.array(ref[kind])), (order, kind)
 
 
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
+def test_kreiss_oliger_coefficients_match_oracle(order):
+    from oracle.fd import ko_weights
+    L, lib = _lib()
+    out = (C.c_double * (order + 3))()
+    L.check(lib.nrgpu_fd_coeffs(order, 3, out))
+    offs, w = ko_weights(order)
+    assert offs == list(range(-(order // 2 + 1), order // 2 + 2))
+    assert np.array_equal(np.array(list(out)), np.array([float(x) for x in w])), order
+
+
 @pytest.mark.parametrize("cs", ["Cartesian", "Spherical", "SinhSpherical"])
 def test_grid_setup_and_timestep_match_oracle(cs):
     from nrpytutorial_gb300 import Grid
@@ -78,6 +89,11 @@ def test_bad_arguments_return_status_not_abort():
     bad2.Nxx_plus_2NGHOSTS1 += 1
     assert lib.rfm_struct__malloc(C.byref(bad2), C.byref(L.rfm_struct())) == 1
     assert lib.nrgpu_fd_coeffs(3, 0, (C.c_double * 4)()) == 1
+    assert lib.nrgpu_fd_coeffs(4, 4, (C.c_double * 7)()) == 1
+    bad3 = L.paramstruct.from_buffer_copy(p)
+    bad3.diss_strength = float("nan")
+    assert lib.rfm_struct__malloc(C.byref(bad3), C.byref(L.rfm_struct())) == 1
+    assert b"diss_strength" in lib.nrgpu_last_error()
 
 
 def test_batch_create_validates_before_touching_the_device():

@@ -200,6 +200,39 @@ def test_oracle_matches_reference_generated_bssn(cfg):
     assert per_gf_rel(obs.enforce_detgammabar(gp, f)[11:17], z["enforce_hDD"]) < 1e-14
 
 
+@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd6", "Cartesian")])
+def test_oracle_kreiss_oliger_matches_reference_generated_bssn(cfg, cs):
+    """rhs_eval with Kreiss-Oliger dissipation on every gridfunction
+    (reference-generated C of the BaikalETK construction) against the
+    oracle; the dissipation term itself is a sizeable part of the RHS."""
+    z = np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))
+    gp = og.GridParams(cs, tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    diss = float(z["diss_strength"])
+    got = obs.rhs_grid(gp, f, RbarDD6=z["aux"], diss_strength=diss)[I]
+    assert per_gf_rel(got, z["rhs"]) < 1e-13
+    plain = obs.rhs_grid(gp, f, RbarDD6=z["aux"])[I]
+    assert per_gf_rel(plain, z["rhs"]) > 1e-6
+
+
+def test_oracle_fd_coefficients_match_reference_exactly():
+    """Exact rational weights of finite_difference.compute_fdcoeffs_fdstencl
+    (first, second, dupD, ddnD and Kreiss-Oliger derivatives, orders 2-8)."""
+    from fractions import Fraction
+    from oracle.fd import fd_weights, ko_weights
+    want = json.load(open(os.path.join(GOLD, "fd_coefficients.json")))
+    for order in (2, 4, 6, 8):
+        cases = {"dD": fd_weights(order, 1), "dDD": fd_weights(order, 2), "dupD": fd_weights(order, 1, +1),
+                 "ddnD": fd_weights(order, 1, -1), "dKOD": ko_weights(order)}
+        for op, (offs, w) in cases.items():
+            nz = [(o, c) for o, c in zip(offs, w) if c != 0]
+            ref = want["%d_%s" % (order, op)]
+            assert [o for o, _ in nz] == ref["offsets"], (order, op)
+            assert [c for _, c in nz] == [Fraction(x) for x in ref["coeffs"]], (order, op)
+
+
 @pytest.mark.parametrize("cfg,cs,fn,ngf", [("sw_cart_fd4", "Cartesian", ow.scalarwave_rhs_grid, 2),
                                           ("sw_sinhsph_fd4", "SinhSpherical", ow.scalarwave_rhs_grid, 2),
                                           ("maxwell_cart_fd4", "Cartesian", ow.maxwell_rhs_grid, 7)])

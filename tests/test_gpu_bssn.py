@@ -187,3 +187,94 @@ def test_cuda_graph_replay_matches_eager_steps(cuda):
     replay()
     torch.cuda.synchronize()
     assert torch.equal(ev.y_n, eager)
+
+
+KO_DISS = 0.25
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_kreiss_oliger_rhs_matches_oracle(cuda, coord, Nxx, order):
+    """diss_strength != 0 adds Kreiss-Oliger dissipation to all 24 RHSs."""
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    G, gp = grids("BSSN", coord, Nxx, order, diss_strength=KO_DISS, **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    f = bssn_random_state(gp.shape, seed=41 + order)
+    t = torch.tensor(f, device=cuda)
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+    out = torch.zeros_like(t)
+    ev.rhs_eval(t, out, auxevol=aux)
+    ref = obs.rhs_grid(gp, f, diss_strength=KO_DISS)
+    assert per_gf_rel(out.cpu().numpy(), ref, gp.NGHOSTS) < FP64_TOL
+    assert per_gf_rel(obs.rhs_grid(gp, f), ref, gp.NGHOSTS) > 1e-4  # the term is not negligible
+
+
+def test_kreiss_oliger_fp32_rhs(cuda):
+    """The FP32 instantiation (plain FP32 stage input); the (hi, lo) pair
+    instantiation is checked through the compensated RK4 step below."""
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    coord, Nxx, order = CASES[2]
+    G, gp = grids("BSSN", coord, Nxx, order, diss_strength=KO_DISS, **KW)
+    ev = Evolution("BSSN", G, precision="mixed", device=cuda)
+    f = bssn_random_state(gp.shape, seed=7, amp=0.05).astype(np.float32)
+    t = torch.tensor(f, device=cuda)
+    aux = torch.zeros((6,) + gp.shape, dtype=torch.float32, device=cuda)
+    out = torch.zeros_like(t)
+    ev.rhs_eval(t, out, auxevol=aux)
+    ref = obs.rhs_grid(gp, f.astype(np.float64), diss_strength=KO_DISS)
+    assert per_gf_rel(out.double().cpu().numpy(), ref, gp.NGHOSTS) < FP32_TOL
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("compensated", 1e-6)])
+@pytest.mark.parametrize("fused", [True, False])
+def test_kreiss_oliger_rk4_step_matches_oracle(cuda, prec, tol, fused):
+    import torch
+    from nrpytutorial_gb300 import SYSTEM_GFS, Evolution
+    coord, Nxx, order = CASES[2]
+    G, gp = grids("BSSN", coord, Nxx, order, diss_strength=KO_DISS, **KW)
+    ev = Evolution("BSSN", G, precision=prec, device=cuda)
+    parity = SYSTEM_GFS["BSSN"][1]
+    layers = ob.build_bcstruct(gp)
+
+    def post(x):
+        ob.apply_bcs(layers, x, parity)
+        x[...] = obs.enforce_detgammabar(gp, x)
+
+    y = bssn_random_state(gp.shape, seed=43, amp=0.02)
+    post(y)
+    ev.y_n.copy_(torch.tensor(y, device=cuda))
+    dt = 0.05 * min(gp.dxx)
+    ev.step(dt, fused=fused)
+    yo, _, _ = ob.rk4_step(y, dt, lambda u: obs.rhs_grid(gp, u, diss_strength=KO_DISS), post, gp.NGHOSTS)
+    assert per_gf_rel(ev.y_n.cpu().numpy(), yo) < tol
+
+
+def test_kreiss_oliger_damps_the_grid_scale_mode(cuda):
+    """The dissipation is dissipative: on flat space plus a checkerboard in
+    trK (the grid-scale mode, where every KO stencil gives -1 x f) the
+    dissipated RHS differs from the plain one by exactly
+    -diss_strength * (invdx0 + invdx1 + invdx2) * trK, and nowhere else."""
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    from oracle.bssn import GF
+    coord, Nxx, order = "Cartesian", (12, 10, 8), 4
+    outs = {}
+    for diss in (0.0, 0.5):
+        G, gp = grids("BSSN", coord, Nxx, order, diss_strength=diss, **KW)
+        ev = Evolution("BSSN", G, device=cuda)
+        y = bssn_random_state(gp.shape, seed=1, amp=0.0)
+        i2, i1, i0 = np.indices(gp.shape)
+        y[GF["trK"]] += 1e-3 * (-1.0) ** (i0 + i1 + i2)
+        t = torch.tensor(y, device=cuda)
+        aux = torch.zeros((6,) + gp.shape, dtype=torch.float64, device=cuda)
+        out = torch.zeros_like(t)
+        ev.rhs_eval(t, out, auxevol=aux)
+        outs[diss] = out.cpu().numpy()
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    d = (outs[0.5] - outs[0.0])[I]
+    want = -0.5 * sum(gp.invdx) * y[GF["trK"]][I[1:]]
+    assert np.allclose(d[GF["trK"]], want, rtol=1e-12, atol=0.0)
+    others = [k for k in range(24) if k != GF["trK"]]
+    assert np.abs(d[others]).max() <= 1e-14

@@ -51,6 +51,37 @@ def test_bssn_matches_reference_generated_c(cuda, cfg):
     assert per_gf_rel(t2.cpu().numpy()[11:17], z["enforce_hDD"]) < 1e-14
 
 
+@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd6", "Cartesian")])
+def test_kreiss_oliger_rhs_matches_reference_generated_c(cuda, cfg, cs):
+    """rhs_eval with Kreiss-Oliger dissipation (diss_strength in the
+    paramstruct) against the reference's generated C of the same RHSs, on
+    both the table path (BSSN_rhs_eval) and the no-precompute signature
+    (BSSN_rhs_eval_xx)."""
+    import ctypes as C
+    import torch
+    from nrpytutorial_gb300 import Evolution, _lib
+    from bench import _rhs_only
+    z = _load(cfg)
+    diss = float(z["diss_strength"])
+    G, gp = grids("BSSN", cs, tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]), diss_strength=diss, **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    t = torch.tensor(f, device=cuda)
+    aux = torch.tensor(z["aux"], device=cuda)
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    out = torch.zeros_like(t)
+    _rhs_only(ev, t, aux, out)
+    assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
+    xx = [torch.tensor(np.asarray(G.xx[d]), dtype=torch.float64, device=cuda) for d in range(3)]
+    xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
+    out_xx = torch.zeros_like(t)
+    _lib.check(ev.lib.BSSN_rhs_eval_xx(C.byref(G.params), xxp, _lib.ptr(aux), _lib.ptr(t), _lib.ptr(out_xx)),
+               "BSSN_rhs_eval_xx")
+    torch.cuda.synchronize()
+    assert per_gf_rel(out_xx.cpu().numpy()[I], z["rhs"]) < TOL
+
+
 @pytest.mark.parametrize("cfg", sorted(CFGS))
 def test_brill_lindquist_matches_reference_initial_data(cuda, cfg):
     import torch
