@@ -15,7 +15,8 @@ start-to-finish drivers do, and writes the C that its code generator emits:
   Read_xxs forms of Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide-
   no_rfm_precompute.ipynb), rhs_eval with Kreiss-Oliger dissipation
   (BSSN_KO: the BSSN RHSs plus BaikalETK's diss_strength * f_dKOD * ReU
-  terms), rhs_eval (ScalarWave, Maxwell System I),
+  terms), psi4_eval (BSSN_PSI4: psi_4 in the quasi-Kinnersley tetrad, six
+  pieces), rhs_eval (ScalarWave, Maxwell System I),
   plus its declare_Cparameters_struct.h / set_Cparameters*.h /
   gridfunction_defines.h.
 Nothing of the reference's source is copied: only what its generator prints.
@@ -42,6 +43,7 @@ CONFIGS = {
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
     "bssn_ko_sinhsph_fd4": ("BSSN_KO", "SinhSpherical", 4, 3),
     "bssn_ko_cart_fd6": ("BSSN_KO", "Cartesian", 6, 4),
+    "bssn_psi4_sph_fd4": ("BSSN_PSI4", "Spherical", 4, 3),
     "sw_cart_fd4": ("ScalarWave", "Cartesian", 4, 2),
     "sw_sinhsph_fd4": ("ScalarWave", "SinhSpherical", 4, 2),
     "maxwell_cart_fd4": ("Maxwell", "Cartesian", 4, 3),
@@ -150,6 +152,24 @@ if SYSTEM in ("BSSN", "BSSN_KO"):
                         params="outCverbose=False").replace("IDX4", "IDX4S"),
          "InteriorPoints,Read_xxs")
     EGC.output_Enforce_Detgammabar_Constraint_Ccode(OUTDIR, exprs=enf, Read_xxs=True)
+elif SYSTEM == "BSSN_PSI4":
+    # psi_4 with the quasi-Kinnersley tetrad, real and imaginary parts in the
+    # reference's three pieces each, as the Two_BHs_Collide-Psi4 driver
+    # generates them (one FD_outputC per piece, CSE_sorting=none).
+    import BSSN.Psi4_tetrads as BP4t
+    par.set_parval_from_str("BSSN.Psi4_tetrads::TetradChoice", "QuasiKinnersley")
+    import BSSN.Psi4 as BP4
+    BP4.Psi4()
+    names = ["psi4r_0pt", "psi4r_1pt", "psi4r_2pt", "psi4i_0pt", "psi4i_1pt", "psi4i_2pt"]
+    gri.register_gridfunctions("AUX", names)
+    exprs = BP4.psi4_re_pt + BP4.psi4_im_pt
+    body = ""
+    for n, e in zip(names, exprs):
+        body += "{\n" + fin.FD_outputC("returnstring", lhrh(lhs=gri.gfaccess("aux_gfs", n), rhs=e),
+                                        params="outCverbose=False,CSE_sorting=none") + "}\n"
+    emit("psi4_eval",
+         "const paramstruct *restrict params, REAL *restrict xx[3], const REAL *restrict in_gfs, REAL *restrict aux_gfs",
+         body.replace("IDX4", "IDX4S"), "InteriorPoints,Read_xxs")
 elif SYSTEM == "ScalarWave":
     if COORD == "Cartesian":
         import ScalarWave.ScalarWave_RHSs as sw
@@ -205,6 +225,9 @@ def shim_source(system, ng, fields, funcs):
     if "enforce_detgammabar_constraint" in funcs:
         wr.append("void ref_enforce_detgammabar_constraint(REAL *x0, REAL *x1, REAL *x2, REAL *in)"
                   " { REAL *xx[3] = {x0, x1, x2}; enforce_detgammabar_constraint(&params_, xx, in); }")
+    if "psi4_eval" in funcs:
+        wr.append("void ref_psi4_eval(REAL *x0, REAL *x1, REAL *x2, const REAL *in, REAL *aux)"
+                  " { REAL *xx[3] = {x0, x1, x2}; psi4_eval(&params_, xx, in, aux); }")
     if "initial_data" in funcs:
         wr.append("void ref_initial_data(REAL *x0, REAL *x1, REAL *x2, REAL *in)"
                   " { REAL *xx[3] = {x0, x1, x2}; initial_data(&params_, xx, in); }")
@@ -265,7 +288,7 @@ def generate(name):
     if r.returncode != 0:
         raise RuntimeError("%s: reference codegen failed:\n%s" % (name, r.stderr[-4000:]))
     funcs = [f for f in ("rhs_eval", "Ricci_eval", "Hamiltonian_constraint", "enforce_detgammabar_constraint",
-                         "initial_data") if os.path.exists(os.path.join(d, f + ".h"))]
+                         "initial_data", "psi4_eval") if os.path.exists(os.path.join(d, f + ".h"))]
     fields = parse_fields(os.path.join(d, "declare_Cparameters_struct.h"))
     with open(os.path.join(d, "shim.c"), "w") as f:
         f.write(shim_source(system, ng, fields, funcs))

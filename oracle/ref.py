@@ -72,6 +72,13 @@ class RefKernels:
         self.lib.ref_enforce_detgammabar_constraint(*self._x(), self._p(g))
         return g
 
+    def psi4(self, in_gfs):
+        """psi4_eval: (re, im) sums of the six generated pieces (aux order
+        psi4i_0pt..2pt, psi4r_0pt..2pt) and the pieces themselves."""
+        aux = np.zeros((6,) + in_gfs.shape[1:])
+        self.lib.ref_psi4_eval(*self._x(), self._p(in_gfs), self._p(aux))
+        return np.array([aux[3] + aux[4] + aux[5], aux[0] + aux[1] + aux[2]]), aux
+
     def initial_data(self, shape24):
         g = np.zeros(shape24)
         self.lib.ref_initial_data(*self._x(), self._p(g))

@@ -16,7 +16,9 @@ Writes:
       enforce_detgammabar_constraint (hDD at all points), Brill-Lindquist
       initial_data (interior points); rhs_eval for ScalarWave / Maxwell;
       for bssn_ko_*: rhs_eval with Kreiss-Oliger dissipation on seeded
-      state and auxevol inputs.
+      state and auxevol inputs; for bssn_psi4_*: the six pieces of psi_4.
+  swsh_m2.json  the reference's generated spin-weight -2 spherical
+      harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
       finite_difference.compute_fdcoeffs_fdstencl (incl. Kreiss-Oliger).
   trusted_values.json  the reference's trusted-value unit tests for the
@@ -52,6 +54,7 @@ FIXTURE_GRIDS = {
     "maxwell_cart_fd4": ("Cartesian", (6, 6, 6), 4, 3, 17),
     "bssn_ko_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 18),
     "bssn_ko_cart_fd6": ("Cartesian", (6, 6, 6), 6, 4, 19),
+    "bssn_psi4_sph_fd4": ("Spherical", (8, 6, 4), 4, 3, 20),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -78,7 +81,13 @@ def ref_outputs():
         g = ng
         I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
         out = dict(seed=seed, Nxx=np.array(N), fd=fd, ng=ng)
-        if cfg.startswith("bssn_ko"):
+        if cfg.startswith("bssn_psi4"):
+            # psi_4 (quasi-Kinnersley tetrad) of a seeded state; the six
+            # generated pieces are stored, re = pieces 3..5, im = 0..2
+            f = bssn_random_state(gp.shape, seed=seed)
+            _, parts = R.psi4(f)
+            out["psi4_parts"] = parts[I]
+        elif cfg.startswith("bssn_ko"):
             # rhs_eval with Kreiss-Oliger dissipation; RbarDD is an input
             # (auxevol) of the generated rhs_eval, so any seeded values do.
             R = RefKernels(cfg, gp, "strict", extra=dict(cart, diss_strength=KO_DISS_STRENGTH))
@@ -133,6 +142,59 @@ def fd_coeffs():
     print("fd coefficients", len(res))
 
 
+SWSH_WORKER = r'''
+import os, sys
+sys.dont_write_bytecode = True
+sys.path.insert(0, sys.argv[1])
+os.chdir(sys.argv[2])
+import SpinWeight_minus2_SphHarmonics.SpinWeight_minus2_SphHarmonics as S
+S.SpinWeight_minus2_SphHarmonics(maximum_l=8, filename=os.path.join(sys.argv[2], "swsh.h"))
+'''
+
+SWSH_MAIN = r"""
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#define REAL double
+#include "swsh.h"
+int main(void) {
+  const double th[5] = {0.05, 0.7, 1.5707963267948966, 2.2, 3.1};
+  const double ph[5] = {-3.0, -0.4, 0.0, 1.3, 2.9};
+  for (int l = 0; l <= 8; l++)
+    for (int m = -l; m <= l; m++)
+      for (int p = 0; p < 5; p++) {
+        double re, im;
+        SpinWeight_minus2_SphHarmonics(l, m, th[p], ph[p], &re, &im);
+        printf("%d %d %.17g %.17g %.17g %.17g\n", l, m, th[p], ph[p], re, im);
+      }
+  return 0;
+}
+"""
+
+
+def swsh():
+    """swsh_m2.json: the reference-generated C of
+    SpinWeight_minus2_SphHarmonics (l <= 8, s = -2) evaluated at five
+    (theta, phi) points for every (l, m)."""
+    import tempfile
+    d = tempfile.mkdtemp()
+    r = subprocess.run([sys.executable, "-c", SWSH_WORKER, REF, d], capture_output=True, text=True,
+                       env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"))
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-3000:])
+    with open(os.path.join(d, "main.c"), "w") as f:
+        f.write(SWSH_MAIN)
+    exe = os.path.join(d, "swsh")
+    subprocess.run(["gcc", "-O2", "-fno-fast-math", "-I" + d, os.path.join(d, "main.c"), "-o", exe, "-lm"],
+                   check=True)
+    rows = [ln.split() for ln in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+            if ln.strip()]
+    out = [[int(a[0]), int(a[1])] + [float(x) for x in a[2:]] for a in rows]
+    with open(os.path.join(HERE, "swsh_m2.json"), "w") as f:
+        json.dump(out, f)
+    print("swsh", len(out))
+
+
 # ------------------------------------------------------------ trusted values
 TRUSTED = [
     # (name, module-relative trusted dict file, dict key, init code, call, globals)
@@ -160,6 +222,12 @@ TRUSTED = [
      "par.initialize_param(par.glb_param('char', 'Maxwell.InitialData','System_to_use','System_I'))\n"
      "import Maxwell.VacuumMaxwell_Flat_Evol_Cartesian as M", "M.VacuumMaxwellRHSs()",
      ["ArhsU", "ErhsU", "C", "psi_rhs"]),
+]
+TRUSTED += [
+    ("Psi4", "BSSN", "Psi4__Psi4__specify_tetrad_False__globals",
+     "import BSSN.Psi4 as M", "M.Psi4(specify_tetrad=False)", ["psi4_re_pt", "psi4_im_pt"]),
+    ("Psi4_tetrads", "BSSN", "Psi4_tetrads__Psi4_tetrads__globals",
+     "import BSSN.Psi4_tetrads as M", "M.Psi4_tetrads()", ["l4U", "n4U", "mre4U", "mim4U"]),
 ]
 for cs in ("Spherical", "SinhSpherical", "Cartesian"):
     TRUSTED.append(("rfm_" + cs, "tests", "rfm_%s__reference_metric__True__globals" % cs,
@@ -202,10 +270,13 @@ print(json.dumps({"inputs": vals, "names": sorted(exprs)}))
 '''
 
 
-def trusted():
+def trusted(only=None):
     import importlib.util
-    out = {}
+    path_json = os.path.join(HERE, "trusted_values.json")
+    out = json.load(open(path_json)) if only and os.path.exists(path_json) else {}
     for name, mod, key, init, call, globs in TRUSTED:
+        if only and name not in only:
+            continue
         spec = json.dumps({"init": init, "call": call, "globals": globs})
         r = subprocess.run([sys.executable, "-c", WORKER, REF, spec], capture_output=True, text=True,
                            env=dict(os.environ, PYTHONDONTWRITEBYTECODE="1"), cwd="/tmp")
@@ -227,12 +298,17 @@ def trusted():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["senr", "ref", "fd", "trusted"]
+    what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted"]
     if "senr" in what:
         senr_bc()
     if "ref" in what:
         ref_outputs()
     if "fd" in what:
         fd_coeffs()
+    if "swsh" in what:
+        swsh()
     if "trusted" in what:
         trusted()
+    names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
+    if names:
+        trusted(names)

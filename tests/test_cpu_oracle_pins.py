@@ -139,6 +139,50 @@ def test_trusted_momentum_constraint():
         assert close(M[i, 0], want, 1e-11), (i, M[i, 0], want)
 
 
+def _complex(sv):
+    return complex(sv.replace(" ", ""))
+
+
+def test_trusted_psi4_with_symbolic_tetrad():
+    """Psi4(specify_tetrad=False): psi_4's six pieces from md5-seeded BSSN
+    symbols, reference-metric coordinates and tetrad components."""
+    import oracle.psi4 as op
+    inp = TV["Psi4"]["inputs"]
+    v = symbols(inp, ["hDD", "aDD", "cf", "trK"])
+    q = og.hatted_at("Spherical", inp.get("xx0", 0.0), inp.get("xx1", 0.0))
+    q = {k: a[..., 0] for k, a in q.items()}
+    adm = op.adm_from_bssn(v, q)
+    tet = {b: [np.array([inp.get("%s%d" % (b, m), 0.0)]) for m in range(4)] for b in ("n4U", "mre4U", "mim4U")}
+    re, im = op.psi4_parts(adm, tet["n4U"], tet["mre4U"], tet["mim4U"])
+    ex = TV["Psi4"]["expected"]
+    for part in range(3):
+        assert close(float(re[part][0]), float(ex["psi4_re_pt[%d]" % part]), 1e-11), part
+        assert close(float(im[part][0]), float(ex["psi4_im_pt[%d]" % part]), 1e-11), part
+
+
+def test_trusted_psi4_tetrads():
+    """Psi4_tetrads(): the quasi-Kinnersley tetrad from md5-seeded hDD, cf
+    and Spherical coordinates (for these random values the metric is not
+    positive definite and some normalisations are imaginary, as in the
+    reference's own trusted values)."""
+    import oracle.psi4 as op
+    inp = TV["Psi4_tetrads"]["inputs"]
+    x0, x1, x2 = inp["xx0"], inp["xx1"], inp["xx2"]
+    q = og.hatted_at("Spherical", x0, x1)
+    q = {k: a[..., 0] for k, a in q.items()}
+    h = np.zeros((3, 3, 1))
+    for (i, j) in [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]:
+        h[i, j] = h[j, i] = inp.get("hDD%d%d" % (i, j), 0.0)
+    gamma = (h * q["ReDD"] + q["ghatDD"]) / inp["cf"] ** 2
+    l4, n4, mre, mim = op.tetrad(gamma, og.SPH, np.array([x0]), np.array([x1]), np.array([x2]))
+    got = {"l4U": l4, "n4U": n4, "mre4U": mre, "mim4U": mim}
+    for k, sv in TV["Psi4_tetrads"]["expected"].items():
+        base, idx = k.split("[")
+        g = complex(np.ravel(got[base][int(idx[0])])[0])
+        w = _complex(sv)
+        assert abs(g - w) <= 1e-12 * max(abs(w), 1.0), (k, g, w)
+
+
 @pytest.mark.parametrize("case,cart", [("ScalarWave_RHSs", True), ("ScalarWaveCurvilinear_RHSs", False)])
 def test_trusted_scalarwave(case, cart):
     inp = TV[case]["inputs"]
@@ -231,6 +275,32 @@ def test_oracle_fd_coefficients_match_reference_exactly():
             ref = want["%d_%s" % (order, op)]
             assert [o for o, _ in nz] == ref["offsets"], (order, op)
             assert [c for _, c in nz] == [Fraction(x) for x in ref["coeffs"]], (order, op)
+
+
+def test_oracle_psi4_matches_reference_generated_c():
+    """psi_4 on a seeded Spherical FD4 grid against the reference's own
+    generated psi4 C (quasi-Kinnersley tetrad, six pieces summed)."""
+    import oracle.psi4 as op
+    z = np.load(os.path.join(GOLD, "ref_bssn_psi4_sph_fd4.npz"))
+    gp = og.GridParams("Spherical", tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    g = gp.NGHOSTS
+    got = op.psi4_grid(gp, f)[:, g:-g, g:-g, g:-g]
+    parts = z["psi4_parts"]
+    want = np.array([parts[3] + parts[4] + parts[5], parts[0] + parts[1] + parts[2]])
+    assert per_gf_rel(got, want) < 1e-12
+
+
+def test_oracle_swsh_matches_reference_generated_c():
+    """Goldberg's formula (s = -2, l <= 8) against the reference's generated
+    SpinWeight_minus2_SphHarmonics C at five (theta, phi) points."""
+    import oracle.psi4 as op
+    rows = json.load(open(os.path.join(GOLD, "swsh_m2.json")))
+    assert len(rows) == 5 * 81
+    for l, m, th, ph, re, im in rows:
+        r, i = op.swsh_m2(l, m, th, ph)
+        scale = max(abs(re), abs(im), 1e-2)  # harmonics are O(1): absolute 1e-14 near their zeros
+        assert abs(float(r) - re) <= 1e-12 * scale and abs(float(i) - im) <= 1e-12 * scale, (l, m, th, ph)
 
 
 @pytest.mark.parametrize("cfg,cs,fn,ngf", [("sw_cart_fd4", "Cartesian", ow.scalarwave_rhs_grid, 2),
