@@ -266,6 +266,25 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *params
 int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
                              const double *in_gfs, double *aux_gfs);
 
+/* psi_4 in the quasi-Kinnersley tetrad (BSSN/Psi4.py:14-193 with
+ * BSSN/Psi4_tetrads.py:25-193; the reference's psi4() of
+ * Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide-Psi4.ipynb writes
+ * it as six pieces psi4r_0pt..2pt, psi4i_0pt..2pt): Re psi_4 into
+ * psi4_gfs[0], Im psi_4 into psi4_gfs[1] (two gridfunctions of the grid), at
+ * interior points with i0_min <= i0 < i0_max (a radial shell or slab; pass
+ * -1, -1 for the whole interior).  FP64. */
+int BSSN_psi4(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs, double *psi4_gfs,
+              int i0_min, int i0_max);
+/* Spin-weight -2 spherical-harmonic modes of psi_4 on the shell i0 of a
+ * Spherical/SinhSpherical grid (driver_psi4_spinweightm2_decomposition and
+ * lowlevel_decompose_psi4_into_swm2_modes of the same notebook;
+ * SpinWeight_minus2_SphHarmonics.py): modes[2q], modes[2q+1] = Re, Im of
+ * sum over interior (theta, phi) of psi4 conj(sY_lm) sin(theta) dxx1 dxx2,
+ * q running over l = 2..l_max (<= 12), m = -l..l.  modes: device, 2 *
+ * ((l_max+1)^2 - 4) doubles.  psi4_gfs as written by BSSN_psi4. */
+int BSSN_psi4_spinweightm2_decomposition(const paramstruct *params, const double *psi4_gfs, int i0, int l_max,
+                                         double *modes);
+
 /* --------------------------------------------------------- initial data */
 /* ScalarWave initial data at ALL points (ScalarWave/InitialData.py:27-88):
  * kind 0 PlaneWave (uu = sin(khat.x - c t) + 2, vv = d uu/dt, khat = kk/|kk|),

@@ -97,6 +97,8 @@ _PROTOS = {
     "BSSN_Ricci_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp]),
     "BSSN_rhs_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp, vp]),
     "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "BSSN_psi4": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp, C.c_int, C.c_int]),
+    "BSSN_psi4_spinweightm2_decomposition": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp]),
     "ScalarWave_initial_data": (C.c_int, [P(paramstruct), C.c_int, C.c_double, P(C.c_double), C.c_double, vp]),
     "BSSN_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double),
                                                    C.c_double, P(C.c_double), vp]),

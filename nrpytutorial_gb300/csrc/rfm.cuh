@@ -115,6 +115,9 @@ template <int CS, typename R, bool LOCAL = false> struct Rfm {
   __device__ __forceinline__ R ghatDDdD(int i, int j, int k) const {
     return q(rq::ghatDDdD + 9 * i + 3 * j + k);
   }
+  __device__ __forceinline__ R ghatDDdDD(int i, int j, int k, int l) const {
+    return q(rq::ghatDDdDD + 27 * i + 9 * j + 3 * k + l);
+  }
   __device__ __forceinline__ R G(int i, int k, int l) const {
     return q(rq::GammahatUDD + 9 * i + 3 * k + l);
   }

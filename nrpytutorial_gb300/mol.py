@@ -215,6 +215,41 @@ class Evolution:
                                                      _lib.ptr(M)), "BSSN_momentum_constraint")
         return M
 
+    def psi4(self, gfs=None, i0_range=None, out=None):
+        """psi_4 (quasi-Kinnersley tetrad) as 2 gridfunctions (Re, Im) at
+        interior points, optionally only for i0 in [i0_range[0], i0_range[1])
+        (an extraction shell).  FP64 state in, FP64 out."""
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        if out is None:
+            out = torch.zeros((2,) + self.grid.shape, dtype=torch.float64, device=self.device)
+        lo, hi = (-1, -1) if i0_range is None else (int(i0_range[0]), int(i0_range[1]))
+        _lib.check(self.lib.BSSN_psi4(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs), _lib.ptr(out), lo, hi),
+                   "BSSN_psi4")
+        return out
+
+    def psi4_modes(self, i0, l_max=8, gfs=None):
+        """Spin-weight -2 modes of psi_4 on the shell of radial index i0:
+        returns ({(l, m): complex}, extraction radius).  psi_4 is evaluated
+        on that shell only."""
+        import numpy as np
+        p4 = self.psi4(gfs, (i0, i0 + 1))
+        n_modes = (l_max + 1) ** 2 - 4
+        modes = torch.zeros(2 * n_modes, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.BSSN_psi4_spinweightm2_decomposition(C.byref(self.grid.params), _lib.ptr(p4), int(i0),
+                                                                 int(l_max), _lib.ptr(modes)),
+                   "BSSN_psi4_spinweightm2_decomposition")
+        v = modes.cpu().numpy()
+        out, q = {}, 0
+        for l in range(2, l_max + 1):
+            for m in range(-l, l + 1):
+                out[(l, m)] = complex(v[2 * q], v[2 * q + 1])
+                q += 1
+        x0 = float(self.grid.xx[0][i0])
+        p = self.grid.params
+        r = x0 if p.CoordSystem == 1 else p.AMPL * np.sinh(x0 / p.SINHW) / np.sinh(1.0 / p.SINHW)
+        return out, r
+
     def maxwell_constraint(self, gfs=None):
         self._sync_stream()
         gfs = self.y_n if gfs is None else gfs
