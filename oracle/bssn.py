@@ -319,6 +319,61 @@ def momentum(v, q):
     return MU * cf * cf / q["ReU"]
 
 
+# ----------------------------------------------------- T^{mu nu} sources
+T4 = [(0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3), (2, 2), (2, 3), (3, 3)]
+
+
+def t4uu_full(T10):
+    """(10, ...) T4UU00, 01, 02, 03, 11, 12, 13, 22, 23, 33 -> (4, 4, ...)."""
+    T = np.empty((4, 4) + np.shape(T10)[1:])
+    for n, (a, b) in enumerate(T4):
+        T[a, b] = T[b, a] = T10[n]
+    return T
+
+
+def stress_energy(v, q, T):
+    """BSSN_stress_energy_source_terms.py:24-85 (inputvars "BSSN") with
+    ADMBSSN_tofrom_4metric.py:38-68: S_ij, S_i, S, rho from T^{mu nu} (4, 4,
+    ...), with gamma_ij = gammabar_ij / W^2, beta^i = vet^i ReU^i and the
+    spatial projector gamma4_{mu nu} = g4_{mu nu} + n_mu n_nu, n_mu = (-alpha, 0, 0, 0)."""
+    alpha = v["alpha"]
+    gbar = v["hDD"] * q["ReDD"] + q["ghatDD"]
+    g = gbar / v["cf"] ** 2
+    beta = v["vetU"] * q["ReU"]
+    betaD = np.einsum("ij...,j...->i...", g, beta)
+    # gamma4[i+1][0] = beta_i, gamma4[i+1][k+1] = gamma_ik
+    P = np.empty((3, 4) + np.shape(alpha))
+    P[:, 0] = betaD
+    P[:, 1:] = g
+    SDD = np.einsum("im...,jn...,mn...->ij...", P, P, T)
+    SD = alpha * np.einsum("im...,m...->i...", P, T[:, 0])
+    gUU, _ = inv3(g)
+    S = np.einsum("ij...,ij...->...", gUU, SDD)
+    rho = alpha * alpha * T[0, 0]
+    return SDD, SD, S, rho
+
+
+def source_terms(v, q, T, PI=np.pi):
+    """BSSN_stress_energy_source_terms.py:88-131 added to the RHSs as the
+    BaikalETK drivers add them (BaikalETK_C_kernels_codegen.py:133-145,
+    before the gauge RHSs, so the Gamma-driver's B picks up 3/4 of the
+    Lambdabar source): returns {gf name: term}."""
+    SDD, SD, S, rho = stress_energy(v, q, T)
+    alpha, cf = v["alpha"], v["cf"]
+    gbar = v["hDD"] * q["ReDD"] + q["ghatDD"]
+    gbUU, _ = inv3(gbar)
+    trS = np.einsum("km...,km...->...", gbUU, SDD)
+    out = {"trK": 4 * PI * alpha * (rho + S)}
+    for (i, j) in SYM:
+        tf = SDD[i, j] - gbar[i, j] * trS / 3.0
+        out["aDD%d%d" % (i, j)] = -8 * PI * alpha * cf * cf * tf / q["ReDD"][i, j]
+    LamU = -16 * PI * alpha * np.einsum("ij...,j...->i...", gbUU, SD)
+    for i in R3:
+        out["lambdaU%d" % i] = LamU[i] / q["ReU"][i]
+        out["betU%d" % i] = 0.75 * LamU[i] / q["ReU"][i]
+    return out, LamU
+
+
 # ------------------------------------------------------------------ grids
 def grid_symbols(gp, gfs, need_ricci=True):
     """Symbol values at interior points from FD of a (24, n2, n1, n0) array."""
@@ -393,12 +448,14 @@ def ricci_grid(gp, gfs):
     return out
 
 
-def rhs_grid(gp, gfs, RbarDD6=None, diss_strength=0.0):
+def rhs_grid(gp, gfs, RbarDD6=None, diss_strength=0.0, T4UU10=None):
     """rhs_eval: 24 RHSs at interior points (zero elsewhere).  RbarDD6, if
     given, is the (6, n2, n1, n0) auxevol array (LeaveRicciSymbolic form).
     diss_strength != 0 adds Kreiss-Oliger dissipation to every RHS,
     diss_strength * sum_k f_dKOD[k] * ReU[k]
-    (BaikalETK/BaikalETK_C_kernels_codegen.py:147-171)."""
+    (BaikalETK/BaikalETK_C_kernels_codegen.py:147-171).  T4UU10, if given,
+    is the (10, n2, n1, n0) stress-energy tensor (T4UU00, 01, 02, 03, 11,
+    12, 13, 22, 23, 33) whose source terms are added (source_terms)."""
     v, q = grid_symbols(gp, gfs, need_ricci=RbarDD6 is None)
     Rbar = None
     if RbarDD6 is not None:
@@ -406,6 +463,11 @@ def rhs_grid(gp, gfs, RbarDD6=None, diss_strength=0.0):
         for n, (i, j) in enumerate(SYM):
             Rbar[i, j] = Rbar[j, i] = gp.interior(RbarDD6[n])
     r = rhs(v, q, gp.eta, Rbar)
+    if T4UU10 is not None:
+        src, _ = source_terms(v, q, t4uu_full(np.array([gp.interior(t) for t in T4UU10])))
+        r = dict(r)
+        for k, val in src.items():
+            r[k] = r[k] + val
     out = np.zeros((24,) + gp.shape)
     if diss_strength != 0.0:
         S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)

@@ -15,7 +15,8 @@ start-to-finish drivers do, and writes the C that its code generator emits:
   Read_xxs forms of Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide-
   no_rfm_precompute.ipynb), rhs_eval with Kreiss-Oliger dissipation
   (BSSN_KO: the BSSN RHSs plus BaikalETK's diss_strength * f_dKOD * ReU
-  terms), psi4_eval (BSSN_PSI4: psi_4 in the quasi-Kinnersley tetrad, six
+  terms), rhs_eval with T^{mu nu} source terms (BSSN_SRC: T4UU as auxevol
+  gridfunctions after RbarDD), psi4_eval (BSSN_PSI4: psi_4 in the quasi-Kinnersley tetrad, six
   pieces), rhs_eval (ScalarWave, Maxwell System I),
   plus its declare_Cparameters_struct.h / set_Cparameters*.h /
   gridfunction_defines.h.
@@ -43,6 +44,7 @@ CONFIGS = {
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
     "bssn_ko_sinhsph_fd4": ("BSSN_KO", "SinhSpherical", 4, 3),
     "bssn_ko_cart_fd6": ("BSSN_KO", "Cartesian", 6, 4),
+    "bssn_src_sinhsph_fd4": ("BSSN_SRC", "SinhSpherical", 4, 3),
     "bssn_psi4_sph_fd4": ("BSSN_PSI4", "Spherical", 4, 3),
     "sw_cart_fd4": ("ScalarWave", "Cartesian", 4, 2),
     "sw_sinhsph_fd4": ("ScalarWave", "SinhSpherical", 4, 2),
@@ -74,9 +76,10 @@ def emit(name, params, body, loopopts):
     with open(os.path.join(OUTDIR, name + ".h"), "w") as f:
         f.write(txt)
 
-if SYSTEM in ("BSSN", "BSSN_KO"):
+if SYSTEM in ("BSSN", "BSSN_KO", "BSSN_SRC"):
     KO = SYSTEM == "BSSN_KO"
-    if not KO:
+    SRC = SYSTEM == "BSSN_SRC"
+    if SYSTEM == "BSSN":
         import BSSN.BrillLindquist as bl
         bl.BrillLindquist()
         with open(os.path.join(OUTDIR, "initial_data.h"), "w") as f:
@@ -87,6 +90,19 @@ if SYSTEM in ("BSSN", "BSSN_KO"):
     par.set_parval_from_str("BSSN.BSSN_gauge_RHSs::ShiftEvolutionOption", "GammaDriving2ndOrder_Covariant")
     par.set_parval_from_str("BSSN.BSSN_quantities::LeaveRicciSymbolic", "True")
     rhs.BSSN_RHSs()
+    if SRC:
+        # T^{mu nu} source terms added as BaikalETK_C_kernels_codegen.py:133-145
+        # adds them: before the gauge RHSs, so B^i sees the Lambdabar source.
+        import indexedexp as ixp
+        import BSSN.BSSN_stress_energy_source_terms as Bsest
+        T4UU = ixp.register_gridfunctions_for_single_rank2("AUXEVOL", "T4UU", "sym01", DIM=4)
+        Bsest.BSSN_source_terms_for_BSSN_RHSs(T4UU)
+        rhs.trK_rhs += Bsest.sourceterm_trK_rhs
+        for i in range(3):
+            rhs.Lambdabar_rhsU[i] += Bsest.sourceterm_Lambdabar_rhsU[i]
+            rhs.lambda_rhsU[i] += Bsest.sourceterm_lambda_rhsU[i]
+            for j in range(3):
+                rhs.a_rhsDD[i][j] += Bsest.sourceterm_a_rhsDD[i][j]
     gaugerhs.BSSN_gauge_RHSs()
     Bq.BSSN_basic_tensors()
     betaU = Bq.betaU
@@ -133,7 +149,7 @@ if SYSTEM in ("BSSN", "BSSN_KO"):
          "const REAL *restrict in_gfs, REAL *restrict rhs_gfs",
          fin.FD_outputC("returnstring", ev, params="outCverbose=False", upwindcontrolvec=betaU).replace("IDX4", "IDX4S"),
          "InteriorPoints,Read_xxs")
-    if KO:
+    if KO or SRC:
         par.generate_Cparameters_Ccodes(OUTDIR)
         gri.output__gridfunction_defines_h__return_gf_lists(OUTDIR)
         print("generated", SYSTEM, COORD, FD)

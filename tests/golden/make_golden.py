@@ -16,7 +16,9 @@ Writes:
       enforce_detgammabar_constraint (hDD at all points), Brill-Lindquist
       initial_data (interior points); rhs_eval for ScalarWave / Maxwell;
       for bssn_ko_*: rhs_eval with Kreiss-Oliger dissipation on seeded
-      state and auxevol inputs; for bssn_psi4_*: the six pieces of psi_4.
+      state and auxevol inputs; for bssn_psi4_*: the six pieces of psi_4;
+      for bssn_src_*: rhs_eval with T^{mu nu} source terms (auxevol = 6
+      RbarDD + 10 T4UU, seeded).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -55,6 +57,7 @@ FIXTURE_GRIDS = {
     "bssn_ko_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 18),
     "bssn_ko_cart_fd6": ("Cartesian", (6, 6, 6), 6, 4, 19),
     "bssn_psi4_sph_fd4": ("Spherical", (8, 6, 4), 4, 3, 20),
+    "bssn_src_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 21),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -87,6 +90,14 @@ def ref_outputs():
             f = bssn_random_state(gp.shape, seed=seed)
             _, parts = R.psi4(f)
             out["psi4_parts"] = parts[I]
+        elif cfg.startswith("bssn_src"):
+            # rhs_eval with T^{mu nu} source terms: auxevol = 6 RbarDD then
+            # 10 T4UU (seeded; T4UU00 kept positive like an energy density)
+            f = bssn_random_state(gp.shape, seed=seed)
+            aux = 0.1 * np.random.default_rng(seed + 100).standard_normal((16,) + gp.shape)
+            aux[6] = np.abs(aux[6])
+            out["aux"] = aux
+            out["rhs"] = R.rhs_eval(f, aux=aux)[I]
         elif cfg.startswith("bssn_ko"):
             # rhs_eval with Kreiss-Oliger dissipation; RbarDD is an input
             # (auxevol) of the generated rhs_eval, so any seeded values do.
@@ -228,6 +239,17 @@ TRUSTED += [
      "import BSSN.Psi4 as M", "M.Psi4(specify_tetrad=False)", ["psi4_re_pt", "psi4_im_pt"]),
     ("Psi4_tetrads", "BSSN", "Psi4_tetrads__Psi4_tetrads__globals",
      "import BSSN.Psi4_tetrads as M", "M.Psi4_tetrads()", ["l4U", "n4U", "mre4U", "mim4U"]),
+]
+_RFM_INIT = ("import BSSN.BSSN_quantities as Bq\nimport reference_metric as rfm\nrfm.reference_metric()\n"
+             "rfm.ref_metric__hatted_quantities()\nimport BSSN.BSSN_stress_energy_source_terms as M")
+TRUSTED += [
+    ("Tmunu_BSSN", "BSSN",
+     "BSSN_stress_energy_source_terms__stress_energy_source_terms_ito_T4UU_and_ADM_or_BSSN_metricvars___BSSN___globals",
+     _RFM_INIT, 'M.stress_energy_source_terms_ito_T4UU_and_ADM_or_BSSN_metricvars("BSSN")',
+     ["SDD", "SD", "S", "rho"]),
+    ("Tmunu_RHS_sources", "BSSN", "BSSN_stress_energy_source_terms__BSSN_source_terms_for_BSSN_RHSs__globals",
+     _RFM_INIT, "M.BSSN_source_terms_for_BSSN_RHSs()",
+     ["sourceterm_trK_rhs", "sourceterm_a_rhsDD", "sourceterm_lambda_rhsU", "sourceterm_Lambdabar_rhsU"]),
 ]
 for cs in ("Spherical", "SinhSpherical", "Cartesian"):
     TRUSTED.append(("rfm_" + cs, "tests", "rfm_%s__reference_metric__True__globals" % cs,

@@ -139,6 +139,43 @@ def test_trusted_momentum_constraint():
         assert close(M[i, 0], want, 1e-11), (i, M[i, 0], want)
 
 
+def _tmunu_case(case):
+    inp = TV[case]["inputs"]
+    v = symbols(inp, ["hDD", "vetU", "alpha", "cf"])
+    v = {k: a for k, a in v.items()}
+    q = og.hatted_at("Spherical", inp.get("xx0", 0.0), inp.get("xx1", 0.0))
+    q = {k: a[..., 0] for k, a in q.items()}
+    T10 = np.array([[inp.get("T4UU%d%d" % ab, 0.0)] for ab in obs.T4])
+    return inp, v, q, obs.t4uu_full(T10)
+
+
+def test_trusted_stress_energy_projections():
+    inp, v, q, T = _tmunu_case("Tmunu_BSSN")
+    SDD, SD, S, rho = obs.stress_energy(v, q, T)
+    for k, want in expect("Tmunu_BSSN").items():
+        idx = [int(c) for c in k if c.isdigit()]
+        got = {"SDD": lambda: SDD[idx[0], idx[1], 0], "SD": lambda: SD[idx[0], 0], "S": lambda: S[0],
+               "rho": lambda: rho[0]}[k.split("[")[0]]()
+        assert close(float(got), want, 1e-12), (k, got, want)
+
+
+def test_trusted_stress_energy_rhs_sources():
+    inp, v, q, T = _tmunu_case("Tmunu_RHS_sources")
+    src, LamU = obs.source_terms(v, q, T, PI=inp["PI"])
+    for k, want in expect("Tmunu_RHS_sources").items():
+        idx = [int(c) for c in k if c.isdigit()]
+        base = k.split("[")[0]
+        if base == "sourceterm_trK_rhs":
+            got = src["trK"][0]
+        elif base == "sourceterm_a_rhsDD":
+            got = src["aDD%d%d" % tuple(sorted(idx))][0]
+        elif base == "sourceterm_lambda_rhsU":
+            got = src["lambdaU%d" % idx[0]][0]
+        else:
+            got = LamU[idx[0], 0]
+        assert close(float(got), want, 1e-12), (k, got, want)
+
+
 def _complex(sv):
     return complex(sv.replace(" ", ""))
 
@@ -259,6 +296,20 @@ def test_oracle_kreiss_oliger_matches_reference_generated_bssn(cfg, cs):
     assert per_gf_rel(got, z["rhs"]) < 1e-13
     plain = obs.rhs_grid(gp, f, RbarDD6=z["aux"])[I]
     assert per_gf_rel(plain, z["rhs"]) > 1e-6
+
+
+def test_oracle_source_terms_match_reference_generated_bssn():
+    """rhs_eval with T^{mu nu} source terms (reference-generated C of the
+    BaikalETK construction; auxevol = RbarDD + T4UU) against the oracle."""
+    z = np.load(os.path.join(GOLD, "ref_bssn_src_sinhsph_fd4.npz"))
+    gp = og.GridParams("SinhSpherical", tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
+    f = bssn_random_state(gp.shape, seed=int(z["seed"]))
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    aux = z["aux"]
+    got = obs.rhs_grid(gp, f, RbarDD6=aux[:6], T4UU10=aux[6:])[I]
+    assert per_gf_rel(got, z["rhs"]) < 1e-13
+    assert per_gf_rel(obs.rhs_grid(gp, f, RbarDD6=aux[:6])[I], z["rhs"]) > 1e-6
 
 
 def test_oracle_fd_coefficients_match_reference_exactly():
