@@ -282,6 +282,22 @@ def run_gpu(args):
     t_ric_64 = kernel_time(lambda: ev.substep_rhs(dt, 1, 1))
     t_rhs_64 = kernel_time(lambda: ev.substep_rhs(dt, 1, 2))
 
+    # ---- psi4 extraction (FP64 diagnostic): whole grid, and one shell + its l <= 8 modes
+    import ctypes as C
+    p4 = torch.zeros((2,) + tuple(y64.shape[1:]), dtype=torch.float64, device=dev)
+    modes = torch.zeros(2 * 77, dtype=torch.float64, device=dev)
+    ish = W["ng"] + W["Nxx"][0] // 2
+
+    def psi4_shell():
+        ev.psi4(y64, (ish, ish + 1), out=p4)
+        _lib.check(lib.BSSN_psi4_spinweightm2_decomposition(C.byref(G.params), _lib.ptr(p4), ish, 8,
+                                                            _lib.ptr(modes)), "psi4 modes")
+
+    t_p4 = kernel_time(lambda: ev.psi4(y64, out=p4))
+    t_p4s = kernel_time(psi4_shell)
+    psi4_info = {"full_grid_ms": t_p4 * 1e3, "points_per_s": nint / t_p4,
+                 "shell_plus_modes_ms": t_p4s * 1e3, "shell_points": W["Nxx"][1] * W["Nxx"][2], "l_max": 8}
+
     # ---- end to end through the C ABI with host buffers (H2D + step + D2H per step)
     host = torch.empty(y0.shape, dtype=torch.float64, pin_memory=True)
     host.copy_(y0.cpu())
@@ -334,6 +350,7 @@ def run_gpu(args):
                               "max_rel_l2_significant_fields": mix_err["max_rel_l2_significant_fields"],
                               "H_l2": Hm},
         "kreiss_oliger": ko,
+        "psi4": psi4_info,
         "compensated_fields": {k: {"rel_l2": v["rel_l2"], "rel_max": v["rel_max"]}
                                for k, v in comp_err["fields"].items() if v["significant"]},
         "clocks": clocks,

@@ -83,6 +83,12 @@ typedef struct paramstruct {
   double diss_strength;               /* Kreiss-Oliger dissipation added to every BSSN
                                          RHS (KO_Dissipation::diss_strength,
                                          BaikalETK_C_kernels_codegen.py:147-171); 0 = off */
+  int    enable_stress_energy_source_terms;  /* 1: the BSSN RHSs add the T^{mu nu}
+                                         source terms (BSSN_stress_energy_source_terms.py,
+                                         as BaikalETK_C_kernels_codegen.py:133-145 adds
+                                         them); auxevol_gfs then holds 16 gridfunctions:
+                                         RbarDD00..22, then T4UU00, 01, 02, 03, 11, 12,
+                                         13, 22, 23, 33 (the stage's storage type) */
 } paramstruct;
 
 /*
@@ -266,6 +272,13 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *params
 int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
                              const double *in_gfs, double *aux_gfs);
 
+/* Matter terms of the constraints (BSSN_stress_energy_source_terms.py:134-161;
+ * BSSN_constraints.py:76-80 adds the H one): H[idx] += -16 pi rho and
+ * MU[i] += -8 pi S^i / ReU^i at interior points, from the ten T4UU
+ * gridfunctions T4UU00, 01, 02, 03, 11, 12, 13, 22, 23, 33 (FP64).  H or MU
+ * may be NULL.  Call after BSSN_Hamiltonian_constraint / BSSN_momentum_constraint. */
+int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+                                      const double *T4UU_gfs, double *H_gf, double *MU_gfs);
 /* psi_4 in the quasi-Kinnersley tetrad (BSSN/Psi4.py:14-193 with
  * BSSN/Psi4_tetrads.py:25-193; the reference's psi4() of
  * Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide-Psi4.ipynb writes

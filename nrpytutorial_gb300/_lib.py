@@ -32,7 +32,7 @@ class paramstruct(C.Structure):
         ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
         ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
         ("eta", C.c_double), ("wavespeed", C.c_double), ("time", C.c_double),
-        ("diss_strength", C.c_double),
+        ("diss_strength", C.c_double), ("enable_stress_energy_source_terms", C.c_int),
     ]
 
 
@@ -98,6 +98,7 @@ _PROTOS = {
     "BSSN_rhs_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp, vp]),
     "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "BSSN_psi4": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp, C.c_int, C.c_int]),
+    "BSSN_constraints_add_source_terms": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp, vp, vp]),
     "BSSN_psi4_spinweightm2_decomposition": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp]),
     "ScalarWave_initial_data": (C.c_int, [P(paramstruct), C.c_int, C.c_double, P(C.c_double), C.c_double, vp]),
     "BSSN_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double),

@@ -296,6 +296,54 @@ __global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gf
   for (int k = 0; k < NUM_EVOL_GFS; k++) gfs[(long long)k * ntot + idx] = out[k];
 }
 
+// Matter terms of the constraints (BSSN_stress_energy_source_terms.py:134-161,
+// BSSN_source_terms_for_BSSN_constraints): H += -16 pi rho, M^i += -8 pi S^i / ReU^i
+// with rho = alpha^2 T^{00}, S_i = alpha gamma4_{i mu} T^{mu 0}, S^i = gamma^ij S_j.
+template <int CS>
+__global__ void constraint_sources_kernel(Grid g, const double *__restrict__ in, const double *__restrict__ tab,
+                                          const double *__restrict__ T4, double *__restrict__ H,
+                                          double *__restrict__ MU) {
+  int i0, i1, i2;
+  long long idx;
+  if (!interior_point(g, i0, i1, i2, idx)) return;
+  using M = RfmMask<CS>;
+  Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const double pi = 3.14159265358979323846;
+  const double alpha = __ldg(P.gf(ALPHA)), cf = __ldg(P.gf(CF));
+  const double T00 = __ldg(T4 + idx);
+  if (H) H[idx] += -16.0 * pi * alpha * alpha * T00;
+  if (!MU) return;
+  double gbar[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = i; j < 3; j++) {
+      const double h = __ldg(P.gf(HDD00 + S6(i, j)));
+      gbar[i][j] = gbar[j][i] = (M::trivial ? h : h * rf.ReDD(i, j)) + (i == j ? rf.ghatDD(i) : 0.0);
+    }
+  double gbUU[3][3], det;
+  sym_inverse(gbar, gbUU, det);
+  const double e4 = 1.0 / (cf * cf);
+  double beta[3], T0[4];
+  for (int j = 0; j < 3; j++) {
+    const double vet = __ldg(P.gf(VETU0 + j));
+    beta[j] = M::trivial ? vet : vet * rf.ReU(j);
+  }
+  for (int m = 0; m < 4; m++) T0[m] = __ldg(T4 + (long long)m * g.ntot + idx);  // T4UU00, 01, 02, 03
+  double SD[3];
+  for (int i = 0; i < 3; i++) {
+    double bD = 0.0, s = 0.0;
+    for (int j = 0; j < 3; j++) {
+      bD += e4 * gbar[i][j] * beta[j];
+      s += e4 * gbar[i][j] * T0[j + 1];
+    }
+    SD[i] = alpha * (bD * T0[0] + s);
+  }
+  for (int i = 0; i < 3; i++) {
+    const double SU = cf * cf * (gbUU[i][0] * SD[0] + gbUU[i][1] * SD[1] + gbUU[i][2] * SD[2]);
+    MU[(long long)i * g.ntot + idx] += -8.0 * pi * (M::trivial ? SU : SU / rf.ReU(i));
+  }
+}
+
 }  // namespace bssn
 
 using namespace bssn;
@@ -308,8 +356,11 @@ int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *i
   NRGPU_REQUIRE(in && auxevol, "NULL gridfunctions");
   NRGPU_BSSN_SWITCH(RICCI_CALL)
 }
+static bool extras_on(const paramstruct *p) {
+  return p->diss_strength != 0.0 || p->enable_stress_energy_source_terms;
+}
 #define RHS_CALL(CS, ORD) \
-  (p->diss_strength != 0.0 ? rhs_launch_t<CS, ORD, true>(rfm, p, a) : rhs_launch_t<CS, ORD, false>(rfm, p, a))
+  (extras_on(p) ? rhs_launch_t<CS, ORD, true>(rfm, p, a) : rhs_launch_t<CS, ORD, false>(rfm, p, a))
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
   int st = check_bssn(rfm, p);
   if (st) return st;
@@ -413,9 +464,9 @@ int BSSN_rhs_eval_xx(const paramstruct *p, double *xx[3], const double *aux, con
   NRGPU_REQUIRE(xx && xx[0] && xx[1] && aux && in && rhs, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
   const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
-#define HXX(CS, ORD)                                                 \
-  (p->diss_strength != 0.0 ? rhs_xx_launch_t<CS, ORD, true>(p, xa, aux, in, rhs) \
-                           : rhs_xx_launch_t<CS, ORD, false>(p, xa, aux, in, rhs))
+#define HXX(CS, ORD)                                                                 \
+  (extras_on(p) ? rhs_xx_launch_t<CS, ORD, true>(p, xa, aux, in, rhs) \
+                : rhs_xx_launch_t<CS, ORD, false>(p, xa, aux, in, rhs))
   NRGPU_BSSN_SWITCH(HXX)
 #undef HXX
 }
@@ -438,6 +489,28 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const 
       return NRGPU_ERR_UNSUPPORTED;
   }
 #undef MOM
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *p, const double *in,
+                                      const double *T4UU, double *H, double *MU) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(in && T4UU && (H || MU), "NULL argument");
+  Grid g = make_grid(p);
+  InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
+  const double *tab = rfm ? rfm->table64 : nullptr;
+  switch (p->CoordSystem) {
+    case NRGPU_COORD_CARTESIAN:
+      constraint_sources_kernel<NRGPU_COORD_CARTESIAN><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H, MU);
+      break;
+    case NRGPU_COORD_SPHERICAL:
+      constraint_sources_kernel<NRGPU_COORD_SPHERICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H, MU);
+      break;
+    default:
+      constraint_sources_kernel<NRGPU_COORD_SINHSPHERICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H,
+                                                                                              MU);
+  }
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }

@@ -23,6 +23,9 @@ SYSTEM_GFS = {
              [4, 5, 6, 7, 8, 9, 0, 1, 2, 3, 0, 4, 5, 6, 7, 8, 9, 1, 2, 3, 0, 1, 2, 3]),
 }
 AUXEVOL_GFS = {"BSSN": ["RbarDD00", "RbarDD01", "RbarDD02", "RbarDD11", "RbarDD12", "RbarDD22"]}
+# With stress-energy source terms the T4UU gridfunctions follow RbarDD in auxevol
+# (alphabetical registration order, as the reference's generated code has them).
+T4UU_GFS = ["T4UU00", "T4UU01", "T4UU02", "T4UU03", "T4UU11", "T4UU12", "T4UU13", "T4UU22", "T4UU23", "T4UU33"]
 
 
 def default_nghosts(system, fd_order):
@@ -36,7 +39,8 @@ class Grid:
     """Numerical grid: paramstruct + cell-centred xx arrays (host, FP64)."""
 
     def __init__(self, CoordSystem, Nxx, FD_order=4, NGHOSTS=2, *, AMPL=10.0, SINHW=0.2,
-                 RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, diss_strength=0.0):
+                 RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, diss_strength=0.0,
+                 stress_energy_source_terms=False):
         lib = _lib.load()
         p = _lib.paramstruct()
         p.CoordSystem = _lib.COORD[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
@@ -48,6 +52,7 @@ class Grid:
         p.xmax = p.ymax = p.zmax = hi
         p.eta, p.wavespeed, p.time = eta, wavespeed, 0.0
         p.diss_strength = diss_strength  # Kreiss-Oliger dissipation of the BSSN RHSs (0 = off)
+        p.enable_stress_energy_source_terms = int(bool(stress_energy_source_terms))  # T4UU in auxevol 6..15
         n = [int(v) for v in Nxx]
         np_ = [v + 2 * NGHOSTS for v in n]
         self.xx = [np.zeros(np_[d]) for d in range(3)]

@@ -12,7 +12,7 @@ import ctypes as C
 import torch
 
 from . import _lib
-from .grid import AUXEVOL_GFS, SYSTEM_GFS, Grid
+from .grid import AUXEVOL_GFS, SYSTEM_GFS, T4UU_GFS, Grid
 
 
 class Evolution:
@@ -46,6 +46,10 @@ class Evolution:
         self.k_odd = torch.zeros(kshape, dtype=stage, **z)
         self.k_even = torch.zeros(kshape, dtype=stage, **z)
         naux = len(AUXEVOL_GFS.get(system, []))
+        self.sources = system == "BSSN" and bool(grid.params.enable_stress_energy_source_terms)
+        if self.sources:
+            naux += len(T4UU_GFS)
+            self.T4UU = torch.zeros((len(T4UU_GFS),) + grid.shape, dtype=torch.float64, **z)
         self.auxevol = torch.zeros((max(naux, 1),) + grid.shape, dtype=stage, **z)
         self.gfs = _lib.MoL_gridfunctions(_lib.PREC[precision], self.y_n.data_ptr(), self.rt.data_ptr(),
                                           self.k_odd.data_ptr(), self.k_even.data_ptr(),
@@ -197,13 +201,28 @@ class Evolution:
              else self.lib.BSSN_enforce_detgammabar_constraint)
         _lib.check(f(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs)), "enforce_detgammabar_constraint")
 
+    def set_stress_energy(self, T4UU):
+        """Stress-energy tensor T^{mu nu} for the BSSN source terms: (10, n2,
+        n1, n0) in the order T4UU00, 01, 02, 03, 11, 12, 13, 22, 23, 33.
+        Kept in FP64 for the constraints and copied into auxevol[6:16] in
+        the stage precision for the RHS kernels."""
+        if not self.sources:
+            raise ValueError("build the Grid with stress_energy_source_terms=True")
+        self.T4UU.copy_(T4UU)
+        self.auxevol[6:16].copy_(self.T4UU)
+
     def hamiltonian(self, gfs=None):
-        """Hamiltonian constraint at interior points (FP64)."""
+        """Hamiltonian constraint at interior points (FP64); with source
+        terms on, including -16 pi rho."""
         self._sync_stream()
         gfs = self.y_n if gfs is None else gfs
         H = torch.zeros((1,) + self.grid.shape, dtype=torch.float64, device=self.device)
         _lib.check(self.lib.BSSN_Hamiltonian_constraint(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs),
                                                         _lib.ptr(H)), "BSSN_Hamiltonian_constraint")
+        if self.sources:
+            _lib.check(self.lib.BSSN_constraints_add_source_terms(self._rfm(), C.byref(self.grid.params),
+                                                                  _lib.ptr(gfs), _lib.ptr(self.T4UU), _lib.ptr(H),
+                                                                  None), "BSSN_constraints_add_source_terms")
         return H
 
     def momentum(self, gfs=None):
@@ -213,6 +232,10 @@ class Evolution:
         M = torch.zeros((3,) + self.grid.shape, dtype=torch.float64, device=self.device)
         _lib.check(self.lib.BSSN_momentum_constraint(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs),
                                                      _lib.ptr(M)), "BSSN_momentum_constraint")
+        if self.sources:
+            _lib.check(self.lib.BSSN_constraints_add_source_terms(self._rfm(), C.byref(self.grid.params),
+                                                                  _lib.ptr(gfs), _lib.ptr(self.T4UU), None,
+                                                                  _lib.ptr(M)), "BSSN_constraints_add_source_terms")
         return M
 
     def psi4(self, gfs=None, i0_range=None, out=None):

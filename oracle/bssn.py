@@ -374,6 +374,15 @@ def source_terms(v, q, T, PI=np.pi):
     return out, LamU
 
 
+def constraint_source_terms(v, q, T, PI=np.pi):
+    """BSSN_stress_energy_source_terms.py:134-161: (-16 pi rho, -8 pi S^i / ReU^i)."""
+    SDD, SD, S, rho = stress_energy(v, q, T)
+    gbar = v["hDD"] * q["ReDD"] + q["ghatDD"]
+    gUU, _ = inv3(gbar / v["cf"] ** 2)
+    SU = np.einsum("ij...,j...->i...", gUU, SD)
+    return -16 * PI * rho, -8 * PI * SU / q["ReU"]
+
+
 # ------------------------------------------------------------------ grids
 def grid_symbols(gp, gfs, need_ricci=True):
     """Symbol values at interior points from FD of a (24, n2, n1, n0) array."""
@@ -481,15 +490,19 @@ def rhs_grid(gp, gfs, RbarDD6=None, diss_strength=0.0, T4UU10=None):
     return out
 
 
-def hamiltonian_grid(gp, gfs):
+def hamiltonian_grid(gp, gfs, T4UU10=None):
     v, q = grid_symbols(gp, gfs)
     out = np.zeros(gp.shape)
-    gp.interior(out)[...] = hamiltonian(v, q)
+    H = hamiltonian(v, q)
+    if T4UU10 is not None:
+        H = H + constraint_source_terms(v, q, t4uu_full(np.array([gp.interior(t) for t in T4UU10])))[0]
+    gp.interior(out)[...] = H
     return out
 
 
-def momentum_grid(gp, gfs):
-    """M^i (3, n2, n1, n0) at interior points, zero elsewhere."""
+def momentum_grid(gp, gfs, T4UU10=None):
+    """M^i (3, n2, n1, n0) at interior points, zero elsewhere (with the
+    -8 pi S^i / ReU^i matter term when T4UU10 is given)."""
     v, q = grid_symbols(gp, gfs, need_ricci=False)
     S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
     f = {n: gfs[GF[n]] for n in EVOL}
@@ -499,6 +512,8 @@ def momentum_grid(gp, gfs):
             a[i, j, k] = a[j, i, k] = S.d1(f["aDD%d%d" % (i, j)], k)
     v["aDD_dD"] = a
     M = momentum(v, q)
+    if T4UU10 is not None:
+        M = M + constraint_source_terms(v, q, t4uu_full(np.array([gp.interior(t) for t in T4UU10])))[1]
     out = np.zeros((3,) + gp.shape)
     for i in R3:
         gp.interior(out[i])[...] = M[i]

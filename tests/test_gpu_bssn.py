@@ -278,3 +278,71 @@ def test_kreiss_oliger_damps_the_grid_scale_mode(cuda):
     assert np.allclose(d[GF["trK"]], want, rtol=1e-12, atol=0.0)
     others = [k for k in range(24) if k != GF["trK"]]
     assert np.abs(d[others]).max() <= 1e-14
+
+
+def _t4uu(shape, seed):
+    """Seeded T^{mu nu} (10 gfs), T^00 > 0."""
+    T = 0.05 * np.random.default_rng(seed).standard_normal((10,) + tuple(shape))
+    T[0] = np.abs(T[0]) + 0.01
+    return T
+
+
+@pytest.mark.parametrize("coord,Nxx,order", CASES)
+def test_source_terms_rhs_matches_oracle(cuda, coord, Nxx, order):
+    """T^{mu nu} source terms on, with and without Kreiss-Oliger dissipation."""
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    for diss in (0.0, KO_DISS):
+        G, gp = grids("BSSN", coord, Nxx, order, stress_energy_source_terms=True, diss_strength=diss, **KW)
+        ev = Evolution("BSSN", G, device=cuda)
+        f = bssn_random_state(gp.shape, seed=51 + order)
+        T = _t4uu(gp.shape, 52 + order)
+        ev.set_stress_energy(torch.tensor(T, device=cuda))
+        t = torch.tensor(f, device=cuda)
+        out = torch.zeros_like(t)
+        ev.rhs_eval(t, out)
+        ref = obs.rhs_grid(gp, f, diss_strength=diss, T4UU10=T)
+        assert per_gf_rel(out.cpu().numpy(), ref, gp.NGHOSTS) < FP64_TOL, diss
+        assert per_gf_rel(obs.rhs_grid(gp, f, diss_strength=diss), ref, gp.NGHOSTS) > 1e-4
+
+
+def test_source_terms_constraints_match_oracle(cuda):
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    coord, Nxx, order = CASES[2]
+    G, gp = grids("BSSN", coord, Nxx, order, stress_energy_source_terms=True, **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    f = bssn_random_state(gp.shape, seed=53)
+    T = _t4uu(gp.shape, 54)
+    ev.set_stress_energy(torch.tensor(T, device=cuda))
+    t = torch.tensor(f, device=cuda)
+    H = ev.hamiltonian(t).cpu().numpy()
+    M = ev.momentum(t).cpu().numpy()
+    g = gp.NGHOSTS
+    assert per_gf_rel(H, obs.hamiltonian_grid(gp, f, T4UU10=T)[None], g) < FP64_TOL
+    assert per_gf_rel(M, obs.momentum_grid(gp, f, T4UU10=T), g) < FP64_TOL
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("compensated", 1e-6), ("mixed", 1e-4)])
+def test_source_terms_rk4_step_matches_oracle(cuda, prec, tol):
+    import torch
+    from nrpytutorial_gb300 import SYSTEM_GFS, Evolution
+    coord, Nxx, order = CASES[2]
+    G, gp = grids("BSSN", coord, Nxx, order, stress_energy_source_terms=True, **KW)
+    ev = Evolution("BSSN", G, precision=prec, device=cuda)
+    T = _t4uu(gp.shape, 56)
+    ev.set_stress_energy(torch.tensor(T, device=cuda))
+    parity = SYSTEM_GFS["BSSN"][1]
+    layers = ob.build_bcstruct(gp)
+
+    def post(x):
+        ob.apply_bcs(layers, x, parity)
+        x[...] = obs.enforce_detgammabar(gp, x)
+
+    y = bssn_random_state(gp.shape, seed=55, amp=0.02)
+    post(y)
+    ev.y_n.copy_(torch.tensor(y, device=cuda))
+    dt = 0.05 * min(gp.dxx)
+    ev.step(dt)
+    yo, _, _ = ob.rk4_step(y, dt, lambda u: obs.rhs_grid(gp, u, T4UU10=T), post, gp.NGHOSTS)
+    assert per_gf_rel(ev.y_n.cpu().numpy(), yo) < tol

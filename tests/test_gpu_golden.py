@@ -82,6 +82,33 @@ def test_kreiss_oliger_rhs_matches_reference_generated_c(cuda, cfg, cs):
     assert per_gf_rel(out_xx.cpu().numpy()[I], z["rhs"]) < TOL
 
 
+def test_source_terms_rhs_matches_reference_generated_c(cuda):
+    """rhs_eval with T^{mu nu} source terms (auxevol = RbarDD + T4UU) against
+    the reference's generated C, table path and no-precompute signature."""
+    import ctypes as C
+    import torch
+    from nrpytutorial_gb300 import Evolution, _lib
+    from bench import _rhs_only
+    z = _load("bssn_src_sinhsph_fd4")
+    G, gp = grids("BSSN", "SinhSpherical", tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]),
+                  stress_energy_source_terms=True, **KW)
+    ev = Evolution("BSSN", G, device=cuda)
+    t = torch.tensor(bssn_random_state(gp.shape, seed=int(z["seed"])), device=cuda)
+    aux = torch.tensor(z["aux"], device=cuda)
+    g = gp.NGHOSTS
+    I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    out = torch.zeros_like(t)
+    _rhs_only(ev, t, aux, out)
+    assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
+    xx = [torch.tensor(np.asarray(G.xx[d]), dtype=torch.float64, device=cuda) for d in range(3)]
+    xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
+    out_xx = torch.zeros_like(t)
+    _lib.check(ev.lib.BSSN_rhs_eval_xx(C.byref(G.params), xxp, _lib.ptr(aux), _lib.ptr(t), _lib.ptr(out_xx)),
+               "BSSN_rhs_eval_xx")
+    torch.cuda.synchronize()
+    assert per_gf_rel(out_xx.cpu().numpy()[I], z["rhs"]) < TOL
+
+
 @pytest.mark.parametrize("cfg", sorted(CFGS))
 def test_brill_lindquist_matches_reference_initial_data(cuda, cfg):
     import torch
