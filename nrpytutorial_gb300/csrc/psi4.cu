@@ -307,14 +307,20 @@ __device__ void psi4_point(const Point<double> &P, const Rfm<CS, double> &rf, co
   im = p0i + p1i + p2i;
 }
 
+// One thread per point of the i0 range x interior (i1, i2), i0 fastest: a
+// single extraction shell fills whole warps too.
+constexpr int kPsi4Threads = 64;
 template <int CS, int ORDER>
-__global__ void __launch_bounds__(128) psi4_kernel(Grid g, const double *__restrict__ in,
-                                                   const double *__restrict__ tab, paramstruct p, int i0lo, int i0hi,
-                                                   double *__restrict__ out_re, double *__restrict__ out_im) {
-  const int i0 = i0lo + blockIdx.x * blockDim.x + threadIdx.x;
-  const int i1 = g.ng + blockIdx.y * blockDim.y + threadIdx.y;
-  const int i2 = g.ng + blockIdx.z;
-  if (i0 >= i0hi || i1 >= g.n1 - g.ng) return;
+__global__ void __launch_bounds__(kPsi4Threads) psi4_kernel(Grid g, const double *__restrict__ in,
+                                                            const double *__restrict__ tab, paramstruct p, int i0lo,
+                                                            int i0hi, double *__restrict__ out_re,
+                                                            double *__restrict__ out_im) {
+  const long long t = (long long)blockIdx.x * kPsi4Threads + threadIdx.x;
+  const int nr = i0hi - i0lo, n1i = g.n1 - 2 * g.ng, n2i = g.n2 - 2 * g.ng;
+  if (t >= (long long)nr * n1i * n2i) return;
+  const int i0 = i0lo + (int)(t % nr);
+  const int i1 = g.ng + (int)((t / nr) % n1i);
+  const int i2 = g.ng + (int)(t / ((long long)nr * n1i));
   const long long idx = i0 + (long long)g.n0 * (i1 + (long long)g.n1 * i2);
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
@@ -333,13 +339,16 @@ constexpr int kModeThreads = 256;
 constexpr int kMaxL = 12;
 
 // One block per (l, m), l = 2..l_max, m = -l..l in that order.  Thread 0
-// tabulates Goldberg's coefficients for the mode; every thread accumulates
-// a strided share of the shell's points; a fixed-order tree reduction makes
-// the result independent of scheduling.
+// tabulates Goldberg's coefficients for the mode; the block then tabulates
+// sY_lm's theta factor times sin(theta) for every interior i1 and
+// cos(m phi), sin(m phi) for every interior i2 in shared memory, and every
+// thread accumulates a strided share of the shell's points; a fixed-order
+// tree reduction makes the result independent of scheduling.
 __global__ void __launch_bounds__(kModeThreads) swm2_modes_kernel(Grid g, paramstruct p, int i0,
                                                                   const double *__restrict__ re_gf,
                                                                   const double *__restrict__ im_gf,
                                                                   double *__restrict__ out) {
+  extern __shared__ double tabs[];  // [n1i] theta factors, then [n2i] cos(m phi), [n2i] sin(m phi)
   __shared__ double coef[kMaxL + 3];
   __shared__ int kexp[kMaxL + 3];
   __shared__ int nterm;
@@ -373,10 +382,9 @@ __global__ void __launch_bounds__(kModeThreads) swm2_modes_kernel(Grid g, params
   }
   __syncthreads();
   const int n1i = g.n1 - 2 * g.ng, n2i = g.n2 - 2 * g.ng;
-  double ar = 0.0, ai = 0.0;
-  for (int q = threadIdx.x; q < n1i * n2i; q += kModeThreads) {
-    const int i1 = g.ng + q / n2i, i2 = g.ng + q % n2i;
-    const double th = xx_of(p.xxmin1, p.dxx1, i1, g.ng), ph = xx_of(p.xxmin2, p.dxx2, i2, g.ng);
+  double *thf = tabs, *cph = tabs + n1i, *sph = tabs + n1i + n2i;
+  for (int j = threadIdx.x; j < n1i; j += kModeThreads) {
+    const double th = xx_of(p.xxmin1, p.dxx1, g.ng + j, g.ng);
     const double sh = sin(0.5 * th), ch = cos(0.5 * th);
     double y = 0.0;
     for (int t = 0; t < nterm; t++) {
@@ -386,11 +394,22 @@ __global__ void __launch_bounds__(kModeThreads) swm2_modes_kernel(Grid g, params
       for (int e = 0; e < k; e++) pw *= ch;
       y += coef[t] * pw;
     }
-    const double c = y * cos(m * ph), d = y * sin(m * ph);
-    const long long idx = i0 + (long long)g.n0 * (i1 + (long long)g.n1 * i2);
-    const double a = re_gf[idx], b = im_gf[idx], w = sin(th);
-    ar += (a * c + b * d) * w;
-    ai += (b * c - a * d) * w;
+    thf[j] = y * sin(th);
+  }
+  for (int j = threadIdx.x; j < n2i; j += kModeThreads) {
+    const double ph = xx_of(p.xxmin2, p.dxx2, g.ng + j, g.ng);
+    cph[j] = cos(m * ph);
+    sph[j] = sin(m * ph);
+  }
+  __syncthreads();
+  double ar = 0.0, ai = 0.0;
+  for (int q = threadIdx.x; q < n1i * n2i; q += kModeThreads) {
+    const int j1 = q / n2i, j2 = q % n2i;
+    const double c = thf[j1] * cph[j2], d = thf[j1] * sph[j2];
+    const long long idx = i0 + (long long)g.n0 * ((g.ng + j1) + (long long)g.n1 * (g.ng + j2));
+    const double a = re_gf[idx], b = im_gf[idx];
+    ar += a * c + b * d;
+    ai += b * c - a * d;
   }
   sre[threadIdx.x] = ar;
   sim[threadIdx.x] = ai;
@@ -431,8 +450,8 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
   NRGPU_REQUIRE(i0_min >= ng && i0_max <= p->Nxx_plus_2NGHOSTS0 - ng && i0_min < i0_max,
                 "i0 range [%d, %d) outside the interior [%d, %d)", i0_min, i0_max, ng, p->Nxx_plus_2NGHOSTS0 - ng);
   Grid g = make_grid(p);
-  dim3 block(32, 4);
-  dim3 grid((i0_max - i0_min + 31) / 32, (p->Nxx1 + 3) / 4, p->Nxx2);
+  const long long npts = (long long)(i0_max - i0_min) * p->Nxx1 * p->Nxx2;
+  dim3 block(kPsi4Threads), grid((unsigned)((npts + kPsi4Threads - 1) / kPsi4Threads));
   const double *tab = rfm ? rfm->table64 : nullptr;
   double *re = psi4_gfs, *im = psi4_gfs + g.ntot;
 #define P4(CS, ORD) psi4_kernel<CS, ORD><<<grid, block, 0, stream()>>>(g, in_gfs, tab, *p, i0_min, i0_max, re, im)
@@ -460,7 +479,9 @@ int BSSN_psi4_spinweightm2_decomposition(const paramstruct *p, const double *psi
   NRGPU_REQUIRE(i0 >= p->NGHOSTS && i0 < p->Nxx_plus_2NGHOSTS0 - p->NGHOSTS, "i0 %d is not an interior shell", i0);
   Grid g = make_grid(p);
   const int n_modes = (l_max + 1) * (l_max + 1) - 4;
-  swm2_modes_kernel<<<n_modes, kModeThreads, 0, stream()>>>(g, *p, i0, psi4_gfs, psi4_gfs + g.ntot, modes);
+  const size_t smem = sizeof(double) * (size_t)(p->Nxx1 + 2 * p->Nxx2);
+  NRGPU_REQUIRE(smem <= 40 * 1024, "shell of %d x %d points too large for the mode tables", p->Nxx1, p->Nxx2);
+  swm2_modes_kernel<<<n_modes, kModeThreads, smem, stream()>>>(g, *p, i0, psi4_gfs, psi4_gfs + g.ntot, modes);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
