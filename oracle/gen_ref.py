@@ -17,7 +17,8 @@ start-to-finish drivers do, and writes the C that its code generator emits:
   (BSSN_KO: the BSSN RHSs plus BaikalETK's diss_strength * f_dKOD * ReU
   terms), rhs_eval with T^{mu nu} source terms (BSSN_SRC: T4UU as auxevol
   gridfunctions after RbarDD), psi4_eval (BSSN_PSI4: psi_4 in the quasi-Kinnersley tetrad, six
-  pieces), rhs_eval (ScalarWave, Maxwell System I),
+  pieces), rhs_eval (ScalarWave, Maxwell System I, and MaxwellCurvi: System II
+  rescaled on the reference metric),
   plus its declare_Cparameters_struct.h / set_Cparameters*.h /
   gridfunction_defines.h.
 Nothing of the reference's source is copied: only what its generator prints.
@@ -49,6 +50,7 @@ CONFIGS = {
     "sw_cart_fd4": ("ScalarWave", "Cartesian", 4, 2),
     "sw_sinhsph_fd4": ("ScalarWave", "SinhSpherical", 4, 2),
     "maxwell_cart_fd4": ("Maxwell", "Cartesian", 4, 3),
+    "maxwell_curvi_sinhsph_fd4": ("MaxwellCurvi", "SinhSpherical", 4, 3),
 }
 
 WORKER = r'''
@@ -200,6 +202,20 @@ elif SYSTEM == "ScalarWave":
     emit("rhs_eval", params,
          fin.FD_outputC("returnstring", [lhrh(lhs=gri.gfaccess("rhs_gfs", "uu"), rhs=uu_rhs),
                                          lhrh(lhs=gri.gfaccess("rhs_gfs", "vv"), rhs=vv_rhs)],
+                        params="outCverbose=False").replace("IDX4", "IDX4S"),
+         "InteriorPoints,Read_xxs")
+elif SYSTEM == "MaxwellCurvi":
+    # Tutorial-Start_to_Finish-Solving_Maxwells_Equations_in_Vacuum-Curvilinear:
+    # System II in rescaled curvilinear form (no rfm precompute here).
+    import Maxwell.InitialData  # registers Maxwell.InitialData::System_to_use
+    par.set_parval_from_str("Maxwell.InitialData::System_to_use", "System_II")
+    import Maxwell.VacuumMaxwell_Flat_Evol_Curvilinear_rescaled as mc
+    mc.VacuumMaxwellRHSs_rescaled()
+    names = ["aU0", "aU1", "aU2", "eU0", "eU1", "eU2", "psi", "Gamma"]
+    exprs = mc.arhsU + mc.erhsU + [mc.psi_rhs, mc.Gamma_rhs]
+    emit("rhs_eval",
+         "const paramstruct *restrict params, REAL *restrict xx[3], const REAL *restrict in_gfs, REAL *restrict rhs_gfs",
+         fin.FD_outputC("returnstring", [lhrh(lhs=gri.gfaccess("rhs_gfs", n), rhs=e) for n, e in zip(names, exprs)],
                         params="outCverbose=False").replace("IDX4", "IDX4S"),
          "InteriorPoints,Read_xxs")
 elif SYSTEM == "Maxwell":

@@ -154,3 +154,122 @@ def scalarwave_id_grid(gp, kind, t=0.0, k=(1.0, 1.0, 1.0), sigma=3.0):
         x, y, z = r * np.sin(X1) * np.cos(X2), r * np.sin(X1) * np.sin(X2), r * np.cos(X1)
     uu, vv = scalarwave_id_pointwise(kind, x, y, z, t, gp.wavespeed, k, sigma)
     return np.stack([uu, vv])
+
+
+# ------------------------------------------------ curvilinear Maxwell (System II)
+MC_GFS = ["Gamma", "aU0", "aU1", "aU2", "eU0", "eU1", "eU2", "psi"]  # alphabetical (uppercase first)
+
+
+def maxwell_curvi_pointwise(v, q):
+    """Maxwell/VacuumMaxwell_Flat_Evol_Curvilinear_rescaled.py:22-190 (System II,
+    rescaled a^i = A^i / ReU^i, e^i = E^i / ReU^i, auxiliary Gamma):
+      d_t a^i = -e^i - ghat^ij psi_,j / ReU^i
+      d_t e^i = [ ghat^ij Gamma_,j - ghat^jk (A^i_,kj + d_j Gammahat^i_mk A^m
+                 + Gammahat^i_mk A^m_,j + Gammahat^i_mj A^m_,k - Gammahat^m_kj A^i_,m
+                 + (Gammahat^i_dj Gammahat^d_mk - Gammahat^d_kj Gammahat^i_md) A^m) ] / ReU^i
+      d_t psi = -Gamma
+      d_t Gamma = -ghat^ij psi_,ij + ghat^ij Gammahat^k_ji psi_,k
+      C = E^i_,i + Gammahat^i_ji E^j,   G = Gamma - A^i_,i + Gammahat^i_ji A^j.
+    v: aU, aU_dD, aU_dDD, eU, eU_dD, psi_dD, psi_dDD, Gamma, Gamma_dD (tensor indices
+    first); q: hatted quantities.  Returns (arhsU, erhsU, psi_rhs, Gamma_rhs, C, G)."""
+    R = range(3)
+    gUU, G, GdD = q["ghatUU"], q["GammahatUDD"], q["GammahatUDDdD"]  # GdD[i,k,l,n] = d_n Gammahat^i_kl
+    ReU, ReUdD, ReUdDD = q["ReU"], q["ReUdD"], q["ReUdDD"]
+    a, ad, add = v["aU"], v["aU_dD"], v["aU_dDD"]
+    A = a * ReU
+    Ad = ad * ReU[:, None] + a[:, None] * ReUdD
+    Add = (add * ReU[:, None, None] + ad[:, :, None] * ReUdD[:, None, :] + ad[:, None, :] * ReUdD[:, :, None]
+           + a[:, None, None] * ReUdDD)
+    arhs = [-v["eU"][i] - sum(gUU[i, j] * v["psi_dD"][j] for j in R) / ReU[i] for i in R]
+    erhs = []
+    for i in R:
+        E = sum(gUU[i, j] * v["Gamma_dD"][j] for j in R)
+        for j in R:
+            for k in R:
+                t = Add[i, k, j]
+                for m in R:
+                    t = t + GdD[i, m, k, j] * A[m] + G[i, m, k] * Ad[m, j] + G[i, m, j] * Ad[m, k] - G[m, k, j] * Ad[i, m]
+                    for d in R:
+                        t = t + (G[i, d, j] * G[d, m, k] - G[d, k, j] * G[i, m, d]) * A[m]
+                E = E - gUU[j, k] * t
+        erhs.append(E / ReU[i])
+    Grhs = 0.0
+    for i in R:
+        for j in R:
+            Grhs = Grhs - gUU[i, j] * v["psi_dDD"][i, j]
+            for k in R:
+                Grhs = Grhs + gUU[i, j] * G[k, j, i] * v["psi_dD"][k]
+    psi_rhs = -v["Gamma"]
+    Gc = v["Gamma"] - sum(Ad[i, i] for i in R) + sum(G[i, j, i] * A[j] for i in R for j in R)
+    e = v["eU"]
+    Ed = v["eU_dD"] * ReU[:, None] + e[:, None] * ReUdD
+    Cc = sum(Ed[i, i] for i in R) + sum(G[i, j, i] * e[j] * ReU[j] for i in R for j in R)
+    return arhs, erhs, psi_rhs, Grhs, Cc, Gc
+
+
+def _mc_symbols(gp, gfs):
+    S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
+    g = gp.NGHOSTS
+    q = {k: a[..., None, g:-g, g:-g] for k, a in hatted(gp).items()}
+    f = {n: gfs[i] for i, n in enumerate(MC_GFS)}
+    v = {"aU": np.array([S.interior(f["aU%d" % i]) for i in range(3)]),
+         "eU": np.array([S.interior(f["eU%d" % i]) for i in range(3)]),
+         "Gamma": S.interior(f["Gamma"])}
+    v["aU_dD"] = np.array([[S.d1(f["aU%d" % i], j) for j in range(3)] for i in range(3)])
+    v["eU_dD"] = np.array([[S.d1(f["eU%d" % i], j) for j in range(3)] for i in range(3)])
+    v["aU_dDD"] = np.array([[[S.d11(f["aU%d" % i], j, k) for k in range(3)] for j in range(3)] for i in range(3)])
+    v["psi_dD"] = np.array([S.d1(f["psi"], j) for j in range(3)])
+    v["psi_dDD"] = np.array([[S.d11(f["psi"], j, k) for k in range(3)] for j in range(3)])
+    v["Gamma_dD"] = np.array([S.d1(f["Gamma"], j) for j in range(3)])
+    return v, q
+
+
+def maxwell_curvi_rhs_grid(gp, gfs):
+    """rhs_eval of the 8 gridfunctions (MC_GFS order) at interior points."""
+    v, q = _mc_symbols(gp, gfs)
+    arhs, erhs, psi_rhs, Grhs, _, _ = maxwell_curvi_pointwise(v, q)
+    out = np.zeros((8,) + gp.shape)
+    for i in range(3):
+        gp.interior(out[1 + i])[...] = arhs[i]
+        gp.interior(out[4 + i])[...] = erhs[i]
+    gp.interior(out[7])[...] = psi_rhs
+    gp.interior(out[0])[...] = Grhs
+    return out
+
+
+def maxwell_curvi_constraints_grid(gp, gfs):
+    """(C, G) at interior points."""
+    v, q = _mc_symbols(gp, gfs)
+    _, _, _, _, Cc, Gc = maxwell_curvi_pointwise(v, q)
+    out = np.zeros((2,) + gp.shape)
+    gp.interior(out[0])[...] = Cc
+    gp.interior(out[1])[...] = Gc
+    return out
+
+
+def maxwell_curvi_toroidal_dipole(gp, t, amp=1.0, lam=1.0):
+    """Toroidal dipole of Maxwell/InitialData.py:26-117 for System II in the
+    grid's basis (the Tutorial-Start_to_Finish-...-Curvilinear driver stores
+    AidU/ReU, EidU/ReU, psi = Gamma = 0): the Cartesian vectors of
+    toroidal_dipole are carried to the xx basis by the inverse Jacobian of
+    xx_to_Cart and divided by ReU."""
+    from .psi4 import _inv_general, cart_and_jacobian
+    X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
+    xyz, J = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW)
+    x, y, z = xyz
+    r = np.sqrt(x * x + y * y + z * z)
+    u, vv = t + r, t - r
+    eu, ev = np.exp(-lam * u ** 2), np.exp(-lam * vv ** 2)
+    deu, dev = -2 * lam * u * eu, -2 * lam * vv * ev
+    F = amp / r * ((ev - eu) / r ** 2 - 2 * lam * (vv * ev + u * eu) / r)
+    dF = amp / r * ((dev - deu) / r ** 2 - 2 * lam * (ev + vv * dev + eu + u * deu) / r)
+    Ac = [-y * F, x * F, 0.0 * x]
+    Ec = [y * dF, -x * dF, 0.0 * x]
+    Ji = _inv_general(J)
+    qf = hatted(gp)
+    ReU = qf["ReU"][:, None]  # (3, 1, n1, n0)
+    out = np.zeros((8,) + gp.shape)
+    for i in range(3):
+        out[1 + i] = sum(Ji[i, j] * Ac[j] for j in range(3)) / ReU[i]
+        out[4 + i] = sum(Ji[i, j] * Ec[j] for j in range(3)) / ReU[i]
+    return out

@@ -14,7 +14,8 @@ Writes:
       on seeded inputs (tests/helpers.py bssn_random_state / numpy
       default_rng): Ricci, rhs_eval, Hamiltonian at interior points,
       enforce_detgammabar_constraint (hDD at all points), Brill-Lindquist
-      initial_data (interior points); rhs_eval for ScalarWave / Maxwell;
+      initial_data (interior points); rhs_eval for ScalarWave / Maxwell
+      (System I Cartesian, System II curvilinear rescaled);
       for bssn_ko_*: rhs_eval with Kreiss-Oliger dissipation on seeded
       state and auxevol inputs; for bssn_psi4_*: the six pieces of psi_4;
       for bssn_src_*: rhs_eval with T^{mu nu} source terms (auxevol = 6
@@ -58,6 +59,7 @@ FIXTURE_GRIDS = {
     "bssn_ko_cart_fd6": ("Cartesian", (6, 6, 6), 6, 4, 19),
     "bssn_psi4_sph_fd4": ("Spherical", (8, 6, 4), 4, 3, 20),
     "bssn_src_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 21),
+    "maxwell_curvi_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 22),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -116,7 +118,7 @@ def ref_outputs():
             out["enforce_hDD"] = R.enforce(f)[11:17]
             out["bl_id"] = R.initial_data((24,) + gp.shape)[I]
         else:
-            ngf = 7 if cfg.startswith("maxwell") else 2
+            ngf = 8 if cfg.startswith("maxwell_curvi") else 7 if cfg.startswith("maxwell") else 2
             f = np.random.default_rng(seed).standard_normal((ngf,) + gp.shape)
             out["rhs"] = R.rhs_eval(f)[I]
         np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % cfg), **out)
@@ -239,6 +241,13 @@ TRUSTED += [
      "import BSSN.Psi4 as M", "M.Psi4(specify_tetrad=False)", ["psi4_re_pt", "psi4_im_pt"]),
     ("Psi4_tetrads", "BSSN", "Psi4_tetrads__Psi4_tetrads__globals",
      "import BSSN.Psi4_tetrads as M", "M.Psi4_tetrads()", ["l4U", "n4U", "mre4U", "mim4U"]),
+]
+TRUSTED += [
+    ("Maxwell_Curvi", "Maxwell", "MWEvol_Curvi__VacuumMaxwellRHSs_rescaled__globals",
+     "import NRPy_param_funcs as par\n"
+     "par.initialize_param(par.glb_param('char', 'Maxwell.InitialData','System_to_use','System_II'))\n"
+     "import Maxwell.VacuumMaxwell_Flat_Evol_Curvilinear_rescaled as M", "M.VacuumMaxwellRHSs_rescaled()",
+     ["erhsU", "arhsU", "psi_rhs", "Gamma_rhs", "C", "G", "EU_Cart", "AU_Cart"]),
 ]
 _RFM_INIT = ("import BSSN.BSSN_quantities as Bq\nimport reference_metric as rfm\nrfm.reference_metric()\n"
              "rfm.ref_metric__hatted_quantities()\nimport BSSN.BSSN_stress_energy_source_terms as M")

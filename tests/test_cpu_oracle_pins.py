@@ -232,6 +232,41 @@ def test_trusted_scalarwave(case, cart):
     assert close(float(np.ravel(w)[0]), ex["vv_rhs"], 1e-12)
 
 
+def test_trusted_maxwell_curvilinear_rescaled():
+    """VacuumMaxwellRHSs_rescaled (System II, Spherical): a, e, psi, Gamma
+    RHSs and the C, G constraints from md5-seeded symbols."""
+    inp = TV["Maxwell_Curvi"]["inputs"]
+    R3_ = range(3)
+    v = {"aU": np.array([[inp.get("aU%d" % i, 0.0)] for i in R3_]),
+         "eU": np.array([[inp.get("eU%d" % i, 0.0)] for i in R3_]),
+         "Gamma": np.array([inp.get("Gamma", 0.0)]),
+         "aU_dD": np.array([[[inp.get("aU_dD%d%d" % (i, j), 0.0)] for j in R3_] for i in R3_]),
+         "eU_dD": np.array([[[inp.get("eU_dD%d%d" % (i, j), 0.0)] for j in R3_] for i in R3_]),
+         "aU_dDD": np.array([[[[inp.get("aU_dDD%d%d%d" % ((i,) + tuple(sorted((j, k)))), 0.0)] for k in R3_]
+                              for j in R3_] for i in R3_]),
+         "psi_dD": np.array([[inp.get("psi_dD%d" % j, 0.0)] for j in R3_]),
+         "psi_dDD": np.array([[[inp.get("psi_dDD%d%d" % tuple(sorted((j, k))), 0.0)] for k in R3_] for j in R3_]),
+         "Gamma_dD": np.array([[inp.get("Gamma_dD%d" % j, 0.0)] for j in R3_])}
+    q = og.hatted_at("Spherical", inp.get("xx0", 0.0), inp.get("xx1", 0.0))
+    q = {k: a[..., 0] for k, a in q.items()}
+    arhs, erhs, psi_rhs, Grhs, Cc, Gc = ow.maxwell_curvi_pointwise(v, q)
+    ex = expect("Maxwell_Curvi")
+    for i in R3_:
+        assert close(float(arhs[i][0]), ex["arhsU[%d]" % i], 1e-12)
+        assert close(float(erhs[i][0]), ex["erhsU[%d]" % i], 1e-12)
+    assert close(float(psi_rhs[0]), ex["psi_rhs"], 1e-12)
+    assert close(float(Grhs[0]), ex["Gamma_rhs"], 1e-12)
+    assert close(float(Cc[0]), ex["C"], 1e-12)
+    assert close(float(Gc[0]), ex["G"], 1e-12)
+    # AU_Cart, EU_Cart: J^i_j A^j with J = d x_Cart / d xx
+    import oracle.psi4 as op
+    _, J = op.cart_and_jacobian(og.SPH, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("xx2", 0.0))
+    for nm, base in (("AU_Cart", "aU"), ("EU_Cart", "eU")):
+        V = v[base][:, 0] * q["ReU"][:, 0]
+        for i in R3_:
+            got = float(sum(J[i, j] * V[j] for j in R3_))
+            assert close(got, ex["%s[%d]" % (nm, i)], 1e-12), nm
+
 def test_trusted_maxwell_system_I():
     inp = TV["Maxwell_I"]["inputs"]
     v = symbols(inp, ["EU", "AU", "psi"])
@@ -356,7 +391,9 @@ def test_oracle_swsh_matches_reference_generated_c():
 
 @pytest.mark.parametrize("cfg,cs,fn,ngf", [("sw_cart_fd4", "Cartesian", ow.scalarwave_rhs_grid, 2),
                                           ("sw_sinhsph_fd4", "SinhSpherical", ow.scalarwave_rhs_grid, 2),
-                                          ("maxwell_cart_fd4", "Cartesian", ow.maxwell_rhs_grid, 7)])
+                                          ("maxwell_cart_fd4", "Cartesian", ow.maxwell_rhs_grid, 7),
+                                          ("maxwell_curvi_sinhsph_fd4", "SinhSpherical", ow.maxwell_curvi_rhs_grid,
+                                           8)])
 def test_oracle_matches_reference_generated_wave_maxwell(cfg, cs, fn, ngf):
     z = np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))
     gp = og.GridParams(cs, tuple(z["Nxx"]), int(z["ng"]), int(z["fd"]), **KW)
