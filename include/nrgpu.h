@@ -53,6 +53,8 @@ extern "C" {
 #define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
 #define NRGPU_SYS_MAXWELL     1   /* AU0..2, EU0..2, psi  (System I)          */
 #define NRGPU_SYS_BSSN        2   /* 24 evolved gfs, alphabetical             */
+#define NRGPU_SYS_MAXWELL_CURVILINEAR 3  /* Gamma, aU0..2, eU0..2, psi (System II
+                                    rescaled, VacuumMaxwell_Flat_Evol_Curvilinear_rescaled.py) */
 
 #define NRGPU_PREC_FP64   0       /* everything FP64                          */
 #define NRGPU_PREC_MIXED  1       /* FP32 stage buffers + FP32 RHS, FP64 y_n  */
@@ -236,6 +238,21 @@ int Maxwell_rhs_eval_f32(const paramstruct *params, const float *in_gfs, float *
 /* Maxwell divergence constraint C = d_i E^i at interior points
  * (VacuumMaxwell_Flat_Evol_Cartesian.py:49-52) into aux_gfs[0]. */
 int Maxwell_Constraints(const paramstruct *params, const double *in_gfs, double *aux_gfs);
+/* Vacuum Maxwell System II in rescaled curvilinear form
+ * (Maxwell/VacuumMaxwell_Flat_Evol_Curvilinear_rescaled.py:22-190; the
+ * rhs_eval of Tutorial-Start_to_Finish-Solving_Maxwells_Equations_in_Vacuum-
+ * Curvilinear.ipynb): 8 gridfunctions Gamma, aU0..2, eU0..2, psi.  rfm may be
+ * NULL on a Cartesian grid.  Constraints C (divergence of E) and G
+ * (Gamma - div A) into aux_gfs[0], aux_gfs[1].  Toroidal-dipole data in the
+ * grid's basis (Maxwell/InitialData.py:26-117, System II) at every point. */
+int MaxwellCurvilinear_rhs_eval(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+                                double *rhs_gfs);
+int MaxwellCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params, const float *in_gfs,
+                                    float *rhs_gfs);
+int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+                                   double *aux_gfs);
+int MaxwellCurvilinear_initial_data_toroidal_dipole(const paramstruct *params, double amp, double lam,
+                                                    double time, double *in_gfs);
 /* BSSN conformal Ricci tensor into auxevol_gfs (RbarDD00..22, 6 gfs):
  * Ricci_eval(rfmstruct, params, in_gfs, auxevol_gfs)
  * (BSSN_quantities.py:260-425; Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:501-502) */

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libnrgpu.so")
 
 COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2}
-SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2}
+SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
 
@@ -98,6 +98,11 @@ _PROTOS = {
     "BSSN_rhs_eval_xx": (C.c_int, [P(paramstruct), P(C.c_void_p), vp, vp, vp]),
     "BSSN_momentum_constraint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "BSSN_psi4": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp, C.c_int, C.c_int]),
+    "MaxwellCurvilinear_rhs_eval": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "MaxwellCurvilinear_rhs_eval_f32": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "MaxwellCurvilinear_constraints": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "MaxwellCurvilinear_initial_data_toroidal_dipole": (C.c_int, [P(paramstruct), C.c_double, C.c_double,
+                                                                  C.c_double, vp]),
     "BSSN_constraints_add_source_terms": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp, vp, vp]),
     "BSSN_psi4_spinweightm2_decomposition": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp]),
     "ScalarWave_initial_data": (C.c_int, [P(paramstruct), C.c_int, C.c_double, P(C.c_double), C.c_double, vp]),

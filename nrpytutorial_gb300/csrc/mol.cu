@@ -18,6 +18,7 @@ namespace nrgpu {
 // 4..9 rank-2 components 00,01,02,11,12,22).
 static const int8_t kParitySW[2] = {0, 0};                           // uu vv
 static const int8_t kParityMaxwell[7] = {1, 2, 3, 1, 2, 3, 0};       // AU0-2 EU0-2 psi
+static const int8_t kParityMaxwellCurvi[8] = {0, 1, 2, 3, 1, 2, 3, 0};  // Gamma aU0-2 eU0-2 psi
 static const int8_t kParityBSSN[24] = {4, 5, 6, 7, 8, 9,             // aDD00..aDD22
                                        0,                            // alpha
                                        1, 2, 3,                      // betU0..2
@@ -32,6 +33,7 @@ int system_num_gfs(int system) {
     case NRGPU_SYS_SCALARWAVE: return 2;
     case NRGPU_SYS_MAXWELL: return 7;
     case NRGPU_SYS_BSSN: return 24;
+    case NRGPU_SYS_MAXWELL_CURVILINEAR: return 8;
   }
   return -1;
 }
@@ -40,6 +42,7 @@ const int8_t *system_parity(int system) {
     case NRGPU_SYS_SCALARWAVE: return kParitySW;
     case NRGPU_SYS_MAXWELL: return kParityMaxwell;
     case NRGPU_SYS_BSSN: return kParityBSSN;
+    case NRGPU_SYS_MAXWELL_CURVILINEAR: return kParityMaxwellCurvi;
   }
   return nullptr;
 }
@@ -109,6 +112,7 @@ static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, co
   switch (system) {
     case NRGPU_SYS_SCALARWAVE: return scalarwave_launch(rfm, p, a);
     case NRGPU_SYS_MAXWELL: return maxwell_launch(p, a);
+    case NRGPU_SYS_MAXWELL_CURVILINEAR: return maxwell_curvi_launch(rfm, p, a);
     case NRGPU_SYS_BSSN: {
       int st = bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
       if (st) return st;

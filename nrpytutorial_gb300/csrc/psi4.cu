@@ -29,56 +29,6 @@ using namespace bssn;
 
 constexpr double kIsqrt2 = 0.707106781186547524400844362104849039;
 
-// xx -> Cartesian and d x_Cart^i / d xx^j (reference_metric.py xx_to_Cart).
-template <int CS>
-__device__ __forceinline__ void cart_jacobian(double xx0, double xx1, double xx2, double AMPL, double SINHW,
-                                              double x[3], double J[3][3]) {
-  if constexpr (CS == NRGPU_COORD_CARTESIAN) {
-    x[0] = xx0;
-    x[1] = xx1;
-    x[2] = xx2;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) J[i][j] = i == j ? 1.0 : 0.0;
-  } else {
-    double r, r1, r2, r3;
-    radial_map(CS, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
-    const double st = sin(xx1), ct = cos(xx1), sp = sin(xx2), cp = cos(xx2);
-    x[0] = r * st * cp;
-    x[1] = r * st * sp;
-    x[2] = r * ct;
-    J[0][0] = r1 * st * cp;
-    J[0][1] = r * ct * cp;
-    J[0][2] = -r * st * sp;
-    J[1][0] = r1 * st * sp;
-    J[1][1] = r * ct * sp;
-    J[1][2] = r * st * cp;
-    J[2][0] = r1 * ct;
-    J[2][1] = -r * st;
-    J[2][2] = 0.0;
-  }
-}
-
-// General 3x3 inverse by cofactors (indexedexp.py generic_matrix_inverter3x3).
-__device__ __forceinline__ void inverse3(const double J[3][3], double Ji[3][3]) {
-  Ji[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-  Ji[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-  Ji[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-  Ji[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-  Ji[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-  Ji[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-  Ji[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-  Ji[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-  Ji[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-  const double det = J[0][0] * Ji[0][0] + J[0][1] * Ji[1][0] + J[0][2] * Ji[2][0];
-  const double id = 1.0 / det;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) Ji[i][j] *= id;
-}
-
 __device__ __forceinline__ double omega(const double u[3], const double w[3], const double g[3][3]) {
   double s = 0.0;
 #pragma unroll
@@ -309,7 +259,7 @@ __device__ void psi4_point(const Point<double> &P, const Rfm<CS, double> &rf, co
 
 // One thread per point of the i0 range x interior (i1, i2), i0 fastest: a
 // single extraction shell fills whole warps too.
-constexpr int kPsi4Threads = 64;
+constexpr int kPsi4Threads = 32;
 template <int CS, int ORDER>
 __global__ void __launch_bounds__(kPsi4Threads) psi4_kernel(Grid g, const double *__restrict__ in,
                                                             const double *__restrict__ tab, paramstruct p, int i0lo,

@@ -31,6 +31,7 @@ template <typename Tin> inline typename InRef<Tin>::type stage_input(const Stage
 
 int scalarwave_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 int maxwell_launch(const paramstruct *p, const StageArgs &a);
+int maxwell_curvi_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64,
                       int prec, void *auxevol);
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);

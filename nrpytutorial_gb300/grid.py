@@ -16,6 +16,7 @@ from . import _lib
 SYSTEM_GFS = {
     "ScalarWave": (["uu", "vv"], [0, 0]),
     "Maxwell": (["AU0", "AU1", "AU2", "EU0", "EU1", "EU2", "psi"], [1, 2, 3, 1, 2, 3, 0]),
+    "MaxwellCurvilinear": (["Gamma", "aU0", "aU1", "aU2", "eU0", "eU1", "eU2", "psi"], [0, 1, 2, 3, 1, 2, 3, 0]),
     "BSSN": (["aDD00", "aDD01", "aDD02", "aDD11", "aDD12", "aDD22", "alpha",
               "betU0", "betU1", "betU2", "cf",
               "hDD00", "hDD01", "hDD02", "hDD11", "hDD12", "hDD22",

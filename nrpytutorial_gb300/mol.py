@@ -155,6 +155,9 @@ class Evolution:
                     self._rfm(), p, _lib.ptr(in_gfs), _lib.ptr(rhs_gfs))
         elif self.system == "Maxwell":
             st = getattr(self.lib, "Maxwell_rhs_eval" + sfx)(p, _lib.ptr(in_gfs), _lib.ptr(rhs_gfs))
+        elif self.system == "MaxwellCurvilinear":
+            st = getattr(self.lib, "MaxwellCurvilinear_rhs_eval" + sfx)(self._rfm(), p, _lib.ptr(in_gfs),
+                                                                        _lib.ptr(rhs_gfs))
         else:
             aux = self.auxevol if auxevol is None else auxevol
             _lib.check(getattr(self.lib, "BSSN_Ricci_eval" + sfx)(self._rfm(), p, _lib.ptr(in_gfs), _lib.ptr(aux)),
@@ -272,6 +275,31 @@ class Evolution:
         p = self.grid.params
         r = x0 if p.CoordSystem == 1 else p.AMPL * np.sinh(x0 / p.SINHW) / np.sinh(1.0 / p.SINHW)
         return out, r
+
+    def maxwell_curvilinear_constraints(self, gfs=None):
+        """(C, G) of curvilinear Maxwell System II at interior points (FP64)."""
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        out = torch.zeros((2,) + self.grid.shape, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.MaxwellCurvilinear_constraints(self._rfm(), C.byref(self.grid.params), _lib.ptr(gfs),
+                                                           _lib.ptr(out)), "MaxwellCurvilinear_constraints")
+        return out
+
+    def initial_data_toroidal_dipole(self, amp=1.0, lam=1.0, time=0.0, gfs=None):
+        """Toroidal-dipole data (Maxwell/InitialData.py) for Maxwell (System I,
+        Cartesian) or MaxwellCurvilinear (System II in the grid's basis)."""
+        self._sync_stream()
+        gfs = self.y_n if gfs is None else gfs
+        p = C.byref(self.grid.params)
+        if self.system == "MaxwellCurvilinear":
+            st = self.lib.MaxwellCurvilinear_initial_data_toroidal_dipole(p, float(amp), float(lam), float(time),
+                                                                          _lib.ptr(gfs))
+        elif self.system == "Maxwell":
+            st = self.lib.Maxwell_initial_data_toroidal_dipole(p, float(amp), float(lam), float(time), _lib.ptr(gfs),
+                                                               None, None)
+        else:
+            raise ValueError("toroidal-dipole data belong to the Maxwell systems")
+        _lib.check(st, "initial_data_toroidal_dipole")
 
     def maxwell_constraint(self, gfs=None):
         self._sync_stream()
