@@ -316,7 +316,8 @@ def run_gpu(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
         "ms_per_step": tc / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 RHS on compensated f32 (hi,lo) stage pairs; f64 RK state",
+        "dtype": "f32 RHS on compensated f32 (hi,lo) stage pairs; RK accumulation in float-float (48-bit "
+                 "significand) on the FP32 pipe; f64 RK state between steps",
         "data": "synthetic: Brill-Lindquist initial data computed on the GPU",
         "config": {"workload": W["name"], "Nxx": list(W["Nxx"]), "NGHOSTS": W["ng"], "FD_order": W["fd"],
                    "interior_points": nint, "parallelism": "replicas" if world > 1 else "single",

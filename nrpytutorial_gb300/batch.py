@@ -146,8 +146,8 @@ class ScalarWaveBatch:
         callable that replays them on the current stream."""
         g = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream(self.device)
+        snapshot = self.y_n.clone()  # before the side stream waits: the warm-up step rewrites y_n
         side.wait_stream(torch.cuda.current_stream(self.device))
-        snapshot = self.y_n.clone()
         with torch.cuda.stream(side):
             self.step()  # warm-up outside the graph
         torch.cuda.current_stream(self.device).wait_stream(side)

@@ -41,6 +41,7 @@ struct BatchInstance {
   double invdx0, invdx1, invdx2;
   double dxx0, dxx1;       // uniform spacings, for the coordinates xx0, xx1
   double dt;               // this instance's time step
+  StageConsts kc;          // dt/6, dt/3, dt/2, dt as FP32 pairs (FP32 stage modes)
 };
 
 constexpr int kBatchNG = 2;     // FD4 ScalarWave ghost zones
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(TX *TY)
       RKEpilogue<TStage> e = epi;
       e.ntot = I.ntot;
       e.dt = I.dt;
+      e.kc = I.kc;
       e.y_n = epi.y_n ? epi.y_n + I.base : nullptr;
       e.rt = epi.rt ? epi.rt + I.base : nullptr;
       e.out = epi.out ? epi.out + I.base : nullptr;
@@ -172,10 +174,67 @@ __global__ void sw_batch_bc_kernel(const BatchInstance *__restrict__ insts, cons
   }
 }
 
-// y_n -> FP32 (hi, lo) pairs over all packed points.
-__global__ void sw_batch_split_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = split_pair(y[i]);
+// Level-scheduled boundary conditions.  A ghost point's level is 1 + the
+// largest level among the points it reads (interior points: 0), following
+// the reference's sequential order (layers inner to outer; per layer outer
+// faces i0, i1, i2, then inner points).  When no point is read before the
+// sequence writes it (checked on the host), every point of one level can be
+// filled at once, from the same final source values and with the same
+// arithmetic as the sequential application, so the result is bit-identical.
+// Per distinct instance shape one template holds the entries sorted by
+// level, outer before inner within a level; tpl_off[lvl][0 / 1] are the
+// starts of a level's outer / inner entries (lvl = 1..kBcMaxLevels + 1).
+constexpr int kBcMaxLevels = 8;
+constexpr int kBcOffStride = 2 * (kBcMaxLevels + 2);
+
+template <typename T>
+__device__ __forceinline__ void bc_apply_entry(T *f, long long ntot, long long d, long long e, bool inner) {
+#pragma unroll
+  for (int g = 0; g < 2; g++) {
+    T *fg = f + g * ntot;
+    fg[d] = inner ? fg[e] : bc_extrapolate(fg + d, e);  // scalars: parity +1
+  }
+}
+
+// Level 1 of every instance: grid (chunks, instances), grid-stride within
+// the instance's template.
+template <typename T>
+__global__ void sw_batch_bc_level1_kernel(const BatchInstance *__restrict__ insts, const int *__restrict__ tpl_off,
+                                          const int *__restrict__ ta, const int *__restrict__ tb, T *gfs) {
+  const BatchInstance I = insts[blockIdx.y];
+  const int *o = tpl_off + I.pad * kBcOffStride;
+  const int si = o[3], e = o[4];
+  T *f = gfs + I.base;
+  for (int p = o[2] + blockIdx.x * blockDim.x + threadIdx.x; p < e; p += gridDim.x * blockDim.x)
+    bc_apply_entry(f, I.ntot, ta[p], tb[p], p >= si);
+}
+
+// Levels 2..nlev of one instance per block, a block barrier between levels.
+template <typename T>
+__global__ void sw_batch_bc_levels_kernel(const BatchInstance *__restrict__ insts, const int *__restrict__ tpl_off,
+                                          const int *__restrict__ ta, const int *__restrict__ tb, int nlev, T *gfs) {
+  const BatchInstance I = insts[blockIdx.x];
+  const int *o = tpl_off + I.pad * kBcOffStride;
+  T *f = gfs + I.base;
+  for (int lv = 2; lv <= nlev; lv++) {
+    const int si = o[2 * lv + 1], e = o[2 * lv + 2];
+    for (int p = o[2 * lv] + threadIdx.x; p < e; p += blockDim.x) bc_apply_entry(f, I.ntot, ta[p], tb[p], p >= si);
+    __syncthreads();
+  }
+}
+
+// Start of an FP32-stage step over all packed points: y_n split in place
+// into (hi, lo) pairs (the float-float accumulation state, and the
+// compensated substep-0 input), and for plain FP32 stages also y_n rounded
+// to FP32 into `f` (substep 0's input).
+template <bool ROUND>
+__global__ void sw_batch_prep_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = split_pair_fast(y[i]);
+    if (ROUND) f[i] = p.x;
+    ((float2 *)y)[i] = p;
+  }
 }
 
 }  // namespace nrgpu
@@ -195,6 +254,10 @@ struct nrgpu_batch {
   float *d_tab32 = nullptr;
   // boundary phases: per instance, kBatchPhases+1 offsets into a/b
   int *d_bc_phases = nullptr, *d_bc_a = nullptr, *d_bc_b = nullptr;
+  // level-scheduled boundary templates (one per distinct instance shape)
+  bool bc_levels = false;
+  int bc_nlev = 0, bc_l1_max = 0;
+  int *d_tpl_off = nullptr, *d_tpl_a = nullptr, *d_tpl_b = nullptr;
   // tuned launch shape
   int tx = 64, tyi = 1, grid = 0;
   int bc_threads = 256;  // block size of the boundary-condition kernel
@@ -207,6 +270,9 @@ static void batch_destroy(nrgpu_batch *b) {
   cudaFree(b->d_bc_phases);
   cudaFree(b->d_bc_a);
   cudaFree(b->d_bc_b);
+  cudaFree(b->d_tpl_off);
+  cudaFree(b->d_tpl_a);
+  cudaFree(b->d_tpl_b);
   cudaFree(b->d_tab64);
   cudaFree(b->d_tab32);
   delete b;
@@ -254,6 +320,19 @@ static int batch_launch_rhs(nrgpu_batch *b, const void *in, bool in_f64, int sta
 }
 
 template <typename T> static int batch_bcs(nrgpu_batch *b, T *gfs) {
+  if (b->bc_levels) {
+    const int t = b->bc_threads;
+    const int chunks = std::max(1, std::min(64, (b->bc_l1_max + 4 * t - 1) / (4 * t)));
+    sw_batch_bc_level1_kernel<T><<<dim3(chunks, b->ninst), t, 0, stream()>>>(b->d_insts, b->d_tpl_off, b->d_tpl_a,
+                                                                             b->d_tpl_b, gfs);
+    NRGPU_LAUNCH_CHECK();
+    if (b->bc_nlev >= 2) {
+      sw_batch_bc_levels_kernel<T><<<b->ninst, t, 0, stream()>>>(b->d_insts, b->d_tpl_off, b->d_tpl_a, b->d_tpl_b,
+                                                                 b->bc_nlev, gfs);
+      NRGPU_LAUNCH_CHECK();
+    }
+    return NRGPU_OK;
+  }
   sw_batch_bc_kernel<T><<<b->ninst, b->bc_threads, 0, stream()>>>(b->d_insts, b->d_bc_phases, b->d_bc_a, b->d_bc_b,
                                                                   gfs);
   NRGPU_LAUNCH_CHECK();
@@ -285,6 +364,11 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
   std::vector<BatchWork> work[4];
   const int TYs[4] = {1, 2, 4, 8};
   std::vector<int> bphase, ba, bb;  // per-instance phase offsets; dest; step or src
+  // level templates, one per distinct (n0, n1, n2)
+  std::vector<long long> tpl_key;
+  std::vector<int> tpl_off, tpl_a, tpl_b;
+  bool levels_ok = true;
+  int nlev_all = 1, l1_max = 0;
   for (int i = 0; i < ninst; i++) {
     paramstruct p{};
     p.CoordSystem = CoordSystem;
@@ -316,6 +400,7 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
     I.invdx2 = p.invdx2;
     I.dxx0 = p.dxx0;
     I.dt = find_timestep(&p, CFL_FACTOR);
+    I.kc = stage_consts(I.dt);
     I.dxx1 = p.dxx1;
     base += 2 * I.ntot;
     tab += (long long)kBatchTab * I.n0 * I.n1;
@@ -358,7 +443,68 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
       }
     }
     bphase.push_back((int)ba.size());  // end of this instance's last phase
+    // level template of this shape (built once per distinct shape)
+    const long long key = ((long long)I.n0 * 4096 + I.n1) * 4096 + I.n2;
+    int tid = (int)(std::find(tpl_key.begin(), tpl_key.end(), key) - tpl_key.begin());
+    if (tid == (int)tpl_key.size() && levels_ok) {
+      // the sequential order: per layer, outer faces i0, i1, i2, then inner points
+      struct Ent {
+        int d, e;
+        bool inner;
+      };
+      std::vector<Ent> seq;
+      for (int g = 0; g < kBatchNG; g++) {
+        for (int k = bc.ob_dir_start[g][0]; k < bc.ob_dir_start[g][3]; k++) seq.push_back({od[k], os[k], false});
+        for (int k = bc.ib_start[g]; k < bc.ib_start[g] + bc.num_ib_gz_pts[g]; k++)
+          seq.push_back({id_[k], is[k], true});
+      }
+      std::vector<int> worder(I.ntot, -1), lvl(I.ntot, 0);
+      for (int k = 0; k < (int)seq.size(); k++) {
+        if (worder[seq[k].d] >= 0) levels_ok = false;  // written twice
+        worder[seq[k].d] = k;
+      }
+      int L = 0;
+      for (int k = 0; k < (int)seq.size() && levels_ok; k++) {
+        const Ent &en = seq[k];
+        int lv = 0;
+        const int nsrc = en.inner ? 1 : 3;
+        for (int j = 0; j < nsrc; j++) {
+          const long long x = en.inner ? en.e : (long long)en.d + (long long)(j + 1) * en.e;
+          if (x < 0 || x >= I.ntot) {
+            levels_ok = false;
+            break;
+          }
+          if (worder[x] > k) levels_ok = false;        // read before it is written: keep the phases
+          else if (worder[x] >= 0) lv = std::max(lv, lvl[x]);
+        }
+        lvl[en.d] = lv + 1;
+        L = std::max(L, lv + 1);
+      }
+      if (L > kBcMaxLevels) levels_ok = false;
+      if (levels_ok) {
+        tpl_key.push_back(key);
+        std::vector<int> off(kBcOffStride, 0);
+        for (int lv = 1; lv <= kBcMaxLevels + 1; lv++) {
+          for (int inner = 0; inner < 2; inner++) {
+            off[2 * lv + inner] = (int)tpl_a.size();
+            if (lv > L) continue;
+            for (const Ent &en : seq)
+              if (lvl[en.d] == lv && (int)en.inner == inner) {
+                tpl_a.push_back(en.d);
+                tpl_b.push_back(en.e);
+              }
+          }
+        }
+        l1_max = std::max(l1_max, off[4] - off[2]);
+        nlev_all = std::max(nlev_all, L);
+        tpl_off.insert(tpl_off.end(), off.begin(), off.end());
+      }
+    }
+    b->h_insts.back().pad = tid;
   }
+  b->bc_levels = levels_ok && !tpl_key.empty();
+  b->bc_nlev = nlev_all;
+  b->bc_l1_max = l1_max;
   b->total_points = base;
   auto up = [&](void **dst, const void *src, size_t bytes) -> int {
     *dst = nullptr;
@@ -381,6 +527,11 @@ int nrgpu_batch_create(int ninst, const int *Nr, int Ntheta, int Nphi, int Coord
   NRGPU_BATCH_TRY(up((void **)&b->d_bc_phases, bphase.data(), bphase.size() * sizeof(int)))
   NRGPU_BATCH_TRY(up((void **)&b->d_bc_a, ba.data(), ba.size() * sizeof(int)))
   NRGPU_BATCH_TRY(up((void **)&b->d_bc_b, bb.data(), bb.size() * sizeof(int)))
+  if (b->bc_levels) {
+    NRGPU_BATCH_TRY(up((void **)&b->d_tpl_off, tpl_off.data(), tpl_off.size() * sizeof(int)))
+    NRGPU_BATCH_TRY(up((void **)&b->d_tpl_a, tpl_a.data(), tpl_a.size() * sizeof(int)))
+    NRGPU_BATCH_TRY(up((void **)&b->d_tpl_b, tpl_b.data(), tpl_b.size() * sizeof(int)))
+  }
   NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab64, tab * sizeof(double)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
   NRGPU_BATCH_TRY(cudaMalloc(&b->d_tab32, tab * sizeof(float)) == cudaSuccess ? NRGPU_OK : NRGPU_ERR_CUDA)
 #undef NRGPU_BATCH_TRY
@@ -569,14 +720,19 @@ int nrgpu_batch_step(nrgpu_batch *b, MoL_gridfunctions *gfs) {
   const bool f64 = b->prec == NRGPU_PREC_FP64, pair = b->prec == NRGPU_PREC_COMPENSATED;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   int st;
-  if (pair) {  // substep 0 reads y_n as FP32 pairs from k_even
+  if (!f64) {  // y_n -> pairs in place (+ FP32 copy in k_even for plain FP32 stages)
     const int blocks = (int)std::min<long long>((b->total_points + 255) / 256, 152LL * 16);
-    sw_batch_split_kernel<<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
+    if (pair)
+      sw_batch_prep_kernel<false><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs, nullptr);
+    else
+      sw_batch_prep_kernel<true><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs,
+                                                               (float *)gfs->k_even_gfs);
     NRGPU_LAUNCH_CHECK();
   }
   for (int s = 0; s < 4; s++) {
-    const void *in = (s == 0) ? (pair ? gfs->k_even_gfs : (const void *)gfs->y_n_gfs) : kbuf[(s + 1) % 2];
-    const bool in_f64 = !pair && ((s == 0) || f64);
+    // substep 0 input: y_n (FP64), its pairs in place (compensated), its FP32 copy (mixed)
+    const void *in = (s == 0) ? (f64 || pair ? (const void *)gfs->y_n_gfs : gfs->k_even_gfs) : kbuf[(s + 1) % 2];
+    const bool in_f64 = f64;
     void *out = (s == 3) ? nullptr : kbuf[s % 2];
     if ((st = batch_launch_rhs(b, in, in_f64, s, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, out))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];

@@ -304,12 +304,12 @@ int rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a
         g, (const double *)a.in, (const double *)a.auxevol, table_of<double>(rfm), p->eta, p->diss_strength,
         t4uu_of<double>(p, a.auxevol, g.ntot), epi);
   } else if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
     rhs_kernel<float, Pair32, CS, ORDER, float2, EXTRA><<<L.grid, L.block, 0, stream()>>>(
         g, stage_input<Pair32>(a), (const float *)a.auxevol, table_of<float>(rfm), eta32, diss32,
         t4uu_of<float>(p, a.auxevol, g.ntot), epi);
   } else {
-    RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
+    RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};
     if (a.in_is_f64)
       rhs_kernel<float, double, CS, ORDER, float, EXTRA><<<L.grid, L.block, 0, stream()>>>(
           g, (const double *)a.in, (const float *)a.auxevol, table_of<float>(rfm), eta32, diss32,

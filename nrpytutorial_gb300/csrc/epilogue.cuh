@@ -11,6 +11,16 @@
 //   substep 3: y_n = y_n + rt + k*dt*(1/6)
 // evaluated left to right in FP64 without FMA contraction, exactly as the
 // generated C writes it, so the fused update rounds like the reference's.
+// With FP32 stage buffers (mixed and compensated precision) GB300's FP64
+// pipe, which issues at 1/64 of the FP32 rate, would bound the update, so
+// the RK accumulation runs in float-float arithmetic on the FP32 pipe: at
+// the start of the step y_n is split in place into (hi, lo) pairs (the
+// y_n buffer holds pairs until substep 3), the running total is kept as
+// pairs in the rt buffer, dt*c are pair constants formed on the host, and
+// substep 3 writes y_n back as the FP64 sum hi + lo.  Accumulation then
+// carries ~48 significant bits (2^-48 ~ 3.6e-15 relative per update)
+// instead of FP64's 53, far below the FP32 RHS arithmetic's error, with
+// about 3 FP64-pipe instructions per value per step instead of ~26.
 #pragma once
 #include <type_traits>
 
@@ -22,6 +32,44 @@ namespace nrgpu {
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 
+// dt/6, dt/3, dt/2 and dt as FP32 (hi, lo) pairs (host).
+struct StageConsts {
+  float2 c6, c3, c2, c1;
+};
+inline float2 pair_const(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+inline StageConsts stage_consts(double dt) {
+  return StageConsts{pair_const(dt * (1.0 / 6.0)), pair_const(dt * (1.0 / 3.0)), pair_const(dt * 0.5),
+                     pair_const(dt)};
+}
+
+// Float-float RK4 substep update of value i (FP32 stage modes): y2, r2 are
+// the y_n and running-total buffers holding (hi, lo) pairs; returns the
+// stage value (substeps 0..2) or writes y_n[i] as FP64 (substep 3).  Shared
+// by the fused epilogue and the unfused update kernel, so both round alike.
+__device__ __forceinline__ float2 ff_rk4_update(int stage, float k, const StageConsts &kc, double *y_n, double *rt,
+                                                long long i) {
+  float2 *y2 = (float2 *)y_n, *r2 = (float2 *)rt;
+  switch (stage) {
+    case 0:
+      r2[i] = ff_mul(k, kc.c6);
+      return ff_add(y2[i], ff_mul(k, kc.c2));
+    case 1:
+      r2[i] = ff_add(r2[i], ff_mul(k, kc.c3));
+      return ff_add(y2[i], ff_mul(k, kc.c2));
+    case 2:
+      r2[i] = ff_add(r2[i], ff_mul(k, kc.c3));
+      return ff_add(y2[i], ff_mul(k, kc.c1));
+    default: {
+      const float2 s = ff_add(ff_add(y2[i], r2[i]), ff_mul(k, kc.c6));
+      y_n[i] = f2d_bits(s.x) + f2d_bits(s.y);
+      return s;
+    }
+  }
+}
+
 // RK4 substep update of one value; stage < 0 stores k itself into `out`.
 template <typename TStage> struct RKEpilogue {
   int stage;          // -1: plain store; 0..3: RK4 substep
@@ -31,11 +79,18 @@ template <typename TStage> struct RKEpilogue {
   double *rt;         // FP64 running total
   TStage *out;        // stage buffer (or rhs buffer for stage -1); float2:
                       // FP32 (hi, lo) pairs of the FP64 stage value
+  StageConsts kc;     // FP32 stage buffers: dt*c pairs (stage_consts(dt))
 
   // Stage value (computed in FP64) into the stage buffer.
   __device__ __forceinline__ void put(long long i, double v) const {
     if constexpr (std::is_same<TStage, float2>::value) out[i] = split_pair(v);
     else out[i] = (TStage)v;
+  }
+  // Stage value (a normalised pair) into an FP32 stage buffer: the pair, or
+  // its leading part (the FP32 rounding of the sum) for plain FP32 stages.
+  __device__ __forceinline__ void put_pair(long long i, float2 v) const {
+    if constexpr (std::is_same<TStage, float2>::value) out[i] = v;
+    else out[i] = (TStage)v.x;
   }
 
   template <typename R> __device__ __forceinline__ void operator()(int gf, long long idx, R value) const {
@@ -43,6 +98,11 @@ template <typename TStage> struct RKEpilogue {
     if (stage < 0) {
       if constexpr (std::is_same<TStage, float2>::value) out[i] = make_float2((float)value, 0.f);
       else out[i] = (TStage)value;
+      return;
+    }
+    if constexpr (!std::is_same<TStage, double>::value) {
+      const float2 v = ff_rk4_update(stage, (float)value, kc, y_n, rt, i);
+      if (stage < 3) put_pair(i, v);
       return;
     }
     const double kdt = dmul((double)value, dt);

@@ -223,12 +223,68 @@ __device__ __forceinline__ R fd_dupwind(const float2 *__restrict__ p, long long 
   return positive ? acc : -acc;
 }
 
+// ------------------------------------------- float-float (FP32 pair) arithmetic
+// Error-free transformations on the FP32 pipe (Dekker 1971; Knuth, TAOCP
+// vol. 2, 4.2.2; the FMA form of the product): a value is the unevaluated
+// sum hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  Written
+// with round-to-nearest intrinsics so no contraction changes them.
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+// a + b, both pairs; normalised result.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  float2 s = ff_two_sum(a.x, b.x);
+  const float2 t = ff_two_sum(a.y, b.y);
+  s = ff_fast_two_sum(s.x, __fadd_rn(s.y, t.x));
+  return ff_fast_two_sum(s.x, __fadd_rn(s.y, t.y));
+}
+// k * C, k an FP32 value, C a pair constant; normalised result.
+__device__ __forceinline__ float2 ff_mul(float k, float2 C) {
+  const float p = __fmul_rn(k, C.x);
+  const float e = __fmaf_rn(k, C.x, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(k, C.y, e));
+}
+
 // FP64 value -> (hi, lo) pair.
 __device__ __forceinline__ float2 split_pair(double v) {
   const float h = __double2float_rn(v);
   return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
 }
 __device__ __forceinline__ double pair_value(float2 p) { return (double)p.x + (double)p.y; }
+
+// The same conversions without the FP64 pipe (GB300 issues FP64 at 1/64 of
+// the FP32 rate).  float -> double is exact bit manipulation for zero and
+// normal floats; double -> pair truncates the significand after 24 bits for
+// hi (integer ops), converts the remaining 29 bits with one int->float
+// conversion scaled by an exact power of two, and normalises with an FP32
+// fast two-sum, so hi = RN(v) up to double rounding and hi + lo = v to
+// 2^-48 relative.  Zero is exact; values outside [2^-74, 2^128) (and inf,
+// NaN) take the FP64-pipe path.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if ((u << 1) == 0) return __longlong_as_double((long long)sign);  // +-0
+  const unsigned ex = (u >> 23) & 0xFFu;
+  if (ex == 0 || ex == 0xFFu) return (double)f;                   // subnormal, inf, NaN
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+__device__ __forceinline__ float2 split_pair_fast(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  if ((b << 1) == 0) return make_float2(__uint_as_float(sign), 0.f);  // +-0
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e < -74 || e > 127) return split_pair(v);
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+  const float mag = __fmul_rn(__uint2float_rn((unsigned)(b & 0x1FFFFFFFu)), __uint_as_float((unsigned)(e + 75) << 23));
+  return ff_fast_two_sum(hi, sign ? -mag : mag);
+}
 
 // Upwinded first derivative (unscaled): dupD if positive, else ddnD.
 // ddnD weights are the negated mirror image of dupD's, so one loop with a

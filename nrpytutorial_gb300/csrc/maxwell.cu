@@ -89,10 +89,10 @@ int maxwell_launch(const paramstruct *p, const StageArgs &a) {
     return dispatch<double, double, double>(p, g, stage_input<double>(a), epi);
   }
   if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
     return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), epi);
   }
-  RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
+  RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};
   if (a.in_is_f64) return dispatch<float, double, float>(p, g, stage_input<double>(a), epi);
   return dispatch<float, float, float>(p, g, stage_input<float>(a), epi);
 }

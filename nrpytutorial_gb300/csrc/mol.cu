@@ -65,10 +65,22 @@ template <typename TStage> __device__ __forceinline__ TStage from_double(double 
 }
 
 template <typename TStage>
-__global__ void rk4_update_kernel(int stage, double dt, long long n, double *__restrict__ y_n,
+__global__ void rk4_update_kernel(int stage, double dt, StageConsts kc, long long n, double *__restrict__ y_n,
                                   double *__restrict__ rt, TStage *__restrict__ k) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
+    if constexpr (!std::is_same<TStage, double>::value) {
+      // FP32 stages: the fused epilogue's float-float update (y_n, rt hold pairs)
+      float kv;
+      if constexpr (std::is_same<TStage, float2>::value) kv = k[i].x;  // rhs_eval stored (k, 0)
+      else kv = k[i];
+      const float2 v = ff_rk4_update(stage, kv, kc, y_n, rt, i);
+      if (stage < 3) {
+        if constexpr (std::is_same<TStage, float2>::value) k[i] = v;
+        else k[i] = v.x;
+      }
+      continue;
+    }
     const double kdt = __dmul_rn(as_double(k[i]), dt);
     switch (stage) {
       case 0:
@@ -88,13 +100,6 @@ __global__ void rk4_update_kernel(int stage, double dt, long long n, double *__r
         break;
     }
   }
-}
-
-// y_n -> FP32 (hi, lo) pairs over all points.
-__global__ void split_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    out[i] = split_pair(y[i]);
 }
 
 static int sm_count() {
@@ -142,12 +147,27 @@ static long long state_len(int system, const paramstruct *p) {
          p->Nxx_plus_2NGHOSTS2;
 }
 
-// Start of a compensated step: y_n -> pairs in k_even_gfs (substep 0's input).
-static int split_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
+// Start of a fused FP32-stage step: y_n split in place into (hi, lo) pairs
+// (the float-float accumulation state of the epilogue, and the compensated
+// substep-0 input); plain FP32 stages also get y_n rounded to FP32 in
+// k_even_gfs (their substep-0 input).
+template <bool ROUND>
+__global__ void prep_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = split_pair_fast(y[i]);
+    if (ROUND) f[i] = p.x;
+    ((float2 *)y)[i] = p;
+  }
+}
+static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
   const long long n = state_len(system, p);
   const int threads = 256;
   const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 8);
-  split_kernel<<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
+  if (gfs->precision == NRGPU_PREC_COMPENSATED)
+    prep_kernel<false><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, nullptr);
+  else
+    prep_kernel<true><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float *)gfs->k_even_gfs);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
@@ -182,16 +202,17 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
   const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
-  if (pair && (st = split_state(system, p, gfs))) return st;
+  if (!f64 && (st = prep_state(system, p, gfs))) return st;
   for (int s = 0; s < 4; s++) {
     StageArgs a{};
     a.stage = s;
     a.dt = dt;
     a.prec = gfs->precision;
-    // substep 0 reads y_n itself (as pairs in k_even when compensated)
-    a.in = (s == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
+    // substep 0 reads y_n: itself in FP64, its pairs in place when compensated,
+    // its FP32 copy in k_even for plain FP32 stages
+    a.in = (s == 0) ? (f64 || pair ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
                     : (const void *)kbuf[(s + 1) % 2];
-    a.in_is_f64 = !pair && ((s == 0) || f64);
+    a.in_is_f64 = f64;
     a.y_n = gfs->y_n_gfs;
     a.rt = gfs->y_nplus1_running_total_gfs;
     a.out = (s == 3) ? nullptr : kbuf[s % 2];
@@ -256,7 +277,7 @@ int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const
     if ((st = apply_sommerfeld_impl(p, nullptr, bc, ngf, system_parity(system), (const double *)a.in,
                                     (double *)kbuf[s % 2])))
       return st;
-    rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+    rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, StageConsts{}, n, gfs->y_n_gfs,
                                                                 gfs->y_nplus1_running_total_gfs,
                                                                 (double *)kbuf[s % 2]);
     NRGPU_LAUNCH_CHECK();
@@ -277,28 +298,29 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
   const long long n = state_len(system, p);
   const int threads = 256;
   const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 16);
-  if (pair && (st = split_state(system, p, gfs))) return st;
+  if (!f64 && (st = prep_state(system, p, gfs))) return st;
+  const StageConsts kc = stage_consts(dt);
   for (int s = 0; s < 4; s++) {
     StageArgs a{};
     a.stage = -1;
     a.dt = dt;
     a.prec = gfs->precision;
-    a.in = (s == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
+    a.in = (s == 0) ? (f64 || pair ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
                     : (const void *)kbuf[(s + 1) % 2];
-    a.in_is_f64 = !pair && ((s == 0) || f64);
+    a.in_is_f64 = f64;
     a.out = kbuf[s % 2];  // RHS_output: k_odd, k_even, k_odd, k_even
     a.auxevol = gfs->auxevol_gfs;
     if ((st = rhs_stage(system, rfm, p, a))) return st;
     if (pair)
-      rk4_update_kernel<float2><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+      rk4_update_kernel<float2><<<blocks, threads, 0, stream()>>>(s, dt, kc, n, gfs->y_n_gfs,
                                                                   gfs->y_nplus1_running_total_gfs,
                                                                   (float2 *)kbuf[s % 2]);
     else if (!f64)
-      rk4_update_kernel<float><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+      rk4_update_kernel<float><<<blocks, threads, 0, stream()>>>(s, dt, kc, n, gfs->y_n_gfs,
                                                                  gfs->y_nplus1_running_total_gfs,
                                                                  (float *)kbuf[s % 2]);
     else
-      rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, n, gfs->y_n_gfs,
+      rk4_update_kernel<double><<<blocks, threads, 0, stream()>>>(s, dt, StageConsts{}, n, gfs->y_n_gfs,
                                                                   gfs->y_nplus1_running_total_gfs,
                                                                   (double *)kbuf[s % 2]);
     NRGPU_LAUNCH_CHECK();

@@ -93,10 +93,10 @@ int scalarwave_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
     return dispatch<double, double, double>(p, g, stage_input<double>(a), rfm, epi);
   }
   if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out};
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
     return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), rfm, epi);
   }
-  RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out};
+  RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};
   if (a.in_is_f64) return dispatch<float, double, float>(p, g, stage_input<double>(a), rfm, epi);
   return dispatch<float, float, float>(p, g, stage_input<float>(a), rfm, epi);
 }
