@@ -275,7 +275,8 @@ int BSSN_Ricci_eval_xx(const paramstruct *params, double *xx[3], const double *i
 int BSSN_rhs_eval_xx(const paramstruct *params, double *xx[3], const double *auxevol_gfs,
                      const double *in_gfs, double *rhs_gfs);
 /* enforce_detgammabar_constraint(rfmstruct, params, in_gfs) at ALL points
- * (Enforce_Detgammabar_Constraint.py:16-75).  Arithmetic is FP64 in both. */
+ * (Enforce_Detgammabar_Constraint.py:16-75).  FP64 arithmetic on FP64 data;
+ * float-float arithmetic (~48 significant bits, FP32 pipe) on FP32 data. */
 int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const paramstruct *params,
                                         double *in_gfs);
 int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const paramstruct *params,

@@ -185,8 +185,9 @@ __global__ void bc_outer_pair_kernel(const int *__restrict__ dest, const int *__
   if (p >= npts || gf >= ngfs) return;
   float2 *f = gfs + (long long)gf * ntot;
   const long long d = dest[p], s = step[p];
-  const double a = pair_value(f[d + s]), b = pair_value(f[d + 2 * s]), c = pair_value(f[d + 3 * s]);
-  f[d] = split_pair(__dadd_rn(__dsub_rn(__dmul_rn(3.0, a), __dmul_rn(3.0, b)), c));
+  // 3 f1 - 3 f2 + f3 in float-float arithmetic (FP32 pipe; ~48 significant bits)
+  const float2 a = ff_mul(3.0f, f[d + s]), b = ff_mul(3.0f, f[d + 2 * s]);
+  f[d] = ff_add(ff_add(a, ff_neg(b)), f[d + 3 * s]);
 }
 
 __global__ void bc_inner_pair_kernel(const int *__restrict__ dest, const int *__restrict__ src,

@@ -36,8 +36,8 @@ static int check_bssn(const rfm_struct *rfm, const paramstruct *p) {
 
 // ---------------------------------------------------- det(gammabar) rescale
 // h'_ij = (|det ghat| / det gammabar)^(1/3) (delta_ij + h_ij) - delta_ij at
-// all points (Enforce_Detgammabar_Constraint.py:42-50), FP64 arithmetic for
-// either storage type.
+// all points (Enforce_Detgammabar_Constraint.py:42-50), FP64 arithmetic on
+// FP64 data (FP32 data: enforce_ff_kernel below).
 template <int CS, typename T>
 __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__restrict__ gfs) {
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
@@ -77,6 +77,53 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
       const double v = f * (d + h[i][j]) - d;
       if constexpr (std::is_same<T, float2>::value) gfs[k] = split_pair(v);
       else gfs[k] = (T)v;
+    }
+}
+
+// The same rescale for FP32 storage (pairs or plain FP32) in float-float
+// arithmetic on the FP32 pipe.  For the orthogonal reference metrics
+// (gammahat_ij = s_i^2 delta_ij, ReDD_ij = s_i s_j) det gammabar / det ghat =
+// det(I + h), so f = det(I + h)^{-1/3}: the FP32 reciprocal cube root, then
+// two Newton steps w <- w + w (1 - D w^3)/3 with the residual in float-float;
+// h'_ij = (f - 1) delta_ij + f h_ij.  About 48 significant bits.
+template <typename T>
+__global__ void enforce_ff_kernel(Grid g, T *__restrict__ gfs) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
+  if (i0 >= g.n0) return;
+  const long long idx = (long long)i0 + (long long)g.n0 * ((long long)i1 + (long long)g.n1 * i2);
+  float2 h[6];
+#pragma unroll
+  for (int s = 0; s < 6; s++) {
+    const long long k = (long long)(HDD00 + s) * g.ntot + idx;
+    if constexpr (std::is_same<T, float2>::value) h[s] = gfs[k];
+    else h[s] = make_float2(gfs[k], 0.f);
+  }
+  const float2 one = make_float2(1.f, 0.f);
+  const float2 a = ff_add(one, h[S6(0, 0)]), b = ff_add(one, h[S6(1, 1)]), c = ff_add(one, h[S6(2, 2)]);
+  const float2 h01 = h[S6(0, 1)], h02 = h[S6(0, 2)], h12 = h[S6(1, 2)];
+  float2 D = ff_mul_ff(ff_mul_ff(a, b), c);
+  const float2 t = ff_mul_ff(ff_mul_ff(h01, h02), h12);
+  D = ff_add(D, ff_add(t, t));
+  D = ff_add(D, ff_neg(ff_mul_ff(a, ff_mul_ff(h12, h12))));
+  D = ff_add(D, ff_neg(ff_mul_ff(b, ff_mul_ff(h02, h02))));
+  D = ff_add(D, ff_neg(ff_mul_ff(c, ff_mul_ff(h01, h01))));
+  float2 w = make_float2(rcbrtf(D.x), 0.f);
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const float2 r = ff_add(one, ff_neg(ff_mul_ff(D, ff_mul_ff(ff_mul_ff(w, w), w))));
+    w = ff_add(w, make_float2(__fmul_rn(w.x, r.x) * (1.0f / 3.0f), 0.f));
+  }
+  const float2 fm1 = ff_add(w, ff_neg(one));
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++) {
+      const int s = S6(i, j);
+      float2 v = ff_mul_ff(w, h[s]);
+      if (i == j) v = ff_add(fm1, v);
+      const long long k = (long long)(HDD00 + s) * g.ntot + idx;
+      if constexpr (std::is_same<T, float2>::value) gfs[k] = v;
+      else gfs[k] = v.x;
     }
 }
 
@@ -374,6 +421,12 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   NRGPU_REQUIRE(gfs != nullptr, "NULL gridfunctions");
   Grid g = make_grid(p);
   dim3 block(64), grid((g.n0 + 63) / 64, g.n1, g.n2);
+  if (!is_f64) {  // FP32 storage: float-float rescale
+    if (pair) enforce_ff_kernel<float2><<<grid, block, 0, stream()>>>(g, (float2 *)gfs);
+    else enforce_ff_kernel<float><<<grid, block, 0, stream()>>>(g, (float *)gfs);
+    NRGPU_LAUNCH_CHECK();
+    return NRGPU_OK;
+  }
   const double *tab = rfm ? rfm->table64 : nullptr;
   const bool cart = p->CoordSystem == NRGPU_COORD_CARTESIAN;
 #define ENF(T)                                                                                           \
@@ -381,8 +434,8 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   else if (p->CoordSystem == NRGPU_COORD_SPHERICAL)                                                      \
     enforce_kernel<NRGPU_COORD_SPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
   else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
-  NRGPU_REQUIRE(!(is_f64 && pair), "pair gridfunctions are FP32");
-  if (is_f64) { ENF(double) } else if (pair) { ENF(float2) } else { ENF(float) }
+  NRGPU_REQUIRE(!pair, "pair gridfunctions are FP32");
+  ENF(double)
 #undef ENF
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;

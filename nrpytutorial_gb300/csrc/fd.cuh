@@ -251,6 +251,16 @@ __device__ __forceinline__ float2 ff_mul(float k, float2 C) {
   return ff_fast_two_sum(p, __fmaf_rn(k, C.y, e));
 }
 
+// a * b, both pairs (Dekker's product with the FMA error term).
+__device__ __forceinline__ float2 ff_mul_ff(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
 // FP64 value -> (hi, lo) pair.
 __device__ __forceinline__ float2 split_pair(double v) {
   const float h = __double2float_rn(v);
