@@ -114,6 +114,7 @@ typedef struct rfm_struct {
  * the inner (parity) points.
  */
 #define NRGPU_MAX_GHOSTS 8
+#define NRGPU_MAX_BC_LEVELS 32
 typedef struct bc_struct {
   int  NGHOSTS;
   int  num_ob_gz_pts[NRGPU_MAX_GHOSTS];        /* outer points in layer g   */
@@ -126,6 +127,19 @@ typedef struct bc_struct {
   int *inner_dest;      /* device: idx3 of each inner ghost point            */
   int *inner_src;       /* device: idx3 of its interior source point         */
   int *inner_parity;    /* device: bit t set <=> parity type t is -1          */
+  /* Level schedule of the same points (built by driver_bcstruct): a point's
+   * level is 1 + the largest level among the points it reads (interior
+   * points 0) in the sequential order above; when no point is read before
+   * that order writes it, every level is applied at once with the same
+   * arithmetic, which gives the sequential result bit for bit.  nlev = 0:
+   * no schedule (the phases above are applied in order). */
+  int  nlev;
+  int  lev_start[NRGPU_MAX_BC_LEVELS + 1];     /* entries of level l: [lev_start[l], lev_start[l+1]) */
+  int  lev_inner[NRGPU_MAX_BC_LEVELS];         /* first inner (parity) entry of level l             */
+  int  lev_tail;        /* levels >= lev_tail are small: one block per gridfunction applies them all */
+  int *lev_dest;        /* device: idx3 of each entry's ghost point          */
+  int *lev_arg;         /* device: outer step, or inner source idx3          */
+  int *lev_parity;      /* device: inner parity bits (0 for outer entries)   */
 } bc_struct;
 
 /*

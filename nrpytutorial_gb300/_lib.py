@@ -13,6 +13,7 @@ COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
+MAX_BC_LEVELS = 32
 
 
 class NrgpuError(RuntimeError):
@@ -51,6 +52,8 @@ class bc_struct(C.Structure):
         ("total_outer", C.c_int), ("total_inner", C.c_int),
         ("outer_dest", C.c_void_p), ("outer_step", C.c_void_p),
         ("inner_dest", C.c_void_p), ("inner_src", C.c_void_p), ("inner_parity", C.c_void_p),
+        ("nlev", C.c_int), ("lev_start", C.c_int * (MAX_BC_LEVELS + 1)), ("lev_inner", C.c_int * MAX_BC_LEVELS),
+        ("lev_tail", C.c_int), ("lev_dest", C.c_void_p), ("lev_arg", C.c_void_p), ("lev_parity", C.c_void_p),
     ]
 
 

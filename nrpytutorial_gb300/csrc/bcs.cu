@@ -21,6 +21,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -202,6 +203,87 @@ __global__ void bc_inner_pair_kernel(const int *__restrict__ dest, const int *__
   f[dest[p]] = neg ? make_float2(-v.x, -v.y) : v;
 }
 
+// ------------------------------------------------- level-scheduled application
+// One entry of the schedule: an outer point (3 f1 - 3 f2 + f3 along its step,
+// the same arithmetic as bc_outer_kernel / bc_outer_pair_kernel) or an inner
+// point (parity copy).
+template <typename T>
+__device__ __forceinline__ void bc_entry(T *f, long long d, long long a, int bits, bool inner, int type) {
+  if (inner) {
+    const T v = f[a];
+    const bool neg = (bits >> type) & 1;
+    if constexpr (std::is_same<T, float2>::value) f[d] = neg ? make_float2(-v.x, -v.y) : v;
+    else f[d] = neg ? -v : v;
+  } else if constexpr (std::is_same<T, double>::value) {
+    f[d] = __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[d + a]), __dmul_rn(3.0, f[d + 2 * a])), f[d + 3 * a]);
+  } else if constexpr (std::is_same<T, float>::value) {
+    f[d] = __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[d + a]), __fmul_rn(3.0f, f[d + 2 * a])), f[d + 3 * a]);
+  } else {
+    const float2 x = ff_mul(3.0f, f[d + a]), y = ff_mul(3.0f, f[d + 2 * a]);
+    f[d] = ff_add(ff_add(x, ff_neg(y)), f[d + 3 * a]);
+  }
+}
+
+// One level: one thread per entry, looping over the gridfunctions (the
+// entry's indices are read once; its per-gridfunction copies are independent).
+constexpr int kBcGfChunk = 6;  // gridfunctions per thread (blockIdx.y picks the chunk)
+template <typename T>
+__global__ void bc_level_kernel(const int *__restrict__ dest, const int *__restrict__ arg,
+                                const int *__restrict__ par, int start, int inner_start, int end, int ngfs,
+                                long long ntot, ParityTypes types, T *gfs) {
+  const int p = start + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= end) return;
+  const long long d = dest[p], a = arg[p];
+  const int bits = par[p];
+  const bool inner = p >= inner_start;
+  const int g0 = blockIdx.y * kBcGfChunk, g1 = min(ngfs, g0 + kBcGfChunk);
+#pragma unroll
+  for (int k = 0; k < kBcGfChunk; k++) {
+    const int gf = g0 + k;
+    if (gf < g1) bc_entry(gfs + (long long)gf * ntot, d, a, bits, inner, types.t[gf]);
+  }
+}
+
+// The small trailing levels: one block per gridfunction, a block barrier
+// between levels.
+struct LevelTable {
+  int start[NRGPU_MAX_BC_LEVELS + 1], inner[NRGPU_MAX_BC_LEVELS];
+};
+template <typename T>
+__global__ void bc_tail_kernel(const int *__restrict__ dest, const int *__restrict__ arg,
+                               const int *__restrict__ par, LevelTable lt, int l0, int nlev, long long ntot,
+                               ParityTypes types, T *gfs) {
+  const int gf = blockIdx.x;
+  T *f = gfs + (long long)gf * ntot;
+  for (int l = l0; l < nlev; l++) {
+    for (int p = lt.start[l] + threadIdx.x; p < lt.start[l + 1]; p += blockDim.x)
+      bc_entry(f, dest[p], arg[p], par[p], p >= lt.inner[l], types.t[gf]);
+    __syncthreads();
+  }
+}
+
+template <typename T>
+static int apply_bcs_levels(const bc_struct *bc, int NUM_GFS, long long ntot, const ParityTypes &types, T *gfs) {
+  const int B = 128;
+  for (int l = 0; l < bc->lev_tail; l++) {
+    const int n = bc->lev_start[l + 1] - bc->lev_start[l];
+    if (n <= 0) continue;
+    dim3 grid((n + B - 1) / B, (NUM_GFS + kBcGfChunk - 1) / kBcGfChunk);
+    bc_level_kernel<T><<<grid, B, 0, stream()>>>(bc->lev_dest, bc->lev_arg, bc->lev_parity, bc->lev_start[l],
+                                                 bc->lev_inner[l], bc->lev_start[l + 1], NUM_GFS, ntot, types, gfs);
+    NRGPU_LAUNCH_CHECK();
+  }
+  if (bc->lev_tail < bc->nlev) {
+    LevelTable lt;
+    memcpy(lt.start, bc->lev_start, sizeof(lt.start));
+    memcpy(lt.inner, bc->lev_inner, sizeof(lt.inner));
+    bc_tail_kernel<T><<<NUM_GFS, 1024, 0, stream()>>>(bc->lev_dest, bc->lev_arg, bc->lev_parity, lt, bc->lev_tail,
+                                                     bc->nlev, ntot, types, gfs);
+    NRGPU_LAUNCH_CHECK();
+  }
+  return NRGPU_OK;
+}
+
 template <typename T>
 int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
                           const int8_t *gfs_parity, T *gfs) {
@@ -219,6 +301,7 @@ int apply_bcs_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
     types.t[g] = (int8_t)t;
   }
   const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  if (bc->nlev > 0) return apply_bcs_levels<T>(bc, NUM_GFS, ntot, types, gfs);
   const int B = 128;
   for (int g = 0; g < bc->NGHOSTS; g++) {
     for (int d = 0; d < 3; d++) {
@@ -257,6 +340,7 @@ int apply_bcs_pair_impl(const paramstruct *p, const bc_struct *bc, int NUM_GFS, 
     types.t[g] = (int8_t)t;
   }
   const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  if (bc->nlev > 0) return apply_bcs_levels<float2>(bc, NUM_GFS, ntot, types, gfs);
   const int B = 128;
   for (int g = 0; g < bc->NGHOSTS; g++) {
     for (int d = 0; d < 3; d++) {
@@ -624,13 +708,72 @@ int driver_bcstruct(const paramstruct *p, bc_struct *bc) {
   if ((st = upload(&bc->inner_dest, id_))) return st;
   if ((st = upload(&bc->inner_src, is_))) return st;
   if ((st = upload(&bc->inner_parity, ip))) return st;
+  // Level schedule.  The sequential order: per layer the outer points (by
+  // face direction), then the inner points.
+  struct Ent {
+    int d, a, par;
+    bool inner;
+  };
+  std::vector<Ent> seq;
+  seq.reserve(od.size() + id_.size());
+  for (int g = 0; g < ng; g++) {
+    for (int k = bc->ob_dir_start[g][0]; k < bc->ob_dir_start[g][3]; k++) seq.push_back({od[k], os[k], 0, false});
+    for (int k = bc->ib_start[g]; k < bc->ib_start[g] + bc->num_ib_gz_pts[g]; k++)
+      seq.push_back({id_[k], is_[k], ip[k], true});
+  }
+  std::vector<int> worder(ntot, -1), lvl(ntot, 0);
+  bool ok = true;
+  for (int k = 0; k < (int)seq.size() && ok; k++) {
+    if (worder[seq[k].d] >= 0) ok = false;  // a point written twice
+    worder[seq[k].d] = k;
+  }
+  int L = 0;
+  for (int k = 0; k < (int)seq.size() && ok; k++) {
+    const Ent &e = seq[k];
+    int lv = 0;
+    for (int j = 0; j < (e.inner ? 1 : 3); j++) {
+      const long long x = e.inner ? e.a : (long long)e.d + (long long)(j + 1) * e.a;
+      if (worder[x] > k) ok = false;  // read before the sequence writes it: keep the phases
+      else if (worder[x] >= 0) lv = std::max(lv, lvl[x]);
+    }
+    lvl[e.d] = lv + 1;
+    L = std::max(L, lv + 1);
+  }
+  if (ok && L >= 1 && L <= NRGPU_MAX_BC_LEVELS) {
+    std::vector<int> ld, la, lp;
+    std::vector<int> count(L + 1, 0);
+    for (int l = 1; l <= L; l++) {
+      bc->lev_start[l - 1] = (int)ld.size();
+      for (int inner = 0; inner < 2; inner++) {
+        if (inner) bc->lev_inner[l - 1] = (int)ld.size();
+        for (const Ent &e : seq)
+          if (lvl[e.d] == l && (int)e.inner == inner) {
+            ld.push_back(e.d);
+            la.push_back(e.a);
+            lp.push_back(e.par);
+          }
+      }
+      count[l] = (int)ld.size() - bc->lev_start[l - 1];
+    }
+    bc->lev_start[L] = (int)ld.size();
+    // the trailing levels of at most kBcTailMax points go to the per-gridfunction tail kernel
+    int tail = L;
+    while (tail > 0 && count[tail] <= 2048) tail--;
+    bc->lev_tail = tail;  // levels [tail, L) (0-based) form the tail
+    if ((st = upload(&bc->lev_dest, ld))) return st;
+    if ((st = upload(&bc->lev_arg, la))) return st;
+    if ((st = upload(&bc->lev_parity, lp))) return st;
+    bc->nlev = L;
+  }
   return NRGPU_OK;
 }
 
 int bcstruct_freemem(bc_struct *bc) {
   if (!bc) return NRGPU_OK;
-  int **ptrs[5] = {&bc->outer_dest, &bc->outer_step, &bc->inner_dest, &bc->inner_src, &bc->inner_parity};
-  for (int k = 0; k < 5; k++)
+  int **ptrs[8] = {&bc->outer_dest, &bc->outer_step, &bc->inner_dest, &bc->inner_src, &bc->inner_parity,
+                   &bc->lev_dest, &bc->lev_arg, &bc->lev_parity};
+  bc->nlev = 0;
+  for (int k = 0; k < 8; k++)
     if (*ptrs[k]) {
       cudaFree(*ptrs[k]);
       *ptrs[k] = nullptr;

@@ -80,8 +80,9 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
     }
 }
 
-// The same rescale for FP32 storage (pairs or plain FP32) in float-float
-// arithmetic on the FP32 pipe.  For the orthogonal reference metrics
+// The same rescale for FP32 storage (pairs or plain FP32), and for the FP64
+// state of the FP32-stage steps (which carry it at float-float precision),
+// in float-float arithmetic on the FP32 pipe.  For the orthogonal reference metrics
 // (gammahat_ij = s_i^2 delta_ij, ReDD_ij = s_i s_j) det gammabar / det ghat =
 // det(I + h), so f = det(I + h)^{-1/3}: the FP32 reciprocal cube root, then
 // two Newton steps w <- w + w (1 - D w^3)/3 with the residual in float-float;
@@ -96,6 +97,7 @@ __global__ void enforce_ff_kernel(Grid g, T *__restrict__ gfs) {
   for (int s = 0; s < 6; s++) {
     const long long k = (long long)(HDD00 + s) * g.ntot + idx;
     if constexpr (std::is_same<T, float2>::value) h[s] = gfs[k];
+    else if constexpr (std::is_same<T, double>::value) h[s] = split_pair_fast(gfs[k]);
     else h[s] = make_float2(gfs[k], 0.f);
   }
   const float2 one = make_float2(1.f, 0.f);
@@ -123,6 +125,7 @@ __global__ void enforce_ff_kernel(Grid g, T *__restrict__ gfs) {
       if (i == j) v = ff_add(fm1, v);
       const long long k = (long long)(HDD00 + s) * g.ntot + idx;
       if constexpr (std::is_same<T, float2>::value) gfs[k] = v;
+      else if constexpr (std::is_same<T, double>::value) gfs[k] = f2d_bits(v.x) + f2d_bits(v.y);
       else gfs[k] = v.x;
     }
 }
@@ -415,14 +418,15 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
   NRGPU_BSSN_SWITCH(RHS_CALL)
 }
 
-int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair) {
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair, bool ff_f64) {
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(gfs != nullptr, "NULL gridfunctions");
   Grid g = make_grid(p);
   dim3 block(64), grid((g.n0 + 63) / 64, g.n1, g.n2);
-  if (!is_f64) {  // FP32 storage: float-float rescale
-    if (pair) enforce_ff_kernel<float2><<<grid, block, 0, stream()>>>(g, (float2 *)gfs);
+  if (!is_f64 || ff_f64) {  // FP32 storage (or the FP32-stage steps' FP64 state): float-float rescale
+    if (is_f64) enforce_ff_kernel<double><<<grid, block, 0, stream()>>>(g, (double *)gfs);
+    else if (pair) enforce_ff_kernel<float2><<<grid, block, 0, stream()>>>(g, (float2 *)gfs);
     else enforce_ff_kernel<float><<<grid, block, 0, stream()>>>(g, (float *)gfs);
     NRGPU_LAUNCH_CHECK();
     return NRGPU_OK;

@@ -130,15 +130,16 @@ static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, co
 
 // Boundary conditions, then (BSSN) the det(gammabar) rescale, on `gfs`
 // (double, float, or float2 pairs when `pair`).
+// reduced: an FP32-stage step (its FP64 y_n is rescaled in float-float arithmetic)
 static int post_rhs(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc, void *gfs,
-                    bool is_f64, bool pair = false) {
+                    bool is_f64, bool pair = false, bool reduced = false) {
   const int ngf = system_num_gfs(system);
   int st;
   if (pair) st = apply_bcs_pair_impl(p, bc, ngf, system_parity(system), (float2 *)gfs);
   else if (is_f64) st = apply_bcs_impl<double>(p, bc, ngf, system_parity(system), (double *)gfs);
   else st = apply_bcs_impl<float>(p, bc, ngf, system_parity(system), (float *)gfs);
   if (st) return st;
-  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64, pair);
+  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64, pair, reduced && is_f64);
   return NRGPU_OK;
 }
 
@@ -220,7 +221,7 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
     if ((st = rhs_stage(system, rfm, p, a))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3))) return st;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64))) return st;
   }
   return NRGPU_OK;
 }
@@ -326,7 +327,7 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
     NRGPU_LAUNCH_CHECK();
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3))) return st;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64))) return st;
   }
   return NRGPU_OK;
 }

@@ -36,7 +36,9 @@ int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *i
                       int prec, void *auxevol);
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 // is_f64: double array; otherwise float, or float2 pairs when pair is set
-int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair = false);
+// ff_f64: FP64 data rescaled in float-float arithmetic (the FP32-stage steps' state)
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair = false,
+                        bool ff_f64 = false);
 
 // Evolved-gridfunction counts and parity types (alphabetical gf order;
 // parity types from CurviBoundaryConditions.py:122-213).
