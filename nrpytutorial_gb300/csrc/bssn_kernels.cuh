@@ -165,7 +165,10 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
   if constexpr (EXTRA) {
     if (T4) source_point<CS, R>(P, rf, T4 + idx, g.ntot, out);
   }
-#pragma unroll
+  // Not unrolled: one copy of the RK update (and of the dissipation stencil)
+  // serves the 24 gridfunctions, keeping its temporaries off the registers
+  // the RHS algebra needs.
+#pragma unroll 1
   for (int gf = 0; gf < NUM_EVOL_GFS; gf++) {
     R v = out[gf];
     if constexpr (EXTRA) {
