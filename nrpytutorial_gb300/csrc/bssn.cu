@@ -7,15 +7,19 @@
 namespace nrgpu {
 namespace bssn {
 
+NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 2)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 6)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 8)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
   switch (p->CoordSystem * 16 + p->FD_order) {                                                \
+    case NRGPU_COORD_CARTESIAN * 16 + 2: return CALL(NRGPU_COORD_CARTESIAN, 2);               \
     case NRGPU_COORD_CARTESIAN * 16 + 4: return CALL(NRGPU_COORD_CARTESIAN, 4);               \
     case NRGPU_COORD_CARTESIAN * 16 + 6: return CALL(NRGPU_COORD_CARTESIAN, 6);               \
+    case NRGPU_COORD_CARTESIAN * 16 + 8: return CALL(NRGPU_COORD_CARTESIAN, 8);               \
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SINHSPHERICAL, 4);       \
     case NRGPU_COORD_SPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SPHERICAL, 4);               \
   }                                                                                           \
@@ -489,10 +493,14 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
   InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
   const double *tab = rfm ? rfm->table64 : nullptr;
   switch (p->CoordSystem * 16 + p->FD_order) {
+    case NRGPU_COORD_CARTESIAN * 16 + 2:
+      hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 2><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6:
       hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 6><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_CARTESIAN * 16 + 8:
+      hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 8><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_SINHSPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4:
@@ -537,8 +545,10 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const 
   const double *tab = rfm ? rfm->table64 : nullptr;
 #define MOM(CS, ORD) momentum_kernel<CS, ORD><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux)
   switch (p->CoordSystem * 16 + p->FD_order) {
+    case NRGPU_COORD_CARTESIAN * 16 + 2: MOM(NRGPU_COORD_CARTESIAN, 2); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4: MOM(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6: MOM(NRGPU_COORD_CARTESIAN, 6); break;
+    case NRGPU_COORD_CARTESIAN * 16 + 8: MOM(NRGPU_COORD_CARTESIAN, 8); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MOM(NRGPU_COORD_SINHSPHERICAL, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4: MOM(NRGPU_COORD_SPHERICAL, 4); break;
     default:

@@ -43,8 +43,12 @@ CONFIGS = {
     "bssn_sph_fd4": ("BSSN", "Spherical", 4, 3),
     "bssn_cart_fd4": ("BSSN", "Cartesian", 4, 3),
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
+    "bssn_cart_fd2": ("BSSN", "Cartesian", 2, 2),
+    "bssn_cart_fd8": ("BSSN", "Cartesian", 8, 5),
     "bssn_ko_sinhsph_fd4": ("BSSN_KO", "SinhSpherical", 4, 3),
     "bssn_ko_cart_fd6": ("BSSN_KO", "Cartesian", 6, 4),
+    "bssn_ko_cart_fd2": ("BSSN_KO", "Cartesian", 2, 2),
+    "bssn_ko_cart_fd8": ("BSSN_KO", "Cartesian", 8, 5),
     "bssn_src_sinhsph_fd4": ("BSSN_SRC", "SinhSpherical", 4, 3),
     "bssn_psi4_sph_fd4": ("BSSN_PSI4", "Spherical", 4, 3),
     "sw_cart_fd4": ("ScalarWave", "Cartesian", 4, 2),

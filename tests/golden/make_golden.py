@@ -5,6 +5,7 @@ or $NRPY_REFERENCE) after `python -m oracle.gen_ref` and
 `python -m oracle.ref_build`:
 
     python tests/golden/make_golden.py
+    python tests/golden/make_golden.py ref:bssn_cart_fd8     # one fixture
 
 Writes:
   senr_bc_spherical_4x4x4.npz  the SENR curvilinear-BC golden file
@@ -60,6 +61,10 @@ FIXTURE_GRIDS = {
     "bssn_psi4_sph_fd4": ("Spherical", (8, 6, 4), 4, 3, 20),
     "bssn_src_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 21),
     "maxwell_curvi_sinhsph_fd4": ("SinhSpherical", (8, 6, 4), 4, 3, 22),
+    "bssn_cart_fd2": ("Cartesian", (6, 6, 6), 2, 2, 23),
+    "bssn_cart_fd8": ("Cartesian", (6, 6, 6), 8, 5, 24),
+    "bssn_ko_cart_fd2": ("Cartesian", (6, 6, 6), 2, 2, 25),
+    "bssn_ko_cart_fd8": ("Cartesian", (6, 6, 6), 8, 5, 26),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -75,12 +80,14 @@ def senr_bc():
     print("senr", vals.shape)
 
 
-def ref_outputs():
+def ref_outputs(only=None):
     import oracle.grid as og
     from oracle.ref import RefKernels
     from tests.helpers import bssn_random_state
     cart = {"xmin": -2.0, "xmax": 2.0, "ymin": -2.0, "ymax": 2.0, "zmin": -2.0, "zmax": 2.0}
     for cfg, (cs, N, fd, ng, seed) in FIXTURE_GRIDS.items():
+        if only and cfg not in only:
+            continue
         gp = og.GridParams(cs, N, ng, fd, **KW)
         R = RefKernels(cfg, gp, "strict", extra=dict(cart, **BL))
         g = ng
@@ -343,3 +350,6 @@ if __name__ == "__main__":
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)
+    cfgs = [w[len("ref:"):] for w in what if w.startswith("ref:")]
+    if cfgs:
+        ref_outputs(cfgs)

@@ -295,8 +295,8 @@ def test_trusted_reference_metric(cs):
 
 # ------------------------------------------------- reference-generated C
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
-CFGS = {"bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical",
-        "bssn_sph_fd4": "Spherical"}
+CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
+        "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical"}
 
 
 @pytest.mark.parametrize("cfg", sorted(CFGS))
@@ -316,7 +316,8 @@ def test_oracle_matches_reference_generated_bssn(cfg):
     assert per_gf_rel(obs.enforce_detgammabar(gp, f)[11:17], z["enforce_hDD"]) < 1e-14
 
 
-@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd6", "Cartesian")])
+@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd2", "Cartesian"),
+                                    ("bssn_ko_cart_fd6", "Cartesian"), ("bssn_ko_cart_fd8", "Cartesian")])
 def test_oracle_kreiss_oliger_matches_reference_generated_bssn(cfg, cs):
     """rhs_eval with Kreiss-Oliger dissipation on every gridfunction
     (reference-generated C of the BaikalETK construction) against the

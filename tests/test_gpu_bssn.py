@@ -15,7 +15,8 @@ FP64_TOL = 1e-12
 FP32_TOL = 5e-5
 
 CASES = [("Cartesian", (8, 8, 8), 4), ("Cartesian", (8, 6, 10), 6),
-         ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4)]
+         ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4),
+         ("Cartesian", (8, 6, 6), 2), ("Cartesian", (6, 8, 6), 8)]
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 
 

@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
-CFGS = {"bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical",
-        "bssn_sph_fd4": "Spherical"}
+CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
+        "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical"}
 TOL = 1e-12
 
 
@@ -51,7 +51,8 @@ def test_bssn_matches_reference_generated_c(cuda, cfg):
     assert per_gf_rel(t2.cpu().numpy()[11:17], z["enforce_hDD"]) < 1e-14
 
 
-@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd6", "Cartesian")])
+@pytest.mark.parametrize("cfg,cs", [("bssn_ko_sinhsph_fd4", "SinhSpherical"), ("bssn_ko_cart_fd2", "Cartesian"),
+                                    ("bssn_ko_cart_fd6", "Cartesian"), ("bssn_ko_cart_fd8", "Cartesian")])
 def test_kreiss_oliger_rhs_matches_reference_generated_c(cuda, cfg, cs):
     """rhs_eval with Kreiss-Oliger dissipation (diss_strength in the
     paramstruct) against the reference's generated C of the same RHSs, on
