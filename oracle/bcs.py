@@ -109,6 +109,24 @@ def build_bcstruct(gp):
     return layers
 
 
+def parity_type(name):
+    """Parity type of a DIM-3 gridfunction from the digits its name ends in,
+    as set_parity_types of CurviBoundaryConditions.py:122-160 assigns it:
+    no index -> 0 (scalar); one index i -> 1 + i; two indices (symmetric)
+    -> 4..9 for 00, 01, 02, 11, 12, 22."""
+    digits = ""
+    for ch in reversed(name):
+        if not ch.isdigit():
+            break
+        digits = ch + digits
+    if len(digits) == 0:
+        return 0
+    if len(digits) == 1:
+        return 1 + int(digits)
+    i, j = sorted((int(digits[-2]), int(digits[-1])))
+    return 4 + {(0, 0): 0, (0, 1): 1, (0, 2): 2, (1, 1): 3, (1, 2): 4, (2, 2): 5}[(i, j)]
+
+
 def apply_bcs(layers, gfs, parity_types):
     """In place on gfs (ngf, n2, n1, n0), sequentially as the reference does."""
     ngf = gfs.shape[0]

@@ -21,6 +21,10 @@ Writes:
       state and auxevol inputs; for bssn_psi4_*: the six pieces of psi_4;
       for bssn_src_*: rhs_eval with T^{mu nu} source terms (auxevol = 6
       RbarDD + 10 T4UU, seeded).
+  ref_bssn_bl_spherical_axisym.npz  the reference's own BSSN validation
+      run (Spherical 72x12x2 and 96x16x2, Brill-Lindquist, CFL 1, to
+      t = 7.5) through the reference's generated kernels: the 72x12x2
+      state and H of both runs at t_final (`evolve`).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -130,6 +134,56 @@ def ref_outputs(only=None):
             out["rhs"] = R.rhs_eval(f)[I]
         np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % cfg), **out)
         print(cfg, {k: getattr(v, "shape", v) for k, v in out.items()})
+
+
+# The reference's own BSSN validation run (Tutorial-Start_to_Finish-
+# BSSNCurvilinear-Two_BHs_Collide.ipynb:165-202, 739-741, 1037-1044, 1235-1251):
+# Spherical, domain_size 7.5, FD4, RK4, CFL 1.0, Brill-Lindquist m = 0.5 at
+# z = +-0.5, grids 72x12x2 and 96x16x2 evolved to t_final = domain_size.
+EVOLVE = dict(RMAX=7.5, CFL=1.0, t_final=7.5, grids=((72, 12, 2), (96, 16, 2)))
+
+
+def evolution():
+    """ref_bssn_bl_spherical_axisym.npz: the reference's generated
+    initial_data / Ricci_eval / rhs_eval / enforce_detgammabar_constraint /
+    Hamiltonian_constraint (strict FP64 build of bssn_sph_fd4) driven through
+    the RK4 step and the curvilinear BCs (oracle/bcs.py) for N_final =
+    int(t_final/dt + 0.5) steps: the interior state and H of the 72x12x2 run
+    and H of the 96x16x2 run at t_final."""
+    import oracle.bcs as ob
+    import oracle.bssn as obs
+    import oracle.grid as og
+    from oracle.ref import RefKernels
+    out = {}
+    for N in EVOLVE["grids"]:
+        gp = og.GridParams("Spherical", N, 3, 4, RMAX=EVOLVE["RMAX"], eta=2.0)
+        R = RefKernels("bssn_sph_fd4", gp, "strict", extra=dict(BL, eta=2.0))
+        layers = ob.build_bcstruct(gp)
+        par = [ob.parity_type(n) for n in obs.EVOL]
+
+        def post(f):
+            ob.apply_bcs(layers, f, par)
+            f[:] = R.enforce(f)
+
+        def rhs(f):
+            return R.rhs_eval(f, aux=R.ricci(f))
+
+        y = R.initial_data((24,) + gp.shape)
+        post(y)
+        dt = og.find_timestep(gp, EVOLVE["CFL"])
+        n_final = int(EVOLVE["t_final"] / dt + 0.5)
+        k_odd = k_even = None
+        for _ in range(n_final):
+            y, k_odd, k_even = ob.rk4_step(y, dt, rhs, post, gp.NGHOSTS, k_odd, k_even)
+        g = gp.NGHOSTS
+        tag = "%dx%dx%d" % N
+        out["n_final_" + tag] = n_final
+        out["dt_" + tag] = dt
+        out["H_" + tag] = R.hamiltonian(y)[g:-g, g:-g, g:-g]
+        if N == EVOLVE["grids"][0]:
+            out["state_" + tag] = y[:, g:-g, g:-g, g:-g]
+        print("evolved", tag, n_final, "steps, dt", dt)
+    np.savez_compressed(os.path.join(HERE, "ref_bssn_bl_spherical_axisym.npz"), **out)
 
 
 FD_WORKER = r'''
@@ -336,7 +390,7 @@ def trusted(only=None):
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted"]
+    what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted", "evolve"]
     if "senr" in what:
         senr_bc()
     if "ref" in what:
@@ -347,6 +401,8 @@ if __name__ == "__main__":
         swsh()
     if "trusted" in what:
         trusted()
+    if "evolve" in what:
+        evolution()
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)

@@ -425,3 +425,12 @@ def test_oracle_bcs_match_senr_golden_file():
     got = senr_bc_case(lambda gp, f: ob.apply_bcs(ob.build_bcstruct(gp), f, SENR_PARITY))
     assert not np.isnan(got).any()
     assert np.array_equal(got.astype(np.int64), want.astype(np.int64))
+
+
+def test_parity_types_follow_the_reference_naming_rule():
+    """Every system's gridfunction parity types (the product's table) are
+    what CurviBoundaryConditions.py:122-160 derives from the names."""
+    import oracle.bcs as ob
+    from nrpytutorial_gb300.grid import SYSTEM_GFS
+    for system, (names, par) in SYSTEM_GFS.items():
+        assert [ob.parity_type(n) for n in names] == list(par), system
