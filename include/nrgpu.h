@@ -44,10 +44,12 @@ extern "C" {
 #define NRGPU_ERR_SIZE         5  /* grid or batch larger than a fixed limit        */
 
 /* ------------------------------------------------------ coordinate systems */
-/* reference_metric.py:100-176 (Spherical, SinhSpherical), :398-428 (Cartesian) */
-#define NRGPU_COORD_CARTESIAN      0
-#define NRGPU_COORD_SPHERICAL      1
-#define NRGPU_COORD_SINHSPHERICAL  2
+/* reference_metric.py:100-176 (Spherical, SinhSpherical, SinhSphericalv2),
+   :398-428 (Cartesian) */
+#define NRGPU_COORD_CARTESIAN        0
+#define NRGPU_COORD_SPHERICAL        1
+#define NRGPU_COORD_SINHSPHERICAL    2
+#define NRGPU_COORD_SINHSPHERICALV2  3  /* r = AMPL (const_dr xx0 + sinh(xx0/SINHW)/sinh(1/SINHW)) */
 
 /* ------------------------------------------------------------- systems */
 #define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
@@ -91,6 +93,7 @@ typedef struct paramstruct {
                                          them); auxevol_gfs then holds 16 gridfunctions:
                                          RbarDD00..22, then T4UU00, 01, 02, 03, 11, 12,
                                          13, 22, 23, 33 (the stage's storage type) */
+  double const_dr;                    /* SinhSphericalv2 (reference_metric.py:141) */
 } paramstruct;
 
 /*

@@ -9,7 +9,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libnrgpu.so")
 
-COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2}
+COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 3}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
@@ -34,6 +34,7 @@ class paramstruct(C.Structure):
         ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
         ("eta", C.c_double), ("wavespeed", C.c_double), ("time", C.c_double),
         ("diss_strength", C.c_double), ("enable_stress_energy_source_terms", C.c_int),
+        ("const_dr", C.c_double),
     ]
 
 

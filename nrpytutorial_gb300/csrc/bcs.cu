@@ -464,7 +464,7 @@ static SommerfeldParams g_somm = [] {
 
 struct SommerfeldGeom {
   int cs, n[3], ng;
-  double xxmin[3], dxx[3], invdx[3], AMPL, SINHW;
+  double xxmin[3], dxx[3], invdx[3], AMPL, SINHW, const_dr;
   const double *xx[3];  // caller's coordinates, or NULL: cell-centred from xxmin/dxx
 };
 
@@ -488,9 +488,11 @@ __device__ __forceinline__ void somm_contraction(const SommerfeldGeom &G, const 
     J[0] = 1.0;
     J[1] = J[2] = 0.0;
   } else {
+    // SinhSpherical; SinhSphericalv2 adds AMPL const_dr xx0 to r
     const double sw = sinh(1.0 / G.SINHW);
-    r = G.AMPL * sinh(x0 / G.SINHW) / sw;
-    J[0] = 1.0 / (G.AMPL * cosh(x0 / G.SINHW) / (G.SINHW * sw));
+    const double lin = G.cs == NRGPU_COORD_SINHSPHERICALV2 ? G.AMPL * G.const_dr : 0.0;
+    r = G.AMPL * sinh(x0 / G.SINHW) / sw + lin * x0;
+    J[0] = 1.0 / (G.AMPL * cosh(x0 / G.SINHW) / (G.SINHW * sw) + lin);
     J[1] = J[2] = 0.0;
   }
   constexpr int NU = FD + 1;
@@ -585,6 +587,7 @@ int apply_sommerfeld_impl(const paramstruct *p, double *const xx[3], const bc_st
   G.invdx[0] = p->invdx0; G.invdx[1] = p->invdx1; G.invdx[2] = p->invdx2;
   G.AMPL = p->AMPL;
   G.SINHW = p->SINHW;
+  G.const_dr = p->const_dr;
   for (int d = 0; d < 3; d++) G.xx[d] = xx ? xx[d] : nullptr;
   const long long ntot = (long long)G.n[0] * G.n[1] * G.n[2];
   const int B = 128;

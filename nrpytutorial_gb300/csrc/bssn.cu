@@ -15,7 +15,7 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
-  switch (p->CoordSystem * 16 + p->FD_order) {                                                \
+  switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {                                   \
     case NRGPU_COORD_CARTESIAN * 16 + 2: return CALL(NRGPU_COORD_CARTESIAN, 2);               \
     case NRGPU_COORD_CARTESIAN * 16 + 4: return CALL(NRGPU_COORD_CARTESIAN, 4);               \
     case NRGPU_COORD_CARTESIAN * 16 + 6: return CALL(NRGPU_COORD_CARTESIAN, 6);               \
@@ -277,6 +277,10 @@ __global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gf
       const Dual ep = dexp((1.0 / p.SINHW) * X0), em = dexp((-1.0 / p.SINHW) * X0);
       r = (p.AMPL / den) * (ep - em);
       dr = (p.AMPL / (p.SINHW * den)) * (ep + em);
+      if (p.CoordSystem == NRGPU_COORD_SINHSPHERICALV2) {  // + AMPL const_dr xx0
+        r = r + (p.AMPL * p.const_dr) * X0;
+        dr = dr + dconst(p.AMPL * p.const_dr);
+      }
     } else {
       r = X0;
       dr = dconst(1.0);
@@ -492,7 +496,7 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
   Grid g = make_grid(p);
   InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
   const double *tab = rfm ? rfm->table64 : nullptr;
-  switch (p->CoordSystem * 16 + p->FD_order) {
+  switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {
     case NRGPU_COORD_CARTESIAN * 16 + 2:
       hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 2><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4:
@@ -517,7 +521,7 @@ int BSSN_Ricci_eval_xx(const paramstruct *p, double *xx[3], const double *in, do
   if (st) return st;
   NRGPU_REQUIRE(xx && xx[0] && xx[1] && in && aux, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
-  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
+  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW, p->const_dr, p->CoordSystem};
 #define RXX(CS, ORD) ricci_xx_launch_t<CS, ORD>(p, xa, in, aux)
   NRGPU_BSSN_SWITCH(RXX)
 #undef RXX
@@ -528,7 +532,7 @@ int BSSN_rhs_eval_xx(const paramstruct *p, double *xx[3], const double *aux, con
   if (st) return st;
   NRGPU_REQUIRE(xx && xx[0] && xx[1] && aux && in && rhs, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
-  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW};
+  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW, p->const_dr, p->CoordSystem};
 #define HXX(CS, ORD)                                                                 \
   (extras_on(p) ? rhs_xx_launch_t<CS, ORD, true>(p, xa, aux, in, rhs) \
                 : rhs_xx_launch_t<CS, ORD, false>(p, xa, aux, in, rhs))
@@ -544,7 +548,7 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const 
   InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
   const double *tab = rfm ? rfm->table64 : nullptr;
 #define MOM(CS, ORD) momentum_kernel<CS, ORD><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux)
-  switch (p->CoordSystem * 16 + p->FD_order) {
+  switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {
     case NRGPU_COORD_CARTESIAN * 16 + 2: MOM(NRGPU_COORD_CARTESIAN, 2); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4: MOM(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6: MOM(NRGPU_COORD_CARTESIAN, 6); break;

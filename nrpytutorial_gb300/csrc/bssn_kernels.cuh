@@ -193,14 +193,15 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
 // no-precompute rhs_eval(params, xx, auxevol_gfs, in_gfs, rhs_gfs) does.
 struct XXArgs {
   const double *xx0, *xx1;
-  double AMPL, SINHW;
+  double AMPL, SINHW, const_dr;
+  int cs;  // the runtime CoordSystem (SinhSphericalv2 runs on the SinhSpherical kernels)
 };
 
 template <int CS>
 __device__ __forceinline__ void hatted_at_point(const XXArgs &xa, int i0, int i1, double *q) {
   if constexpr (CS != NRGPU_COORD_CARTESIAN) {
     ScaleFactors S;
-    scale_factors(CS, xa.AMPL, xa.SINHW, xa.xx0[i0], xa.xx1[i1], &S);
+    scale_factors(xa.cs, xa.AMPL, xa.SINHW, xa.xx0[i0], xa.xx1[i1], &S, xa.const_dr);
     hatted_quantities(S, q);
   }
 }

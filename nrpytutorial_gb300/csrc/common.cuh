@@ -55,6 +55,15 @@ struct Grid {
   double invdx0, invdx1, invdx2;
 };
 
+// The kernel instantiation a coordinate system runs on.  Kernels specialise
+// on the structure of the reference metric (which scale factor depends on
+// which coordinate, RfmMask) and read its values from the rfm tables;
+// SinhSphericalv2 has SinhSpherical's structure and differs only in r(xx0),
+// which the tables and the runtime CoordSystem carry.
+inline int dispatch_cs(int cs) {
+  return cs == NRGPU_COORD_SINHSPHERICALV2 ? NRGPU_COORD_SINHSPHERICAL : cs;
+}
+
 inline Grid make_grid(const paramstruct *p) {
   Grid g;
   g.n0 = p->Nxx_plus_2NGHOSTS0;

@@ -29,7 +29,7 @@ void count_launch(int n) { g_launches += n; }
 
 int check_params(const paramstruct *p) {
   NRGPU_REQUIRE(p != nullptr, "params is NULL");
-  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 2, "unknown CoordSystem %d", p->CoordSystem);
+  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 3, "unknown CoordSystem %d", p->CoordSystem);
   NRGPU_REQUIRE(p->FD_order == 2 || p->FD_order == 4 || p->FD_order == 6 || p->FD_order == 8,
                 "FD_order %d not in {2,4,6,8}", p->FD_order);
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 && p->NGHOSTS <= NRGPU_MAX_GHOSTS,
@@ -55,7 +55,7 @@ __global__ void rfm_define_kernel(paramstruct p, double *tab64, float *tab32) {
   const double xx0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS);
   const double xx1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS);
   ScaleFactors S;
-  scale_factors(p.CoordSystem, p.AMPL, p.SINHW, xx0, xx1, &S);
+  scale_factors(p.CoordSystem, p.AMPL, p.SINHW, xx0, xx1, &S, p.const_dr);
   double out[rq::NQ];
   hatted_quantities(S, out);
   const long long plane = (long long)n0 * n1, col = (long long)i1 * n0 + i0;
@@ -121,7 +121,7 @@ int set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3], paramstr
   double xmin[3], xmax[3];
   int cs = p->CoordSystem;
   // EigenCoord of the Spherical family is Spherical (reference_metric.py:946-952).
-  if (EigenCoord && cs == NRGPU_COORD_SINHSPHERICAL) cs = NRGPU_COORD_SPHERICAL;
+  if (EigenCoord && spherical_family(cs)) cs = NRGPU_COORD_SPHERICAL;
   if (cs == NRGPU_COORD_CARTESIAN) {
     xmin[0] = p->xmin; xmax[0] = p->xmax;
     xmin[1] = p->ymin; xmax[1] = p->ymax;
@@ -158,7 +158,7 @@ double find_timestep(const paramstruct *p, double CFL_FACTOR) {
       const double xx0 = xx_of(p->xxmin0, p->dxx0, i0, ng);
       const double xx1 = xx_of(p->xxmin1, p->dxx1, i1, ng);
       ScaleFactors S;
-      scale_factors(p->CoordSystem, p->AMPL, p->SINHW, xx0, xx1, &S);
+      scale_factors(p->CoordSystem, p->AMPL, p->SINHW, xx0, xx1, &S, p->const_dr);
       const double ds0 = p->dxx0 * S.s[0], ds1 = p->dxx1 * S.s[1], ds2 = p->dxx2 * S.s[2];
       dsmin = fmin(dsmin, fmin(ds0, fmin(ds1, ds2)));
     }

@@ -165,7 +165,7 @@ __global__ void maxwell_curvi_id_kernel(paramstruct p, double amp, double lam, d
   const double xx0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS), xx1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS),
                xx2 = xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS);
   double x[3], J[3][3], Ji[3][3];
-  cart_jacobian<CS>(xx0, xx1, xx2, p.AMPL, p.SINHW, x, J);
+  cart_jacobian(p.CoordSystem, xx0, xx1, xx2, p.AMPL, p.SINHW, p.const_dr, x, J);
   inverse3(J, Ji);
   const double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
   const double u = t + r, v = t - r;
@@ -177,7 +177,7 @@ __global__ void maxwell_curvi_id_kernel(paramstruct p, double amp, double lam, d
   double s[3] = {1.0, 1.0, 1.0};
   if constexpr (CS != NRGPU_COORD_CARTESIAN) {
     ScaleFactors S;
-    scale_factors(CS, p.AMPL, p.SINHW, xx0, xx1, &S);
+    scale_factors(p.CoordSystem, p.AMPL, p.SINHW, xx0, xx1, &S, p.const_dr);
     for (int i = 0; i < 3; i++) s[i] = S.s[i];  // 1/ReU^i
   }
   for (int i = 0; i < 3; i++) {
@@ -215,7 +215,8 @@ template <typename R, typename Tin, typename TStage>
 static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::type in, const rfm_struct *rfm,
                     const RKEpilogue<TStage> &epi) {
 #define MC_CASE(CSV, ORD) \
-  if (p->CoordSystem == CSV && p->FD_order == ORD) return launch_one<R, Tin, TStage, CSV, ORD>(g, in, rfm, epi);
+  if (dispatch_cs(p->CoordSystem) == CSV && p->FD_order == ORD)                                     \
+    return launch_one<R, Tin, TStage, CSV, ORD>(g, in, rfm, epi);
   MC_CASE(NRGPU_COORD_CARTESIAN, 2) MC_CASE(NRGPU_COORD_CARTESIAN, 4)
   MC_CASE(NRGPU_COORD_SPHERICAL, 2) MC_CASE(NRGPU_COORD_SPHERICAL, 4)
   MC_CASE(NRGPU_COORD_SINHSPHERICAL, 2) MC_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
@@ -279,7 +280,7 @@ int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const paramstruct *p, 
   InteriorLaunch L = interior_launch(g, 64, 4);
   const double *tab = rfm ? rfm->table64 : nullptr;
 #define MCC(CSV, ORD) maxwell_curvi_constraint_kernel<CSV, ORD><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux)
-  switch (p->CoordSystem * 16 + p->FD_order) {
+  switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {
     case NRGPU_COORD_CARTESIAN * 16 + 2: MCC(NRGPU_COORD_CARTESIAN, 2); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4: MCC(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 2: MCC(NRGPU_COORD_SPHERICAL, 2); break;

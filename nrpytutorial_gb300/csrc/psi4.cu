@@ -40,7 +40,7 @@ __device__ __forceinline__ double omega(const double u[3], const double w[3], co
 
 template <int ORDER, int CS>
 __device__ void psi4_point(const Point<double> &P, const Rfm<CS, double> &rf, const double inv[3], double xx0,
-                           double xx1, double xx2, double AMPL, double SINHW, double &re, double &im) {
+                           double xx1, double xx2, const paramstruct &prm, double &re, double &im) {
   using M = RfmMask<CS>;
   // ---- BSSN variables and their centred derivatives; gammabar, Abar
   double g[3][3], gd[6][3], gdd[6][6], Ab[3][3], Abd[6][3];
@@ -141,7 +141,7 @@ __device__ void psi4_point(const Point<double> &P, const Rfm<CS, double> &rf, co
 
   // ---- tetrad (xx basis)
   double x[3], J[3][3], Ji[3][3];
-  cart_jacobian<CS>(xx0, xx1, xx2, AMPL, SINHW, x, J);
+  cart_jacobian(prm.CoordSystem, xx0, xx1, xx2, prm.AMPL, prm.SINHW, prm.const_dr, x, J);
   inverse3(J, Ji);
   const double v1C[3] = {-x[1], x[0], 0.0};
   double v1[3], v2[3], v3[3];
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kPsi4Threads) psi4_kernel(Grid g, const double
   const double xx1 = xx_of(p.xxmin1, p.dxx1, i1, g.ng);
   const double xx2 = xx_of(p.xxmin2, p.dxx2, i2, g.ng);
   double re, im;
-  psi4_point<ORDER, CS>(P, rf, inv, xx0, xx1, xx2, p.AMPL, p.SINHW, re, im);
+  psi4_point<ORDER, CS>(P, rf, inv, xx0, xx1, xx2, p, re, im);
   out_re[idx] = re;
   out_im[idx] = im;
 }
@@ -405,7 +405,7 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
   const double *tab = rfm ? rfm->table64 : nullptr;
   double *re = psi4_gfs, *im = psi4_gfs + g.ntot;
 #define P4(CS, ORD) psi4_kernel<CS, ORD><<<grid, block, 0, stream()>>>(g, in_gfs, tab, *p, i0_min, i0_max, re, im)
-  switch (p->CoordSystem * 16 + p->FD_order) {
+  switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {
     case NRGPU_COORD_CARTESIAN * 16 + 4: P4(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6: P4(NRGPU_COORD_CARTESIAN, 6); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: P4(NRGPU_COORD_SINHSPHERICAL, 4); break;

@@ -1,5 +1,6 @@
 // rfm.cuh -- reference metric ("hatted" quantities) for orthogonal,
-// diagonal coordinate systems: Cartesian, Spherical, SinhSpherical.
+// diagonal coordinate systems: Cartesian, Spherical, SinhSpherical,
+// SinhSphericalv2.
 //
 // reference_metric.py:487-601 derives, from the orthogonal scale factors
 // s_i(xx) (ghat_ii = s_i^2, ReU_i = 1/s_i, ReDD_ij = s_i s_j), the first and
@@ -140,20 +141,31 @@ __device__ __forceinline__ Rfm<CS, R> rfm_at(const R *tab, int n0, int n1, int i
 // --------------------------------------------------- scale-factor closed forms
 // s[i], ds[i][k] = d s_i / d xx_k, dds[i][k][l], at uniform coordinates
 // (xx0, xx1).  Spherical: r = xx0; SinhSpherical: r = AMPL sinh(xx0/SINHW) /
-// sinh(1/SINHW), written with exponentials as reference_metric.py:125-126 does.
+// sinh(1/SINHW), written with exponentials as reference_metric.py:125-126 does;
+// SinhSphericalv2 adds AMPL const_dr xx0 (reference_metric.py:142-143).
+// Every system of the family has the Spherical angles and the Spherical
+// eigen-coordinates, so only r(xx0) and its derivatives differ.
 struct ScaleFactors {
   double s[3], ds[3][3], dds[3][3][3];
 };
 
+__host__ __device__ inline bool spherical_family(int cs) {
+  return cs == NRGPU_COORD_SPHERICAL || cs == NRGPU_COORD_SINHSPHERICAL || cs == NRGPU_COORD_SINHSPHERICALV2;
+}
+
+// r(x) and its first three derivatives.
 __host__ __device__ inline void radial_map(int cs, double AMPL, double SINHW, double x,
-                                           double *r, double *r1, double *r2, double *r3) {
-  if (cs == NRGPU_COORD_SINHSPHERICAL) {
+                                           double *r, double *r1, double *r2, double *r3,
+                                           double const_dr = 0.0) {
+  if (cs == NRGPU_COORD_SINHSPHERICAL || cs == NRGPU_COORD_SINHSPHERICALV2) {
     const double ep = exp(x / SINHW), em = exp(-x / SINHW);
     const double den = exp(1.0 / SINHW) - exp(-1.0 / SINHW);
-    *r = AMPL * (ep - em) / den;
-    *r1 = AMPL * (ep + em) / (SINHW * den);
-    *r2 = *r / (SINHW * SINHW);
-    *r3 = *r1 / (SINHW * SINHW);
+    const double sh = AMPL * (ep - em) / den, ch = AMPL * (ep + em) / (SINHW * den);
+    const double lin = cs == NRGPU_COORD_SINHSPHERICALV2 ? AMPL * const_dr : 0.0;
+    *r = sh + lin * x;
+    *r1 = ch + lin;
+    *r2 = sh / (SINHW * SINHW);
+    *r3 = ch / (SINHW * SINHW);
   } else {
     *r = x;
     *r1 = 1.0;
@@ -163,7 +175,7 @@ __host__ __device__ inline void radial_map(int cs, double AMPL, double SINHW, do
 }
 
 __host__ __device__ inline void scale_factors(int cs, double AMPL, double SINHW, double xx0,
-                                              double xx1, ScaleFactors *S) {
+                                              double xx1, ScaleFactors *S, double const_dr = 0.0) {
   for (int i = 0; i < 3; i++) {
     S->s[i] = 1.0;
     for (int k = 0; k < 3; k++) {
@@ -173,7 +185,7 @@ __host__ __device__ inline void scale_factors(int cs, double AMPL, double SINHW,
   }
   if (cs == NRGPU_COORD_CARTESIAN) return;
   double r, r1, r2, r3;
-  radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
+  radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3, const_dr);
   const double sn = sin(xx1), cs1 = cos(xx1);
   S->s[0] = r1;
   S->s[1] = r;
@@ -254,10 +266,9 @@ __host__ __device__ inline void hatted_quantities(const ScaleFactors &S, double 
 }
 
 // xx -> Cartesian and d x_Cart^i / d xx^j (reference_metric.py xx_to_Cart).
-template <int CS>
-__host__ __device__ inline void cart_jacobian(double xx0, double xx1, double xx2, double AMPL, double SINHW,
-                                              double x[3], double J[3][3]) {
-  if constexpr (CS == NRGPU_COORD_CARTESIAN) {
+__host__ __device__ inline void cart_jacobian(int cs, double xx0, double xx1, double xx2, double AMPL,
+                                              double SINHW, double const_dr, double x[3], double J[3][3]) {
+  if (cs == NRGPU_COORD_CARTESIAN) {
     x[0] = xx0;
     x[1] = xx1;
     x[2] = xx2;
@@ -267,7 +278,7 @@ __host__ __device__ inline void cart_jacobian(double xx0, double xx1, double xx2
       for (int j = 0; j < 3; j++) J[i][j] = i == j ? 1.0 : 0.0;
   } else {
     double r, r1, r2, r3;
-    radial_map(CS, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
+    radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3, const_dr);
     const double st = sin(xx1), ct = cos(xx1), sp = sin(xx2), cp = cos(xx2);
     x[0] = r * st * cp;
     x[1] = r * st * sp;

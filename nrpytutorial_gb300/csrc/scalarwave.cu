@@ -74,7 +74,8 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
                     const RKEpilogue<TStage> &epi) {
   const double c2 = p->wavespeed * p->wavespeed;
 #define SW_CASE(CSV, ORD) \
-  if (p->CoordSystem == CSV && p->FD_order == ORD) return launch_one<R, Tin, TStage, CSV, ORD>(g, in, rfm, c2, epi);
+  if (dispatch_cs(p->CoordSystem) == CSV && p->FD_order == ORD)                                             \
+    return launch_one<R, Tin, TStage, CSV, ORD>(g, in, rfm, c2, epi);
   SW_CASE(NRGPU_COORD_CARTESIAN, 2) SW_CASE(NRGPU_COORD_CARTESIAN, 4)
   SW_CASE(NRGPU_COORD_CARTESIAN, 6) SW_CASE(NRGPU_COORD_CARTESIAN, 8)
   SW_CASE(NRGPU_COORD_SPHERICAL, 2) SW_CASE(NRGPU_COORD_SPHERICAL, 4)
@@ -122,7 +123,7 @@ __global__ void sw_initial_data_kernel(paramstruct p, int kind, double t, double
     z = x2;
   } else {
     double r, r1, r2, r3;
-    radial_map(p.CoordSystem, p.AMPL, p.SINHW, x0, &r, &r1, &r2, &r3);
+    radial_map(p.CoordSystem, p.AMPL, p.SINHW, x0, &r, &r1, &r2, &r3, p.const_dr);
     x = r * sin(x1) * cos(x2);
     y = r * sin(x1) * sin(x2);
     z = r * cos(x1);

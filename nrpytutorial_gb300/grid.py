@@ -41,13 +41,14 @@ class Grid:
 
     def __init__(self, CoordSystem, Nxx, FD_order=4, NGHOSTS=2, *, AMPL=10.0, SINHW=0.2,
                  RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, diss_strength=0.0,
-                 stress_energy_source_terms=False):
+                 stress_energy_source_terms=False, const_dr=0.0625):
         lib = _lib.load()
         p = _lib.paramstruct()
         p.CoordSystem = _lib.COORD[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
         p.FD_order = FD_order
         p.NGHOSTS = NGHOSTS
         p.AMPL, p.SINHW, p.RMAX = AMPL, SINHW, RMAX
+        p.const_dr = const_dr  # SinhSphericalv2's constant-spacing term (reference default 0.0625)
         lo, hi = domain
         p.xmin = p.ymin = p.zmin = lo
         p.xmax = p.ymax = p.zmax = hi

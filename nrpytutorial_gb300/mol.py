@@ -274,6 +274,8 @@ class Evolution:
         x0 = float(self.grid.xx[0][i0])
         p = self.grid.params
         r = x0 if p.CoordSystem == 1 else p.AMPL * np.sinh(x0 / p.SINHW) / np.sinh(1.0 / p.SINHW)
+        if p.CoordSystem == 3:  # SinhSphericalv2 (reference_metric.py:142-143)
+            r += p.AMPL * p.const_dr * x0
         return out, r
 
     def maxwell_curvilinear_constraints(self, gfs=None):

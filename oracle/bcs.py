@@ -19,7 +19,7 @@ then the post-RHS calls (BCs, then the det(gammabar) rescale for BSSN).
 """
 import numpy as np
 
-from .grid import CART, GridParams
+from .grid import CART, GridParams, radial
 
 
 def build_bcstruct(gp):
@@ -199,10 +199,8 @@ def _radial_geometry(gp, i0, i1, i2):
         return r, (x0 / r, x1 / r, x2 / r)
     if gp.CoordSystem == 1:  # Spherical: xx0 = r
         return x0, (1.0, 0.0, 0.0)
-    w, A = gp.SINHW, gp.AMPL
-    r = A * np.sinh(x0 / w) / np.sinh(1.0 / w)
-    drdx = A * np.cosh(x0 / w) / (w * np.sinh(1.0 / w))
-    return r, (1.0 / drdx, 0.0, 0.0)
+    r, drdx = radial(gp.CoordSystem, x0, gp.AMPL, gp.SINHW, gp.const_dr)
+    return r, (1.0 / float(drdx), 0.0, 0.0)
 
 
 def _sommerfeld_dr(gp, f, idx3, face, fd_order):

@@ -41,6 +41,7 @@ OUT = os.path.join(HERE, "_ref", "src")
 CONFIGS = {
     "bssn_sinhsph_fd4": ("BSSN", "SinhSpherical", 4, 3),
     "bssn_sph_fd4": ("BSSN", "Spherical", 4, 3),
+    "bssn_sinhv2_fd4": ("BSSN", "SinhSphericalv2", 4, 3),
     "bssn_cart_fd4": ("BSSN", "Cartesian", 4, 3),
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
     "bssn_cart_fd2": ("BSSN", "Cartesian", 2, 2),

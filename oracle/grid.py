@@ -4,11 +4,12 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 
 - `GridParams` restates reference_metric.py:1330-1395
   (set_Nxx_dxx_invdx_params__and__xx): domain per CoordSystem
-  (Spherical :106-108, SinhSpherical :118-120, Cartesian :400-403),
+  (Spherical :106-108, SinhSpherical :118-120, SinhSphericalv2 :137-138,
+  Cartesian :400-403),
   dxx = (xxmax - xxmin)/Nxx, cell-centred xx[j] = xxmin + (j - NGHOSTS + 1/2) dxx.
 - `hatted` restates reference_metric.py:487-601: for orthogonal scale factors
   s_i (reference_metric.py:168-175: s0 = dr/dxx0, s1 = r, s2 = r sin(xx1);
-  Cartesian s_i = 1) it returns ReU, ReDD, ghat and their first and second
+  r(xx0) of :111, :125-126 and :142-143; Cartesian s_i = 1) it returns ReU, ReDD, ghat and their first and second
   derivatives, GammahatUDD and its derivatives, det(ghat) and derivatives.
   Where the reference differentiates symbolically, here the derivatives of
   s_i are written in closed form and propagated by the product/quotient
@@ -17,22 +18,42 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 """
 import numpy as np
 
-CART, SPH, SINHSPH = 0, 1, 2
-NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH}
+CART, SPH, SINHSPH, SINHSPHV2 = 0, 1, 2, 3
+NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH, "SinhSphericalv2": SINHSPHV2}
+
+
+def radial(cs, x0, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
+    """r(xx0) and dr/dxx0 of the Spherical family: Spherical r = xx0
+    (reference_metric.py:111); SinhSpherical r = AMPL sinh(xx0/SINHW) /
+    sinh(1/SINHW) (:125-126); SinhSphericalv2 adds AMPL const_dr xx0
+    (:142-143)."""
+    x0 = np.asarray(x0, dtype=float)
+    if cs == SPH:
+        return x0, np.ones_like(x0)
+    den = np.exp(1.0 / SINHW) - np.exp(-1.0 / SINHW)
+    r = AMPL * (np.exp(x0 / SINHW) - np.exp(-x0 / SINHW)) / den
+    drdx = AMPL * (np.exp(x0 / SINHW) + np.exp(-x0 / SINHW)) / (SINHW * den)
+    if cs == SINHSPHV2:
+        r = r + AMPL * const_dr * x0
+        drdx = drdx + AMPL * const_dr
+    elif cs != SINHSPH:
+        raise ValueError(cs)
+    return r, drdx
 
 
 class GridParams:
     def __init__(self, CoordSystem, Nxx, NGHOSTS, FD_order=4, AMPL=10.0, SINHW=0.2, RMAX=10.0,
-                 domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0):
+                 domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, const_dr=0.0625):
         cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
         self.CoordSystem = cs
         self.FD_order = FD_order
         self.NGHOSTS = NGHOSTS
         self.AMPL, self.SINHW, self.RMAX = AMPL, SINHW, RMAX
+        self.const_dr = const_dr
         self.eta, self.wavespeed = eta, wavespeed
         self.Nxx = [int(n) for n in Nxx]
         self.np = [n + 2 * NGHOSTS for n in self.Nxx]
-        ecs = SPH if (EigenCoord and cs == SINHSPH) else cs
+        ecs = SPH if (EigenCoord and cs in (SINHSPH, SINHSPHV2)) else cs
         if ecs == CART:
             lo, hi = domain
             self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
@@ -62,13 +83,16 @@ def scale_factors(gp, xx0, xx1):
     dds = [[[z.copy() for _ in range(3)] for _ in range(3)] for _ in range(3)]
     if gp.CoordSystem == CART:
         return s, ds, dds
-    if gp.CoordSystem == SINHSPH:
+    if gp.CoordSystem in (SINHSPH, SINHSPHV2):
         A, w = gp.AMPL, gp.SINHW
         den = np.exp(1.0 / w) - np.exp(-1.0 / w)
-        r = A * (np.exp(x0 / w) - np.exp(-x0 / w)) / den
-        r1 = A * (np.exp(x0 / w) + np.exp(-x0 / w)) / (w * den)
-        r2 = r / w ** 2
-        r3 = r1 / w ** 2
+        sh = A * (np.exp(x0 / w) - np.exp(-x0 / w)) / den
+        ch = A * (np.exp(x0 / w) + np.exp(-x0 / w)) / (w * den)
+        lin = A * gp.const_dr if gp.CoordSystem == SINHSPHV2 else 0.0
+        r = sh + lin * x0
+        r1 = ch + lin
+        r2 = sh / w ** 2
+        r3 = ch / w ** 2
     else:
         r, r1, r2, r3 = x0, one, z, z
     st, ct = np.sin(x1), np.cos(x1)
@@ -91,14 +115,14 @@ def hatted(gp):
 
 
 class _PointParams:
-    def __init__(self, cs, AMPL, SINHW):
-        self.CoordSystem, self.AMPL, self.SINHW = cs, AMPL, SINHW
+    def __init__(self, cs, AMPL, SINHW, const_dr):
+        self.CoordSystem, self.AMPL, self.SINHW, self.const_dr = cs, AMPL, SINHW, const_dr
 
 
-def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2):
+def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
     """Hatted quantities at one point (xx0, xx1): arrays with point shape (1, 1)."""
     cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else CoordSystem
-    return hatted_from_scale_factors(*scale_factors(_PointParams(cs, AMPL, SINHW),
+    return hatted_from_scale_factors(*scale_factors(_PointParams(cs, AMPL, SINHW, const_dr),
                                                     np.array([xx0]), np.array([xx1])))
 
 

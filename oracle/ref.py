@@ -34,7 +34,8 @@ class RefKernels:
                 "Nxx_plus_2NGHOSTS0": gp.np[0], "Nxx_plus_2NGHOSTS1": gp.np[1], "Nxx_plus_2NGHOSTS2": gp.np[2],
                 "dxx0": gp.dxx[0], "dxx1": gp.dxx[1], "dxx2": gp.dxx[2],
                 "invdx0": gp.invdx[0], "invdx1": gp.invdx[1], "invdx2": gp.invdx[2],
-                "AMPL": gp.AMPL, "SINHW": gp.SINHW, "RMAX": gp.RMAX, "eta": gp.eta, "wavespeed": gp.wavespeed}
+                "AMPL": gp.AMPL, "SINHW": gp.SINHW, "RMAX": gp.RMAX, "eta": gp.eta, "wavespeed": gp.wavespeed,
+                "const_dr": getattr(gp, "const_dr", 0.0625)}
         vals.update(extra or {})
         for k, v in vals.items():
             self.lib.ref_set(k.encode(), float(v))

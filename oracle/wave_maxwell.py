@@ -10,7 +10,7 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 import numpy as np
 
 from .fd import Stencils
-from .grid import CART, hatted
+from .grid import CART, hatted, radial
 
 
 def scalarwave_rhs_grid(gp, gfs):
@@ -150,7 +150,7 @@ def scalarwave_id_grid(gp, kind, t=0.0, k=(1.0, 1.0, 1.0), sigma=3.0):
     if gp.CoordSystem == 0:
         x, y, z = X0, X1, X2
     else:
-        r = X0 if gp.CoordSystem == 1 else gp.AMPL * np.sinh(X0 / gp.SINHW) / np.sinh(1.0 / gp.SINHW)
+        r, _ = radial(gp.CoordSystem, X0, gp.AMPL, gp.SINHW, gp.const_dr)
         x, y, z = r * np.sin(X1) * np.cos(X2), r * np.sin(X1) * np.sin(X2), r * np.cos(X1)
     uu, vv = scalarwave_id_pointwise(kind, x, y, z, t, gp.wavespeed, k, sigma)
     return np.stack([uu, vv])
@@ -255,7 +255,7 @@ def maxwell_curvi_toroidal_dipole(gp, t, amp=1.0, lam=1.0):
     xx_to_Cart and divided by ReU."""
     from .psi4 import _inv_general, cart_and_jacobian
     X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
-    xyz, J = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW)
+    xyz, J = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW, gp.const_dr)
     x, y, z = xyz
     r = np.sqrt(x * x + y * y + z * z)
     u, vv = t + r, t - r

@@ -279,10 +279,11 @@ def test_trusted_maxwell_system_I():
     assert close(float(C[0]), ex["C"], 1e-13)
 
 
-@pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "Cartesian"])
+@pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cartesian"])
 def test_trusted_reference_metric(cs):
     inp = TV["rfm_" + cs]["inputs"]
-    q = og.hatted_at(cs, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("AMPL", 10.0), inp.get("SINHW", 0.2))
+    q = og.hatted_at(cs, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("AMPL", 10.0), inp.get("SINHW", 0.2),
+                     inp.get("const_dr", 0.0625))
     n = 0
     for k, want in expect("rfm_" + cs).items():
         base, _, rest = k.partition("[")
@@ -296,7 +297,8 @@ def test_trusted_reference_metric(cs):
 # ------------------------------------------------- reference-generated C
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
-        "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical"}
+        "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical",
+        "bssn_sinhv2_fd4": "SinhSphericalv2"}
 
 
 @pytest.mark.parametrize("cfg", sorted(CFGS))

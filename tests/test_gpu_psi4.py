@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CASES = [("Cartesian", (8, 6, 10), 4), ("Cartesian", (8, 8, 6), 6),
-         ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4)]
+         ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4), ("SinhSphericalv2", (10, 8, 8), 4)]
 
 
 def _evo(cuda, coord, Nxx, order, **kw):
@@ -64,7 +64,7 @@ def test_psi4_shell_range_writes_only_that_shell(cuda):
         ev.psi4(t, (0, 1))  # ghost shell
 
 
-@pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical"])
+@pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical", "SinhSphericalv2"])
 def test_psi4_modes_match_oracle(cuda, coord):
     import torch
     ev, gp = _evo(cuda, coord, (8, 12, 16), 4)
@@ -78,7 +78,7 @@ def test_psi4_modes_match_oracle(cuda, coord):
     for k, (a, b) in ref.items():
         assert abs(modes[k] - complex(a, b)) <= 1e-12 * scale, (k, modes[k], (a, b))
     x0 = gp.xx[0][i0]
-    want_r = x0 if coord == "Spherical" else gp.AMPL * np.sinh(x0 / gp.SINHW) / np.sinh(1 / gp.SINHW)
+    want_r = float(og.radial(gp.CoordSystem, x0, gp.AMPL, gp.SINHW, gp.const_dr)[0])
     assert r == pytest.approx(want_r, rel=1e-14)
 
 

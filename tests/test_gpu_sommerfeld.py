@@ -25,6 +25,7 @@ def _set(fd, ngf, falloff=3.0):
     ("Maxwell", "Cartesian", (10, 8, 12), 4, 2),
     ("ScalarWave", "Spherical", (10, 8, 6), 4, 2),
     ("ScalarWave", "SinhSpherical", (10, 8, 6), 4, 4),
+    ("ScalarWave", "SinhSphericalv2", (10, 8, 6), 4, 4),
 ])
 def test_sommerfeld_rhs_matches_oracle(cuda, system, coord, Nxx, order, fd):
     import torch
