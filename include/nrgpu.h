@@ -50,6 +50,11 @@ extern "C" {
 #define NRGPU_COORD_SPHERICAL        1
 #define NRGPU_COORD_SINHSPHERICAL    2
 #define NRGPU_COORD_SINHSPHERICALV2  3  /* r = AMPL (const_dr xx0 + sinh(xx0/SINHW)/sinh(1/SINHW)) */
+/* reference_metric.py:226-300: (rho, phi, z); the reference metric depends on
+   xx0 and xx2, so its tables are per (i0, i2) column */
+#define NRGPU_COORD_CYLINDRICAL      4  /* rho = xx0, z = xx2                                 */
+#define NRGPU_COORD_SINHCYLINDRICAL  5  /* rho = AMPLRHO sinh(xx0/SINHWRHO)/sinh(1/SINHWRHO),
+                                           z = AMPLZ sinh(xx2/SINHWZ)/sinh(1/SINHWZ)       */
 
 /* ------------------------------------------------------------- systems */
 #define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
@@ -94,17 +99,22 @@ typedef struct paramstruct {
                                          RbarDD00..22, then T4UU00, 01, 02, 03, 11, 12,
                                          13, 22, 23, 33 (the stage's storage type) */
   double const_dr;                    /* SinhSphericalv2 (reference_metric.py:141) */
+  double RHOMAX, ZMIN, ZMAX;          /* Cylindrical (reference_metric.py:233)     */
+  double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  /* SinhCylindrical (:249-251)          */
 } paramstruct;
 
 /*
  * rfm_struct: FP64 reference-metric precompute tables (the rfm_precompute
  * arrays of reference_metric.py:603-886, here as dense derived quantities per
- * (i0,i1) column), plus an FP32 copy for the mixed-precision kernels.
+ * (i0,iB) column, iB = i1 for the Spherical family and i2 for the Cylindrical
+ * family), plus an FP32 copy for the mixed-precision kernels.
  */
 typedef struct rfm_struct {
   int     CoordSystem;
-  int     N0, N1;            /* table extents = Nxx_plus_2NGHOSTS0, 1          */
-  int     nquant;            /* doubles per (i0,i1)                            */
+  int     N0, N1;            /* table extents = Nxx_plus_2NGHOSTS0 and that of
+                                the second coordinate (Nxx_plus_2NGHOSTS1, or
+                                Nxx_plus_2NGHOSTS2 for the Cylindrical family) */
+  int     nquant;            /* doubles per (i0,iB)                            */
   double *table64;           /* device, [nquant][N1][N0]                       */
   float  *table32;           /* device, same layout                            */
 } rfm_struct;

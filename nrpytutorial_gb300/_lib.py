@@ -9,7 +9,8 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libnrgpu.so")
 
-COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 3}
+COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 3, "Cylindrical": 4,
+         "SinhCylindrical": 5}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
@@ -35,6 +36,8 @@ class paramstruct(C.Structure):
         ("eta", C.c_double), ("wavespeed", C.c_double), ("time", C.c_double),
         ("diss_strength", C.c_double), ("enable_stress_energy_source_terms", C.c_int),
         ("const_dr", C.c_double),
+        ("RHOMAX", C.c_double), ("ZMIN", C.c_double), ("ZMAX", C.c_double),
+        ("AMPLRHO", C.c_double), ("SINHWRHO", C.c_double), ("AMPLZ", C.c_double), ("SINHWZ", C.c_double),
     ]
 
 

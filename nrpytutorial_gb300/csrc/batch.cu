@@ -104,7 +104,9 @@ __global__ void sw_batch_table_kernel(const BatchInstance *__restrict__ insts, i
     const double xx0 = xx_of(xxmin0, I.dxx0, i0, kBatchNG);
     const double xx1 = xx_of(xxmin1, I.dxx1, i1, kBatchNG);
     ScaleFactors S;
-    scale_factors(cs, AMPL, SINHW, xx0, xx1, &S);
+    CoordParams cp{};
+    cp.cs = cs, cp.AMPL = AMPL, cp.SINHW = SINHW;
+    scale_factors(cp, xx0, xx1, 0.0, &S);
     double q[rq::NQ];
     hatted_quantities(S, q);
     double v[kBatchTab];
@@ -132,9 +134,11 @@ __global__ void sw_batch_gaussian_kernel(const BatchInstance *__restrict__ insts
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < I.ntot; c += gridDim.x * (long long)blockDim.x) {
     const int i0 = (int)(c % I.n0);
     const double xx0 = xx_of(xxmin0, I.dxx0, i0, kBatchNG);
-    double r, r1, r2, r3;
-    radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3);
-    const double x = (r - r0[inst]) / w[inst];
+    CoordParams cp{};
+    cp.cs = cs, cp.AMPL = AMPL, cp.SINHW = SINHW;
+    double r[4];
+    radial_map(cp, xx0, r);
+    const double x = (r[0] - r0[inst]) / w[inst];
     y[I.base + c] = A[inst] * exp(-x * x);
     y[I.base + I.ntot + c] = 0.0;
   }

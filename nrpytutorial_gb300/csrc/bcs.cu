@@ -35,6 +35,12 @@ static void eigen_xx_to_cart(int cs, double x0, double x1, double x2, double out
     out[0] = x0; out[1] = x1; out[2] = x2;
     return;
   }
+  if (cs == NRGPU_COORD_CYLINDRICAL) {  // reference_metric.py:296-298
+    out[0] = x0 * cos(x1);
+    out[1] = x0 * sin(x1);
+    out[2] = x2;
+    return;
+  }
   // Spherical eigen-coordinates (reference_metric.py:163-166)
   out[0] = x0 * sin(x1) * cos(x2);
   out[1] = x0 * sin(x1) * sin(x2);
@@ -46,6 +52,12 @@ static void eigen_cart_to_xx(int cs, const double c[3], double out[3]) {
     out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
     return;
   }
+  if (cs == NRGPU_COORD_CYLINDRICAL) {  // reference_metric.py:240-242
+    out[0] = sqrt(c[0] * c[0] + c[1] * c[1]);
+    out[1] = atan2(c[1], c[0]);
+    out[2] = c[2];
+    return;
+  }
   // reference_metric.py:113-115
   const double r = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
   out[0] = r;
@@ -54,11 +66,19 @@ static void eigen_cart_to_xx(int cs, const double c[3], double out[3]) {
 }
 
 // Unit vectors (rows) of the eigen-coordinate basis at (x0,x1,x2)
-// (reference_metric.py:180-182 for the Spherical family; identity otherwise).
+// (reference_metric.py:180-182 for the Spherical family, :300-302 for the
+// Cylindrical family with phi = x1; identity otherwise).
 static void unit_vectors(int cs, double x1, double x2, double U[3][3]) {
   if (cs == NRGPU_COORD_CARTESIAN) {
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) U[i][j] = (i == j) ? 1.0 : 0.0;
+    return;
+  }
+  if (cs == NRGPU_COORD_CYLINDRICAL) {
+    const double sp = sin(x1), cp = cos(x1);
+    U[0][0] = cp;  U[0][1] = sp;  U[0][2] = 0.0;
+    U[1][0] = -sp; U[1][1] = cp;  U[1][2] = 0.0;
+    U[2][0] = 0.0; U[2][1] = 0.0; U[2][2] = 1.0;
     return;
   }
   const double st = sin(x1), ct = cos(x1), sp = sin(x2), cp = cos(x2);
@@ -83,9 +103,17 @@ static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
     xs[d].resize(np[d]);
     xxp[d] = xs[d].data();
   }
+  // The map is invariant under the eigen grid's radial / z extent; a
+  // zero-initialised extent parameter (not read by this CoordSystem itself)
+  // gets a unit extent instead of a degenerate grid.
+  if (!(e.RMAX > 0.0)) e.RMAX = 1.0;
+  if (!(e.RHOMAX > 0.0)) e.RHOMAX = 1.0;
+  if (!(e.ZMAX > e.ZMIN)) e.ZMIN = -1.0, e.ZMAX = 1.0;
   int st = set_Nxx_dxx_invdx_params__and__xx(1, Nxx, &e, xxp);
   if (st) return st;
-  const int cs = (p->CoordSystem == NRGPU_COORD_CARTESIAN) ? NRGPU_COORD_CARTESIAN : NRGPU_COORD_SPHERICAL;
+  const int cs = p->CoordSystem == NRGPU_COORD_CARTESIAN     ? NRGPU_COORD_CARTESIAN
+                 : cylindrical_family(p->CoordSystem) ? NRGPU_COORD_CYLINDRICAL
+                                                      : NRGPU_COORD_SPHERICAL;
   const int ng = p->NGHOSTS;
   const double dxx[3] = {e.dxx0, e.dxx1, e.dxx2};
   // set_up__bc_gz_map_and_parity_condns.h:17-19 recovers xxmin from xx[d][0].
@@ -465,6 +493,7 @@ static SommerfeldParams g_somm = [] {
 struct SommerfeldGeom {
   int cs, n[3], ng;
   double xxmin[3], dxx[3], invdx[3], AMPL, SINHW, const_dr;
+  CoordParams c;
   const double *xx[3];  // caller's coordinates, or NULL: cell-centred from xxmin/dxx
 };
 
@@ -487,6 +516,14 @@ __device__ __forceinline__ void somm_contraction(const SommerfeldGeom &G, const 
     r = x0;
     J[0] = 1.0;
     J[1] = J[2] = 0.0;
+  } else if (cylindrical_family(G.cs)) {
+    // r = sqrt(rho^2 + z^2); dxx0/dr = (rho/r) / (drho/dxx0), dxx2/dr = (z/r) / (dz/dxx2)
+    double rho[4], z[4];
+    cylinder_maps(G.c, x0, somm_xx(G, 2, idx3[2]), rho, z);
+    r = sqrt(rho[0] * rho[0] + z[0] * z[0]);
+    J[0] = rho[0] / r / rho[1];
+    J[1] = 0.0;
+    J[2] = z[0] / r / z[1];
   } else {
     // SinhSpherical; SinhSphericalv2 adds AMPL const_dr xx0 to r
     const double sw = sinh(1.0 / G.SINHW);
@@ -588,6 +625,7 @@ int apply_sommerfeld_impl(const paramstruct *p, double *const xx[3], const bc_st
   G.AMPL = p->AMPL;
   G.SINHW = p->SINHW;
   G.const_dr = p->const_dr;
+  G.c = coord_params(*p);
   for (int d = 0; d < 3; d++) G.xx[d] = xx ? xx[d] : nullptr;
   const long long ntot = (long long)G.n[0] * G.n[1] * G.n[2];
   const int B = 128;

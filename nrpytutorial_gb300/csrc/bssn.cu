@@ -12,6 +12,7 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 6)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 8)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHCYLINDRICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
@@ -21,6 +22,7 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
     case NRGPU_COORD_CARTESIAN * 16 + 6: return CALL(NRGPU_COORD_CARTESIAN, 6);               \
     case NRGPU_COORD_CARTESIAN * 16 + 8: return CALL(NRGPU_COORD_CARTESIAN, 8);               \
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SINHSPHERICAL, 4);       \
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: return CALL(NRGPU_COORD_SINHCYLINDRICAL, 4);   \
     case NRGPU_COORD_SPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SPHERICAL, 4);               \
   }                                                                                           \
   set_error("BSSN: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order); \
@@ -32,8 +34,7 @@ static int check_bssn(const rfm_struct *rfm, const paramstruct *p) {
   // The upwinded stencils reach FD_order/2 + 1 points (NGHOSTS rule of
   // Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:835).
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2+1 (have %d)", p->NGHOSTS);
-  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || (rfm && rfm->table64 && rfm->N0 == p->Nxx_plus_2NGHOSTS0 &&
-                                                             rfm->N1 == p->Nxx_plus_2NGHOSTS1),
+  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || rfm_matches(rfm, p),
                 "curvilinear BSSN needs an rfm_struct defined for this grid");
   return NRGPU_OK;
 }
@@ -47,7 +48,7 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
   if (i0 >= g.n0) return;
   const long long idx = (long long)i0 + (long long)g.n0 * ((long long)i1 + (long long)g.n1 * i2);
-  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g, i0, i1, i2);
   double h[3][3], gb[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY)
   if (!interior_point(g, i0, i1, i2, idx)) return;
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
-  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g, i0, i1, i2);
   double MU[3];
   momentum_point<ORDER, CS, double>(P, rf, inv, MU);
 #pragma unroll
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY)
   using M = RfmMask<CS>;
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const R inv[3] = {g.invdx0, g.invdx1, g.invdx2};
-  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g, i0, i1, i2);
   Metric<CS, R> m;
   metric_point<ORDER, CS, R>(P, rf, inv, m);
   R Rbar[6];
@@ -264,27 +265,36 @@ __global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gf
   const Dual X1{xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS), {0.0, 1.0, 0.0}};
   const Dual X2{xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS), {0.0, 0.0, 1.0}};
   Dual xc[3], J[3][3], s[3];
+  // sinh map A sinh(x/w)/sinh(1/w) (+ A c x) as a dual number, and its derivative
+  auto dsinh_map = [](double A, double w, double c, const Dual &x, Dual &f, Dual &df) {
+    const double den = exp(1.0 / w) - exp(-1.0 / w);
+    const Dual ep = dexp((1.0 / w) * x), em = dexp((-1.0 / w) * x);
+    f = (A / den) * (ep - em) + (A * c) * x;
+    df = (A / (w * den)) * (ep + em) + dconst(A * c);
+  };
   if (CS == NRGPU_COORD_CARTESIAN) {
     xc[0] = X0; xc[1] = X1; xc[2] = X2;
     for (int a = 0; a < 3; a++) {
       s[a] = dconst(1.0);
       for (int b = 0; b < 3; b++) J[a][b] = dconst(a == b ? 1.0 : 0.0);
     }
-  } else {
-    Dual r, dr;
-    if (CS == NRGPU_COORD_SINHSPHERICAL) {
-      const double den = exp(1.0 / p.SINHW) - exp(-1.0 / p.SINHW);
-      const Dual ep = dexp((1.0 / p.SINHW) * X0), em = dexp((-1.0 / p.SINHW) * X0);
-      r = (p.AMPL / den) * (ep - em);
-      dr = (p.AMPL / (p.SINHW * den)) * (ep + em);
-      if (p.CoordSystem == NRGPU_COORD_SINHSPHERICALV2) {  // + AMPL const_dr xx0
-        r = r + (p.AMPL * p.const_dr) * X0;
-        dr = dr + dconst(p.AMPL * p.const_dr);
-      }
-    } else {
-      r = X0;
-      dr = dconst(1.0);
+  } else if (cylindrical_family(p.CoordSystem)) {
+    // (rho cos phi, rho sin phi, z) (reference_metric.py:296-298)
+    Dual rho = X0, drho = dconst(1.0), z = X2, dz = dconst(1.0);
+    if (p.CoordSystem == NRGPU_COORD_SINHCYLINDRICAL) {
+      dsinh_map(p.AMPLRHO, p.SINHWRHO, 0.0, X0, rho, drho);
+      dsinh_map(p.AMPLZ, p.SINHWZ, 0.0, X2, z, dz);
     }
+    const Dual sp = dsin(X1), cp = dcos(X1);
+    xc[0] = rho * cp; xc[1] = rho * sp; xc[2] = z;
+    J[0][0] = drho * cp; J[0][1] = -(rho * sp); J[0][2] = dconst(0.0);
+    J[1][0] = drho * sp; J[1][1] = rho * cp;    J[1][2] = dconst(0.0);
+    J[2][0] = dconst(0.0); J[2][1] = dconst(0.0); J[2][2] = dz;
+    s[0] = drho; s[1] = rho; s[2] = dz;
+  } else {
+    Dual r = X0, dr = dconst(1.0);
+    if (p.CoordSystem == NRGPU_COORD_SINHSPHERICAL || p.CoordSystem == NRGPU_COORD_SINHSPHERICALV2)
+      dsinh_map(p.AMPL, p.SINHW, p.CoordSystem == NRGPU_COORD_SINHSPHERICALV2 ? p.const_dr : 0.0, X0, r, dr);
     const Dual st = dsin(X1), ct = dcos(X1), sp = dsin(X2), cp = dcos(X2);
     xc[0] = r * st * cp; xc[1] = r * st * sp; xc[2] = r * ct;
     J[0][0] = dr * st * cp; J[0][1] = r * ct * cp; J[0][2] = -(r * st * sp);
@@ -366,7 +376,7 @@ __global__ void constraint_sources_kernel(Grid g, const double *__restrict__ in,
   if (!interior_point(g, i0, i1, i2, idx)) return;
   using M = RfmMask<CS>;
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
-  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g, i0, i1, i2);
   const double pi = 3.14159265358979323846;
   const double alpha = __ldg(P.gf(ALPHA)), cf = __ldg(P.gf(CF));
   const double T00 = __ldg(T4 + idx);
@@ -445,6 +455,8 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   if (cart) enforce_kernel<NRGPU_COORD_CARTESIAN, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);     \
   else if (p->CoordSystem == NRGPU_COORD_SPHERICAL)                                                      \
     enforce_kernel<NRGPU_COORD_SPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
+  else if (cylindrical_family(p->CoordSystem))                                                            \
+    enforce_kernel<NRGPU_COORD_SINHCYLINDRICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);      \
   else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
   NRGPU_REQUIRE(!pair, "pair gridfunctions are FP32");
   ENF(double)
@@ -507,6 +519,8 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
       hamiltonian_kernel<NRGPU_COORD_CARTESIAN, 8><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_SINHSPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4:
+      hamiltonian_kernel<NRGPU_COORD_SINHCYLINDRICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_SPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     default:
@@ -519,9 +533,9 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
 int BSSN_Ricci_eval_xx(const paramstruct *p, double *xx[3], const double *in, double *aux) {
   int st = check_params(p);
   if (st) return st;
-  NRGPU_REQUIRE(xx && xx[0] && xx[1] && in && aux, "NULL argument");
+  NRGPU_REQUIRE(xx && xx[0] && xx[1] && xx[2] && in && aux, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
-  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW, p->const_dr, p->CoordSystem};
+  const XXArgs xa{xx[0], xx[1], xx[2], coord_params(*p)};
 #define RXX(CS, ORD) ricci_xx_launch_t<CS, ORD>(p, xa, in, aux)
   NRGPU_BSSN_SWITCH(RXX)
 #undef RXX
@@ -530,9 +544,9 @@ int BSSN_Ricci_eval_xx(const paramstruct *p, double *xx[3], const double *in, do
 int BSSN_rhs_eval_xx(const paramstruct *p, double *xx[3], const double *aux, const double *in, double *rhs) {
   int st = check_params(p);
   if (st) return st;
-  NRGPU_REQUIRE(xx && xx[0] && xx[1] && aux && in && rhs, "NULL argument");
+  NRGPU_REQUIRE(xx && xx[0] && xx[1] && xx[2] && aux && in && rhs, "NULL argument");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 + 1, "BSSN needs NGHOSTS >= FD_order/2 + 1");
-  const XXArgs xa{xx[0], xx[1], p->AMPL, p->SINHW, p->const_dr, p->CoordSystem};
+  const XXArgs xa{xx[0], xx[1], xx[2], coord_params(*p)};
 #define HXX(CS, ORD)                                                                 \
   (extras_on(p) ? rhs_xx_launch_t<CS, ORD, true>(p, xa, aux, in, rhs) \
                 : rhs_xx_launch_t<CS, ORD, false>(p, xa, aux, in, rhs))
@@ -554,6 +568,7 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const 
     case NRGPU_COORD_CARTESIAN * 16 + 6: MOM(NRGPU_COORD_CARTESIAN, 6); break;
     case NRGPU_COORD_CARTESIAN * 16 + 8: MOM(NRGPU_COORD_CARTESIAN, 8); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MOM(NRGPU_COORD_SINHSPHERICAL, 4); break;
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: MOM(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4: MOM(NRGPU_COORD_SPHERICAL, 4); break;
     default:
       set_error("momentum constraint: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
@@ -577,6 +592,11 @@ int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *
       break;
     case NRGPU_COORD_SPHERICAL:
       constraint_sources_kernel<NRGPU_COORD_SPHERICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H, MU);
+      break;
+    case NRGPU_COORD_CYLINDRICAL:
+    case NRGPU_COORD_SINHCYLINDRICAL:
+      constraint_sources_kernel<NRGPU_COORD_SINHCYLINDRICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU,
+                                                                                              H, MU);
       break;
     default:
       constraint_sources_kernel<NRGPU_COORD_SINHSPHERICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H,

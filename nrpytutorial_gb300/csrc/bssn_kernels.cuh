@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
   if (!interior_point(g, i0, i1, i2, idx)) return;
   Point<Tin> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
-  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g, i0, i1, i2);
   Metric<CS, R> m;
   metric_point<ORDER, CS, R>(P, rf, inv, m);
   R Rbar[6];
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
   if (!interior_point(g, i0, i1, i2, idx)) return;
   Point<Tin> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
-  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g, i0, i1, i2);
   R Rbar[6];
 #pragma unroll
   for (int k = 0; k < 6; k++) Rbar[k] = (R)__ldg(aux + (long long)k * g.ntot + idx);
@@ -189,19 +189,18 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
 }
 
 // The same kernels with the reference metric evaluated at each point from the
-// caller's coordinate arrays xx0[i0], xx1[i1] (FP64), as the reference's
+// caller's coordinate arrays xx0[i0], xx1[i1], xx2[i2] (FP64), as the reference's
 // no-precompute rhs_eval(params, xx, auxevol_gfs, in_gfs, rhs_gfs) does.
 struct XXArgs {
-  const double *xx0, *xx1;
-  double AMPL, SINHW, const_dr;
-  int cs;  // the runtime CoordSystem (SinhSphericalv2 runs on the SinhSpherical kernels)
+  const double *xx0, *xx1, *xx2;
+  CoordParams c;  // the runtime CoordSystem and its parameters
 };
 
 template <int CS>
-__device__ __forceinline__ void hatted_at_point(const XXArgs &xa, int i0, int i1, double *q) {
+__device__ __forceinline__ void hatted_at_point(const XXArgs &xa, int i0, int i1, int i2, double *q) {
   if constexpr (CS != NRGPU_COORD_CARTESIAN) {
     ScaleFactors S;
-    scale_factors(xa.cs, xa.AMPL, xa.SINHW, xa.xx0[i0], xa.xx1[i1], &S, xa.const_dr);
+    scale_factors(xa.c, xa.xx0[i0], xa.xx1[i1], xa.xx2[i2], &S);
     hatted_quantities(S, q);
   }
 }
@@ -213,7 +212,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
   long long idx;
   if (!interior_point(g, i0, i1, i2, idx)) return;
   double q[rq::NQ];
-  hatted_at_point<CS>(xa, i0, i1, q);
+  hatted_at_point<CS>(xa, i0, i1, i2, q);
   const Rfm<CS, double, true> rf{q, 1};
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
@@ -233,7 +232,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
   long long idx;
   if (!interior_point(g, i0, i1, i2, idx)) return;
   double q[rq::NQ];
-  hatted_at_point<CS>(xa, i0, i1, q);
+  hatted_at_point<CS>(xa, i0, i1, i2, q);
   const Rfm<CS, double, true> rf{q, 1};
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};

@@ -59,9 +59,12 @@ struct Grid {
 // on the structure of the reference metric (which scale factor depends on
 // which coordinate, RfmMask) and read its values from the rfm tables;
 // SinhSphericalv2 has SinhSpherical's structure and differs only in r(xx0),
-// which the tables and the runtime CoordSystem carry.
+// Cylindrical has SinhCylindrical's with the identity maps; the tables and
+// the runtime CoordSystem carry the values.
 inline int dispatch_cs(int cs) {
-  return cs == NRGPU_COORD_SINHSPHERICALV2 ? NRGPU_COORD_SINHSPHERICAL : cs;
+  return cs == NRGPU_COORD_SINHSPHERICALV2 ? NRGPU_COORD_SINHSPHERICAL
+         : cs == NRGPU_COORD_CYLINDRICAL   ? NRGPU_COORD_SINHCYLINDRICAL
+                                           : cs;
 }
 
 inline Grid make_grid(const paramstruct *p) {

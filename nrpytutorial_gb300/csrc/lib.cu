@@ -29,7 +29,7 @@ void count_launch(int n) { g_launches += n; }
 
 int check_params(const paramstruct *p) {
   NRGPU_REQUIRE(p != nullptr, "params is NULL");
-  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 3, "unknown CoordSystem %d", p->CoordSystem);
+  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 5, "unknown CoordSystem %d", p->CoordSystem);
   NRGPU_REQUIRE(p->FD_order == 2 || p->FD_order == 4 || p->FD_order == 6 || p->FD_order == 8,
                 "FD_order %d not in {2,4,6,8}", p->FD_order);
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 && p->NGHOSTS <= NRGPU_MAX_GHOSTS,
@@ -47,18 +47,21 @@ int check_params(const paramstruct *p) {
 }
 
 // ----------------------------------------------------------------- rfm define
+// One thread per (i0, iB) column: iB = i1 for the Spherical family, i2 for
+// the Cylindrical family (the coordinate the reference metric depends on).
 __global__ void rfm_define_kernel(paramstruct p, double *tab64, float *tab32) {
+  const bool cyl = cylindrical_family(p.CoordSystem);
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i1 = blockIdx.y;
-  const int n0 = p.Nxx_plus_2NGHOSTS0, n1 = p.Nxx_plus_2NGHOSTS1;
-  if (i0 >= n0 || i1 >= n1) return;
+  const int iB = blockIdx.y;
+  const int n0 = p.Nxx_plus_2NGHOSTS0, nB = cyl ? p.Nxx_plus_2NGHOSTS2 : p.Nxx_plus_2NGHOSTS1;
+  if (i0 >= n0 || iB >= nB) return;
   const double xx0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS);
-  const double xx1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS);
+  const double xxB = cyl ? xx_of(p.xxmin2, p.dxx2, iB, p.NGHOSTS) : xx_of(p.xxmin1, p.dxx1, iB, p.NGHOSTS);
   ScaleFactors S;
-  scale_factors(p.CoordSystem, p.AMPL, p.SINHW, xx0, xx1, &S, p.const_dr);
+  scale_factors(coord_params(p), xx0, xxB, xxB, &S);
   double out[rq::NQ];
   hatted_quantities(S, out);
-  const long long plane = (long long)n0 * n1, col = (long long)i1 * n0 + i0;
+  const long long plane = (long long)n0 * nB, col = (long long)iB * n0 + i0;
   for (int q = 0; q < rq::NQ; q++) {
     tab64[q * plane + col] = out[q];
     tab32[q * plane + col] = (float)out[q];
@@ -120,12 +123,20 @@ int set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3], paramstr
   p->Nxx_plus_2NGHOSTS2 = Nxx[2] + 2 * p->NGHOSTS;
   double xmin[3], xmax[3];
   int cs = p->CoordSystem;
-  // EigenCoord of the Spherical family is Spherical (reference_metric.py:946-952).
+  // EigenCoord of the Spherical family is Spherical, of the Cylindrical
+  // family Cylindrical (reference_metric.py:946-952).
   if (EigenCoord && spherical_family(cs)) cs = NRGPU_COORD_SPHERICAL;
+  if (EigenCoord && cylindrical_family(cs)) cs = NRGPU_COORD_CYLINDRICAL;
   if (cs == NRGPU_COORD_CARTESIAN) {
     xmin[0] = p->xmin; xmax[0] = p->xmax;
     xmin[1] = p->ymin; xmax[1] = p->ymax;
     xmin[2] = p->zmin; xmax[2] = p->zmax;
+  } else if (cylindrical_family(cs)) {
+    // Cylindrical :233-234; SinhCylindrical :246-247
+    const bool plain = cs == NRGPU_COORD_CYLINDRICAL;
+    xmin[0] = 0.0;                     xmax[0] = plain ? p->RHOMAX : 1.0;
+    xmin[1] = -M_PI;                   xmax[1] = M_PI;
+    xmin[2] = plain ? p->ZMIN : -1.0;  xmax[2] = plain ? p->ZMAX : 1.0;
   } else {
     xmin[0] = 0.0;
     xmax[0] = (cs == NRGPU_COORD_SPHERICAL) ? p->RMAX : 1.0;
@@ -151,14 +162,17 @@ int set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3], paramstr
 
 double find_timestep(const paramstruct *p, double CFL_FACTOR) {
   if (check_params(p) != NRGPU_OK) return -1.0;
+  // min over interior points of dxx_i s_i; the scale factors depend on
+  // (xx0, xx1) (Spherical family) or (xx0, xx2) (Cylindrical family) only
+  const bool cyl = cylindrical_family(p->CoordSystem);
+  const int ng = p->NGHOSTS, nB = cyl ? p->Nxx_plus_2NGHOSTS2 : p->Nxx_plus_2NGHOSTS1;
   double dsmin = 1e38;
-  const int ng = p->NGHOSTS;
-  for (int i1 = ng; i1 < p->Nxx_plus_2NGHOSTS1 - ng; i1++)
+  for (int iB = ng; iB < nB - ng; iB++)
     for (int i0 = ng; i0 < p->Nxx_plus_2NGHOSTS0 - ng; i0++) {
       const double xx0 = xx_of(p->xxmin0, p->dxx0, i0, ng);
-      const double xx1 = xx_of(p->xxmin1, p->dxx1, i1, ng);
+      const double xxB = cyl ? xx_of(p->xxmin2, p->dxx2, iB, ng) : xx_of(p->xxmin1, p->dxx1, iB, ng);
       ScaleFactors S;
-      scale_factors(p->CoordSystem, p->AMPL, p->SINHW, xx0, xx1, &S, p->const_dr);
+      scale_factors(coord_params(*p), xx0, xxB, xxB, &S);
       const double ds0 = p->dxx0 * S.s[0], ds1 = p->dxx1 * S.s[1], ds2 = p->dxx2 * S.s[2];
       dsmin = fmin(dsmin, fmin(ds0, fmin(ds1, ds2)));
     }
@@ -172,7 +186,7 @@ int rfm_struct__malloc(const paramstruct *p, rfm_struct *rfm) {
   memset(rfm, 0, sizeof(*rfm));
   rfm->CoordSystem = p->CoordSystem;
   rfm->N0 = p->Nxx_plus_2NGHOSTS0;
-  rfm->N1 = p->Nxx_plus_2NGHOSTS1;
+  rfm->N1 = rfm_second_extent(p);
   rfm->nquant = rq::NQ;
   const size_t n = (size_t)rq::NQ * rfm->N0 * rfm->N1;
   NRGPU_CUDA_CHECK(cudaMalloc(&rfm->table64, n * sizeof(double)));
@@ -184,8 +198,7 @@ int rfm_struct__define(const paramstruct *p, rfm_struct *rfm) {
   int st = check_params(p);
   if (st) return st;
   NRGPU_REQUIRE(rfm && rfm->table64 && rfm->table32, "rfm tables not allocated");
-  NRGPU_REQUIRE(rfm->N0 == p->Nxx_plus_2NGHOSTS0 && rfm->N1 == p->Nxx_plus_2NGHOSTS1,
-                "rfm tables sized for another grid");
+  NRGPU_REQUIRE(rfm_matches(rfm, p), "rfm tables sized for another grid");
   dim3 block(64), grid((rfm->N0 + 63) / 64, rfm->N1);
   rfm_define_kernel<<<grid, block, 0, stream()>>>(*p, rfm->table64, rfm->table32);
   NRGPU_LAUNCH_CHECK();

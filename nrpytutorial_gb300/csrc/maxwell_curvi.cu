@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128)
   using M = RfmMask<CS>;
   const long long st[3] = {1, g.n0, (long long)g.n0 * g.n1};
   const R inv[3] = {(R)g.invdx0, (R)g.invdx1, (R)g.invdx2};
-  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, R> rf = rfm_at<CS, R>(tab, g, i0, i1, i2);
   auto gf = [&](int k) { return in + (long long)k * g.ntot + idx; };
   // A^i, A^i_,j and the unmixed A^i_,jj
   R A[3], Ad[3][3], Add[3][3];
@@ -118,7 +118,7 @@ __global__ void maxwell_curvi_constraint_kernel(Grid g, const double *__restrict
   using M = RfmMask<CS>;
   const long long st[3] = {1, g.n0, (long long)g.n0 * g.n1};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
-  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g, i0, i1, i2);
   double C = 0.0, G = __ldg(in + (long long)GAMMA * g.ntot + idx);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -165,7 +165,7 @@ __global__ void maxwell_curvi_id_kernel(paramstruct p, double amp, double lam, d
   const double xx0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS), xx1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS),
                xx2 = xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS);
   double x[3], J[3][3], Ji[3][3];
-  cart_jacobian(p.CoordSystem, xx0, xx1, xx2, p.AMPL, p.SINHW, p.const_dr, x, J);
+  cart_jacobian(coord_params(p), xx0, xx1, xx2, x, J);
   inverse3(J, Ji);
   const double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
   const double u = t + r, v = t - r;
@@ -177,7 +177,7 @@ __global__ void maxwell_curvi_id_kernel(paramstruct p, double amp, double lam, d
   double s[3] = {1.0, 1.0, 1.0};
   if constexpr (CS != NRGPU_COORD_CARTESIAN) {
     ScaleFactors S;
-    scale_factors(p.CoordSystem, p.AMPL, p.SINHW, xx0, xx1, &S, p.const_dr);
+    scale_factors(coord_params(p), xx0, xx1, xx2, &S);
     for (int i = 0; i < 3; i++) s[i] = S.s[i];  // 1/ReU^i
   }
   for (int i = 0; i < 3; i++) {
@@ -220,6 +220,7 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
   MC_CASE(NRGPU_COORD_CARTESIAN, 2) MC_CASE(NRGPU_COORD_CARTESIAN, 4)
   MC_CASE(NRGPU_COORD_SPHERICAL, 2) MC_CASE(NRGPU_COORD_SPHERICAL, 4)
   MC_CASE(NRGPU_COORD_SINHSPHERICAL, 2) MC_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
+  MC_CASE(NRGPU_COORD_SINHCYLINDRICAL, 2) MC_CASE(NRGPU_COORD_SINHCYLINDRICAL, 4)
 #undef MC_CASE
   set_error("curvilinear Maxwell: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order);
   return NRGPU_ERR_UNSUPPORTED;
@@ -287,6 +288,8 @@ int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const paramstruct *p, 
     case NRGPU_COORD_SPHERICAL * 16 + 4: MCC(NRGPU_COORD_SPHERICAL, 4); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 2: MCC(NRGPU_COORD_SINHSPHERICAL, 2); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MCC(NRGPU_COORD_SINHSPHERICAL, 4); break;
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 2: MCC(NRGPU_COORD_SINHCYLINDRICAL, 2); break;
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: MCC(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
     default: set_error("curvilinear Maxwell constraints: FD_order %d not built", p->FD_order); return NRGPU_ERR_UNSUPPORTED;
   }
 #undef MCC

@@ -141,7 +141,7 @@ __device__ void psi4_point(const Point<double> &P, const Rfm<CS, double> &rf, co
 
   // ---- tetrad (xx basis)
   double x[3], J[3][3], Ji[3][3];
-  cart_jacobian(prm.CoordSystem, xx0, xx1, xx2, prm.AMPL, prm.SINHW, prm.const_dr, x, J);
+  cart_jacobian(coord_params(prm), xx0, xx1, xx2, x, J);
   inverse3(J, Ji);
   const double v1C[3] = {-x[1], x[0], 0.0};
   double v1[3], v2[3], v3[3];
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kPsi4Threads) psi4_kernel(Grid g, const double
   const long long idx = i0 + (long long)g.n0 * (i1 + (long long)g.n1 * i2);
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
-  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g.n0, g.n1, i0, i1);
+  const Rfm<CS, double> rf = rfm_at<CS, double>(tab, g, i0, i1, i2);
   const double xx0 = xx_of(p.xxmin0, p.dxx0, i0, g.ng);
   const double xx1 = xx_of(p.xxmin1, p.dxx1, i1, g.ng);
   const double xx2 = xx_of(p.xxmin2, p.dxx2, i2, g.ng);
@@ -389,8 +389,7 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
   if (st) return st;
   NRGPU_REQUIRE(in_gfs && psi4_gfs, "NULL gridfunctions");
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2, "psi4 needs NGHOSTS >= FD_order/2");
-  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || (rfm && rfm->table64 && rfm->N0 == p->Nxx_plus_2NGHOSTS0 &&
-                                                             rfm->N1 == p->Nxx_plus_2NGHOSTS1),
+  NRGPU_REQUIRE(p->CoordSystem == NRGPU_COORD_CARTESIAN || rfm_matches(rfm, p),
                 "curvilinear psi4 needs an rfm_struct defined for this grid");
   const int ng = p->NGHOSTS;
   if (i0_min < 0 && i0_max < 0) {
@@ -409,6 +408,7 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
     case NRGPU_COORD_CARTESIAN * 16 + 4: P4(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6: P4(NRGPU_COORD_CARTESIAN, 6); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: P4(NRGPU_COORD_SINHSPHERICAL, 4); break;
+    case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: P4(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4: P4(NRGPU_COORD_SPHERICAL, 4); break;
     default:
       set_error("psi4: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
@@ -424,7 +424,7 @@ int BSSN_psi4_spinweightm2_decomposition(const paramstruct *p, const double *psi
   int st = check_params(p);
   if (st) return st;
   NRGPU_REQUIRE(psi4_gfs && modes, "NULL argument");
-  NRGPU_REQUIRE(p->CoordSystem != NRGPU_COORD_CARTESIAN, "the mode decomposition needs a spherical-like grid");
+  NRGPU_REQUIRE(spherical_family(p->CoordSystem), "the mode decomposition needs a spherical-like grid");
   NRGPU_REQUIRE(l_max >= 2 && l_max <= kMaxL, "l_max %d outside [2, %d]", l_max, kMaxL);
   NRGPU_REQUIRE(i0 >= p->NGHOSTS && i0 < p->Nxx_plus_2NGHOSTS0 - p->NGHOSTS, "i0 %d is not an interior shell", i0);
   Grid g = make_grid(p);

@@ -1,14 +1,15 @@
 // rfm.cuh -- reference metric ("hatted" quantities) for orthogonal,
 // diagonal coordinate systems: Cartesian, Spherical, SinhSpherical,
-// SinhSphericalv2.
+// SinhSphericalv2, Cylindrical, SinhCylindrical.
 //
 // reference_metric.py:487-601 derives, from the orthogonal scale factors
 // s_i(xx) (ghat_ii = s_i^2, ReU_i = 1/s_i, ReDD_ij = s_i s_j), the first and
 // second derivatives of ReU, ReDD and ghat, the Christoffel symbols
 // GammahatUDD and their derivatives, and det(ghat) with derivatives.  Here
 // the same quantities are evaluated numerically in FP64 from closed-form
-// s_i, ds_i, d2s_i, once per (i0,i1) column of the grid (none depends on
-// xx2 for these systems), and stored as dense tables -- the analogue of the
+// s_i, ds_i, d2s_i, once per (i0,iB) column of the grid (the Spherical family
+// depends on xx0 and xx1 only, iB = i1; the Cylindrical family on xx0 and xx2
+// only, iB = i2), and stored as dense tables -- the analogue of the
 // rfm_precompute arrays of reference_metric.py:603-886.
 //
 // Which entries can be non-zero follows from which coordinates each s_i
@@ -42,9 +43,15 @@ constexpr int NQ = 403;
 }  // namespace rq
 
 // ------------------------------------------------------- dependency masks
+__host__ __device__ constexpr bool cylindrical_family(int cs) {
+  return cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICAL;
+}
+
 // dep(CS, i, k): does scale factor s_i depend on xx_k?
 __host__ __device__ constexpr bool dep(int cs, int i, int k) {
   return cs == NRGPU_COORD_CARTESIAN ? false
+         // Cylindrical family: s0 = drho/dxx0, s1 = rho(xx0), s2 = dz/dxx2
+         : cylindrical_family(cs) ? ((k == 0 && i <= 1) || (k == 2 && i == 2))
          // Spherical family: s0 = dr/dxx0, s1 = r(xx0), s2 = r(xx0) sin(xx1)
          : (k == 0) ? true : (k == 1 ? i == 2 : false);
 }
@@ -78,14 +85,14 @@ template <int CS> struct RfmMask {
 };
 
 // ------------------------------------------------------- point accessor
-// Reads hatted quantities at one (i0,i1) column.  R is the arithmetic type
+// Reads hatted quantities at one (i0,iB) column.  R is the arithmetic type
 // of the caller; tables are FP64 (tab64) with an FP32 copy (tab32).
 // LOCAL: base points at this thread's own NQ values (plane 1), computed from
 // the caller's coordinates instead of read from the precomputed table.
 template <int CS, typename R, bool LOCAL = false> struct Rfm {
   using M = RfmMask<CS>;
-  const R *__restrict__ base;  // table + i1*N0 + i0
-  long long plane;             // N0*N1
+  const R *__restrict__ base;  // table + iB*N0 + i0
+  long long plane;             // N0*NB
 
   __device__ __forceinline__ R q(int slot) const {
     if constexpr (LOCAL) return base[slot];
@@ -130,52 +137,90 @@ template <int CS, typename R, bool LOCAL = false> struct Rfm {
   __device__ __forceinline__ R detgdDD(int k, int l) const { return q(rq::detgammahatdDD + 3 * k + l); }
 };
 
+// Extent of the table's second coordinate, and whether tables fit a grid.
+inline int rfm_second_extent(const paramstruct *p) {
+  return cylindrical_family(p->CoordSystem) ? p->Nxx_plus_2NGHOSTS2 : p->Nxx_plus_2NGHOSTS1;
+}
+inline bool rfm_matches(const rfm_struct *rfm, const paramstruct *p) {
+  return rfm && rfm->table64 && rfm->CoordSystem == p->CoordSystem && rfm->N0 == p->Nxx_plus_2NGHOSTS0 &&
+         rfm->N1 == rfm_second_extent(p);
+}
+
 template <int CS, typename R>
-__device__ __forceinline__ Rfm<CS, R> rfm_at(const R *tab, int n0, int n1, int i0, int i1) {
+__device__ __forceinline__ Rfm<CS, R> rfm_at(const R *tab, const Grid &g, int i0, int i1, int i2) {
+  constexpr bool cyl = cylindrical_family(CS);
+  const int nB = cyl ? g.n2 : g.n1, iB = cyl ? i2 : i1;
   Rfm<CS, R> r;
-  r.base = tab ? tab + (long long)i1 * n0 + i0 : nullptr;
-  r.plane = (long long)n0 * n1;
+  r.base = tab ? tab + (long long)iB * g.n0 + i0 : nullptr;
+  r.plane = (long long)g.n0 * nB;
   return r;
 }
 
 // --------------------------------------------------- scale-factor closed forms
-// s[i], ds[i][k] = d s_i / d xx_k, dds[i][k][l], at uniform coordinates
-// (xx0, xx1).  Spherical: r = xx0; SinhSpherical: r = AMPL sinh(xx0/SINHW) /
-// sinh(1/SINHW), written with exponentials as reference_metric.py:125-126 does;
-// SinhSphericalv2 adds AMPL const_dr xx0 (reference_metric.py:142-143).
-// Every system of the family has the Spherical angles and the Spherical
-// eigen-coordinates, so only r(xx0) and its derivatives differ.
-struct ScaleFactors {
-  double s[3], ds[3][3], dds[3][3][3];
+// The coordinate parameters of a paramstruct that the maps below read.
+struct CoordParams {
+  int cs;
+  double AMPL, SINHW, const_dr;             // Spherical family
+  double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  // SinhCylindrical
 };
+
+__host__ __device__ inline CoordParams coord_params(const paramstruct &p) {
+  return CoordParams{p.CoordSystem, p.AMPL, p.SINHW, p.const_dr, p.AMPLRHO, p.SINHWRHO, p.AMPLZ, p.SINHWZ};
+}
 
 __host__ __device__ inline bool spherical_family(int cs) {
   return cs == NRGPU_COORD_SPHERICAL || cs == NRGPU_COORD_SINHSPHERICAL || cs == NRGPU_COORD_SINHSPHERICALV2;
 }
 
-// r(x) and its first three derivatives.
-__host__ __device__ inline void radial_map(int cs, double AMPL, double SINHW, double x,
-                                           double *r, double *r1, double *r2, double *r3,
-                                           double const_dr = 0.0) {
-  if (cs == NRGPU_COORD_SINHSPHERICAL || cs == NRGPU_COORD_SINHSPHERICALV2) {
-    const double ep = exp(x / SINHW), em = exp(-x / SINHW);
-    const double den = exp(1.0 / SINHW) - exp(-1.0 / SINHW);
-    const double sh = AMPL * (ep - em) / den, ch = AMPL * (ep + em) / (SINHW * den);
-    const double lin = cs == NRGPU_COORD_SINHSPHERICALV2 ? AMPL * const_dr : 0.0;
-    *r = sh + lin * x;
-    *r1 = ch + lin;
-    *r2 = sh / (SINHW * SINHW);
-    *r3 = ch / (SINHW * SINHW);
+// f(x) = A sinh(x/w) / sinh(1/w) + A c x and its first three derivatives,
+// with the exponentials written as reference_metric.py:125-126, 255-258 does.
+__host__ __device__ inline void sinh_map(double A, double w, double c, double x, double f[4]) {
+  const double ep = exp(x / w), em = exp(-x / w);
+  const double den = exp(1.0 / w) - exp(-1.0 / w);
+  const double sh = A * (ep - em) / den, ch = A * (ep + em) / (w * den);
+  f[0] = sh + A * c * x;
+  f[1] = ch + A * c;
+  f[2] = sh / (w * w);
+  f[3] = ch / (w * w);
+}
+
+// Spherical family: r(xx0) and three derivatives.  Spherical: r = xx0;
+// SinhSpherical: the sinh map (reference_metric.py:125-126); SinhSphericalv2
+// adds AMPL const_dr xx0 (:142-143).
+__host__ __device__ inline void radial_map(const CoordParams &c, double x, double r[4]) {
+  if (c.cs == NRGPU_COORD_SINHSPHERICAL || c.cs == NRGPU_COORD_SINHSPHERICALV2) {
+    sinh_map(c.AMPL, c.SINHW, c.cs == NRGPU_COORD_SINHSPHERICALV2 ? c.const_dr : 0.0, x, r);
   } else {
-    *r = x;
-    *r1 = 1.0;
-    *r2 = 0.0;
-    *r3 = 0.0;
+    r[0] = x;
+    r[1] = 1.0;
+    r[2] = r[3] = 0.0;
   }
 }
 
-__host__ __device__ inline void scale_factors(int cs, double AMPL, double SINHW, double xx0,
-                                              double xx1, ScaleFactors *S, double const_dr = 0.0) {
+// Cylindrical family: rho(xx0) and z(xx2) with three derivatives each
+// (Cylindrical: the identity, reference_metric.py:237-239; SinhCylindrical:
+// sinh maps, :255-258).
+__host__ __device__ inline void cylinder_maps(const CoordParams &c, double x0, double x2, double rho[4],
+                                              double z[4]) {
+  if (c.cs == NRGPU_COORD_SINHCYLINDRICAL) {
+    sinh_map(c.AMPLRHO, c.SINHWRHO, 0.0, x0, rho);
+    sinh_map(c.AMPLZ, c.SINHWZ, 0.0, x2, z);
+  } else {
+    rho[0] = x0; rho[1] = 1.0; rho[2] = rho[3] = 0.0;
+    z[0] = x2; z[1] = 1.0; z[2] = z[3] = 0.0;
+  }
+}
+
+// s[i], ds[i][k] = d s_i / d xx_k, dds[i][k][l] at uniform coordinates
+// (xx0, xx1, xx2) (reference_metric.py:168-175 Spherical family: s0 = dr/dxx0,
+// s1 = r, s2 = r sin(xx1); :289-291 Cylindrical family: s0 = drho/dxx0,
+// s1 = rho, s2 = dz/dxx2; Cartesian: 1).
+struct ScaleFactors {
+  double s[3], ds[3][3], dds[3][3][3];
+};
+
+__host__ __device__ inline void scale_factors(const CoordParams &c, double xx0, double xx1, double xx2,
+                                              ScaleFactors *S) {
   for (int i = 0; i < 3; i++) {
     S->s[i] = 1.0;
     for (int k = 0; k < 3; k++) {
@@ -183,22 +228,36 @@ __host__ __device__ inline void scale_factors(int cs, double AMPL, double SINHW,
       for (int l = 0; l < 3; l++) S->dds[i][k][l] = 0.0;
     }
   }
-  if (cs == NRGPU_COORD_CARTESIAN) return;
-  double r, r1, r2, r3;
-  radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3, const_dr);
+  if (c.cs == NRGPU_COORD_CARTESIAN) return;
+  if (cylindrical_family(c.cs)) {
+    double rho[4], z[4];
+    cylinder_maps(c, xx0, xx2, rho, z);
+    S->s[0] = rho[1];
+    S->s[1] = rho[0];
+    S->s[2] = z[1];
+    S->ds[0][0] = rho[2];
+    S->ds[1][0] = rho[1];
+    S->ds[2][2] = z[2];
+    S->dds[0][0][0] = rho[3];
+    S->dds[1][0][0] = rho[2];
+    S->dds[2][2][2] = z[3];
+    return;
+  }
+  double r[4];
+  radial_map(c, xx0, r);
   const double sn = sin(xx1), cs1 = cos(xx1);
-  S->s[0] = r1;
-  S->s[1] = r;
-  S->s[2] = r * sn;
-  S->ds[0][0] = r2;
-  S->ds[1][0] = r1;
-  S->ds[2][0] = r1 * sn;
-  S->ds[2][1] = r * cs1;
-  S->dds[0][0][0] = r3;
-  S->dds[1][0][0] = r2;
-  S->dds[2][0][0] = r2 * sn;
-  S->dds[2][0][1] = S->dds[2][1][0] = r1 * cs1;
-  S->dds[2][1][1] = -r * sn;
+  S->s[0] = r[1];
+  S->s[1] = r[0];
+  S->s[2] = r[0] * sn;
+  S->ds[0][0] = r[2];
+  S->ds[1][0] = r[1];
+  S->ds[2][0] = r[1] * sn;
+  S->ds[2][1] = r[0] * cs1;
+  S->dds[0][0][0] = r[3];
+  S->dds[1][0][0] = r[2];
+  S->dds[2][0][0] = r[2] * sn;
+  S->dds[2][0][1] = S->dds[2][1][0] = r[1] * cs1;
+  S->dds[2][1][1] = -r[0] * sn;
 }
 
 // Fills all rq::NQ derived quantities from scale factors (dense, FP64).
@@ -265,32 +324,47 @@ __host__ __device__ inline void hatted_quantities(const ScaleFactors &S, double 
   }
 }
 
-// xx -> Cartesian and d x_Cart^i / d xx^j (reference_metric.py xx_to_Cart).
-__host__ __device__ inline void cart_jacobian(int cs, double xx0, double xx1, double xx2, double AMPL,
-                                              double SINHW, double const_dr, double x[3], double J[3][3]) {
-  if (cs == NRGPU_COORD_CARTESIAN) {
+// xx -> Cartesian and d x_Cart^i / d xx^j (reference_metric.py xx_to_Cart:
+// Spherical family :159-161, Cylindrical family :296-298).
+__host__ __device__ inline void cart_jacobian(const CoordParams &c, double xx0, double xx1, double xx2,
+                                              double x[3], double J[3][3]) {
+  if (c.cs == NRGPU_COORD_CARTESIAN) {
     x[0] = xx0;
     x[1] = xx1;
     x[2] = xx2;
-#pragma unroll
     for (int i = 0; i < 3; i++)
-#pragma unroll
       for (int j = 0; j < 3; j++) J[i][j] = i == j ? 1.0 : 0.0;
+  } else if (cylindrical_family(c.cs)) {
+    double rho[4], z[4];
+    cylinder_maps(c, xx0, xx2, rho, z);
+    const double sp = sin(xx1), cp = cos(xx1);
+    x[0] = rho[0] * cp;
+    x[1] = rho[0] * sp;
+    x[2] = z[0];
+    J[0][0] = rho[1] * cp;
+    J[0][1] = -rho[0] * sp;
+    J[0][2] = 0.0;
+    J[1][0] = rho[1] * sp;
+    J[1][1] = rho[0] * cp;
+    J[1][2] = 0.0;
+    J[2][0] = 0.0;
+    J[2][1] = 0.0;
+    J[2][2] = z[1];
   } else {
-    double r, r1, r2, r3;
-    radial_map(cs, AMPL, SINHW, xx0, &r, &r1, &r2, &r3, const_dr);
+    double r[4];
+    radial_map(c, xx0, r);
     const double st = sin(xx1), ct = cos(xx1), sp = sin(xx2), cp = cos(xx2);
-    x[0] = r * st * cp;
-    x[1] = r * st * sp;
-    x[2] = r * ct;
-    J[0][0] = r1 * st * cp;
-    J[0][1] = r * ct * cp;
-    J[0][2] = -r * st * sp;
-    J[1][0] = r1 * st * sp;
-    J[1][1] = r * ct * sp;
-    J[1][2] = r * st * cp;
-    J[2][0] = r1 * ct;
-    J[2][1] = -r * st;
+    x[0] = r[0] * st * cp;
+    x[1] = r[0] * st * sp;
+    x[2] = r[0] * ct;
+    J[0][0] = r[1] * st * cp;
+    J[0][1] = r[0] * ct * cp;
+    J[0][2] = -r[0] * st * sp;
+    J[1][0] = r[1] * st * sp;
+    J[1][1] = r[0] * ct * sp;
+    J[1][2] = r[0] * st * cp;
+    J[2][0] = r[1] * ct;
+    J[2][1] = -r[0] * st;
     J[2][2] = 0.0;
   }
 }

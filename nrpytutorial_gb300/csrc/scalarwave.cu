@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256)
     for (int d = 0; d < 3; d++) lap += fd_d2<ORDER, R>(uu, st[d]) * (inv[d] * inv[d]);
   } else {
     using M = RfmMask<CS>;
-    const Rfm<CS, R> rf = rfm_at<CS, R>(rfmtab, g.n0, g.n1, i0, i1);
+    const Rfm<CS, R> rf = rfm_at<CS, R>(rfmtab, g, i0, i1, i2);
     R contracted[3] = {(R)0, (R)0, (R)0};
 #pragma unroll
     for (int k = 0; k < 3; k++)
@@ -80,6 +80,7 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
   SW_CASE(NRGPU_COORD_CARTESIAN, 6) SW_CASE(NRGPU_COORD_CARTESIAN, 8)
   SW_CASE(NRGPU_COORD_SPHERICAL, 2) SW_CASE(NRGPU_COORD_SPHERICAL, 4)
   SW_CASE(NRGPU_COORD_SINHSPHERICAL, 2) SW_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
+  SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 2) SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 4)
 #undef SW_CASE
   set_error("ScalarWave: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order);
   return NRGPU_ERR_UNSUPPORTED;
@@ -116,18 +117,9 @@ __global__ void sw_initial_data_kernel(paramstruct p, int kind, double t, double
   const long long idx = i0 + (long long)n0 * (i1 + (long long)n1 * i2);
   const double x0 = xx_of(p.xxmin0, p.dxx0, i0, p.NGHOSTS), x1 = xx_of(p.xxmin1, p.dxx1, i1, p.NGHOSTS),
                x2 = xx_of(p.xxmin2, p.dxx2, i2, p.NGHOSTS);
-  double x, y, z;
-  if (p.CoordSystem == NRGPU_COORD_CARTESIAN) {
-    x = x0;
-    y = x1;
-    z = x2;
-  } else {
-    double r, r1, r2, r3;
-    radial_map(p.CoordSystem, p.AMPL, p.SINHW, x0, &r, &r1, &r2, &r3, p.const_dr);
-    x = r * sin(x1) * cos(x2);
-    y = r * sin(x1) * sin(x2);
-    z = r * cos(x1);
-  }
+  double X[3], J[3][3];
+  cart_jacobian(coord_params(p), x0, x1, x2, X, J);  // xx_to_Cart
+  const double x = X[0], y = X[1], z = X[2];
   const double c = p.wavespeed;
   double uu, vv;
   if (kind == 0) {

@@ -19,7 +19,7 @@ then the post-RHS calls (BCs, then the det(gammabar) rescale for BSSN).
 """
 import numpy as np
 
-from .grid import CART, GridParams, radial
+from .grid import CART, GridParams, cylinder_maps, cylindrical, radial
 
 
 def build_bcstruct(gp):
@@ -27,14 +27,19 @@ def build_bcstruct(gp):
     outer = list of (idx3, step) in application order (grouped per face dir:
     list of 3 arrays), inner = (dest idx3, src idx3, parity (n,10) ints)."""
     eg = GridParams(gp.CoordSystem, gp.Nxx, gp.NGHOSTS, gp.FD_order, gp.AMPL, gp.SINHW, gp.RMAX,
-                    EigenCoord=1)
+                    EigenCoord=1, RHOMAX=gp.RHOMAX, ZMIN=gp.ZMIN, ZMAX=gp.ZMAX)
     n0, n1, n2 = eg.np
     ng = gp.NGHOSTS
     cart = gp.CoordSystem == CART
+    cyl = cylindrical(gp.CoordSystem)
     X2, X1, X0 = np.meshgrid(eg.xx[2], eg.xx[1], eg.xx[0], indexing="ij")
     if cart:
         xc = [X0, X1, X2]
         xin = [X0, X1, X2]
+    elif cyl:
+        # Cylindrical eigen-coordinates (reference_metric.py:240-242, 296-298)
+        xc = [X0 * np.cos(X1), X0 * np.sin(X1), X2]
+        xin = [np.sqrt(xc[0] ** 2 + xc[1] ** 2), np.arctan2(xc[1], xc[0]), X2]
     else:
         xc = [X0 * np.sin(X1) * np.cos(X2), X0 * np.sin(X1) * np.sin(X2), X0 * np.cos(X1)]
         r = np.sqrt(xc[0] ** 2 + xc[1] ** 2 + xc[2] ** 2)
@@ -51,6 +56,9 @@ def build_bcstruct(gp):
             for i in range(3):
                 e[i, i] = 1.0
             return e
+        if cyl:  # reference_metric.py:300-302, phi = xx1
+            sp, cp, z0 = np.sin(x1), np.cos(x1), 0 * np.asarray(x1, dtype=float)
+            return np.array([[cp, sp, z0], [-sp, cp, z0], [z0, z0, z0 + 1.0]])
         st, ct, sp, cp = np.sin(x1), np.cos(x1), np.sin(x2), np.cos(x2)
         return np.array([[st * cp, st * sp, ct], [ct * cp, ct * sp, -st], [-sp, cp, 0 * st]])
 
@@ -199,6 +207,10 @@ def _radial_geometry(gp, i0, i1, i2):
         return r, (x0 / r, x1 / r, x2 / r)
     if gp.CoordSystem == 1:  # Spherical: xx0 = r
         return x0, (1.0, 0.0, 0.0)
+    if cylindrical(gp.CoordSystem):  # r = sqrt(rho^2 + z^2)
+        (rho, drho), (z, dz) = cylinder_maps(gp, x0, x2)
+        r = float(np.sqrt(rho * rho + z * z))
+        return r, (float(rho / r / drho), 0.0, float(z / r / dz))
     r, drdx = radial(gp.CoordSystem, x0, gp.AMPL, gp.SINHW, gp.const_dr)
     return r, (1.0 / float(drdx), 0.0, 0.0)
 

@@ -22,7 +22,7 @@ Restated from (zachetienne/nrpytutorial):
 import numpy as np
 
 from .fd import Stencils
-from .grid import CART, hatted
+from .grid import CART, hatted_grid
 
 EVOL = ["aDD00", "aDD01", "aDD02", "aDD11", "aDD12", "aDD22", "alpha", "betU0", "betU1", "betU2", "cf",
         "hDD00", "hDD01", "hDD02", "hDD11", "hDD12", "hDD22", "lambdaU0", "lambdaU1", "lambdaU2", "trK",
@@ -388,10 +388,9 @@ def grid_symbols(gp, gfs, need_ricci=True):
     """Symbol values at interior points from FD of a (24, n2, n1, n0) array."""
     S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
     f = {n: gfs[GF[n]] for n in EVOL}
-    qf = hatted(gp)
     g = gp.NGHOSTS
-    # hatted arrays are (tensor..., n1, n0): trim to the interior, add an i2 axis
-    q = {k: a[..., None, g:-g, g:-g] for k, a in qf.items()}
+    # hatted arrays broadcast over the interior (an i2 or i1 axis of length 1)
+    q = hatted_grid(gp, interior=True)
     v = {}
 
     def t2(base):
@@ -522,15 +521,14 @@ def momentum_grid(gp, gfs, T4UU10=None):
 
 def enforce_detgammabar(gp, gfs):
     """Enforce_Detgammabar_Constraint.py:42-50 at ALL points (in place copy)."""
-    qf = hatted(gp)
+    qf = hatted_grid(gp)
     out = gfs.copy()
     h = np.empty((3, 3) + gp.shape)
     for (i, j) in SYM:
         h[i, j] = h[j, i] = gfs[GF["hDD%d%d" % (i, j)]]
-    ReDD = qf["ReDD"][:, :, None]
-    gbar = h * ReDD + qf["ghatDD"][:, :, None]
+    gbar = h * qf["ReDD"] + qf["ghatDD"]
     _, det = inv3(gbar)
-    fac = np.cbrt(np.abs(qf["detgammahat"][None]) / det)
+    fac = np.cbrt(np.abs(qf["detgammahat"]) / det)
     for (i, j) in SYM:
         d = 1.0 if i == j else 0.0
         out[GF["hDD%d%d" % (i, j)]] = fac * (d + h[i, j]) - d

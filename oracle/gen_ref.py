@@ -42,6 +42,7 @@ CONFIGS = {
     "bssn_sinhsph_fd4": ("BSSN", "SinhSpherical", 4, 3),
     "bssn_sph_fd4": ("BSSN", "Spherical", 4, 3),
     "bssn_sinhv2_fd4": ("BSSN", "SinhSphericalv2", 4, 3),
+    "bssn_sinhcyl_fd4": ("BSSN", "SinhCylindrical", 4, 3),
     "bssn_cart_fd4": ("BSSN", "Cartesian", 4, 3),
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
     "bssn_cart_fd2": ("BSSN", "Cartesian", 2, 2),
@@ -56,6 +57,8 @@ CONFIGS = {
     "sw_sinhsph_fd4": ("ScalarWave", "SinhSpherical", 4, 2),
     "maxwell_cart_fd4": ("Maxwell", "Cartesian", 4, 3),
     "maxwell_curvi_sinhsph_fd4": ("MaxwellCurvi", "SinhSpherical", 4, 3),
+    "maxwell_curvi_sinhcyl_fd4": ("MaxwellCurvi", "SinhCylindrical", 4, 3),
+    "sw_sinhcyl_fd4": ("ScalarWave", "SinhCylindrical", 4, 2),
 }
 
 WORKER = r'''

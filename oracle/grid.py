@@ -5,11 +5,13 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 - `GridParams` restates reference_metric.py:1330-1395
   (set_Nxx_dxx_invdx_params__and__xx): domain per CoordSystem
   (Spherical :106-108, SinhSpherical :118-120, SinhSphericalv2 :137-138,
-  Cartesian :400-403),
+  Cylindrical :233-234, SinhCylindrical :246-247, Cartesian :400-403),
   dxx = (xxmax - xxmin)/Nxx, cell-centred xx[j] = xxmin + (j - NGHOSTS + 1/2) dxx.
 - `hatted` restates reference_metric.py:487-601: for orthogonal scale factors
   s_i (reference_metric.py:168-175: s0 = dr/dxx0, s1 = r, s2 = r sin(xx1);
-  r(xx0) of :111, :125-126 and :142-143; Cartesian s_i = 1) it returns ReU, ReDD, ghat and their first and second
+  r(xx0) of :111, :125-126 and :142-143; :289-291 for the Cylindrical family:
+  s0 = drho/dxx0, s1 = rho, s2 = dz/dxx2 with rho(xx0), z(xx2) of :237-239,
+  :255-258; Cartesian s_i = 1) it returns ReU, ReDD, ghat and their first and second
   derivatives, GammahatUDD and its derivatives, det(ghat) and derivatives.
   Where the reference differentiates symbolically, here the derivatives of
   s_i are written in closed form and propagated by the product/quotient
@@ -18,8 +20,29 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 """
 import numpy as np
 
-CART, SPH, SINHSPH, SINHSPHV2 = 0, 1, 2, 3
-NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH, "SinhSphericalv2": SINHSPHV2}
+CART, SPH, SINHSPH, SINHSPHV2, CYL, SINHCYL = 0, 1, 2, 3, 4, 5
+NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH, "SinhSphericalv2": SINHSPHV2,
+         "Cylindrical": CYL, "SinhCylindrical": SINHCYL}
+
+
+def cylindrical(cs):
+    return cs in (CYL, SINHCYL)
+
+
+def sinh_map(A, w, x):
+    """A sinh(x/w) / sinh(1/w) and its derivative, with exponentials as
+    reference_metric.py:125-126, 255-258 write them."""
+    x = np.asarray(x, dtype=float)
+    den = np.exp(1.0 / w) - np.exp(-1.0 / w)
+    return A * (np.exp(x / w) - np.exp(-x / w)) / den, A * (np.exp(x / w) + np.exp(-x / w)) / (w * den)
+
+
+def cylinder_maps(gp, x0, x2):
+    """(rho, drho/dxx0), (z, dz/dxx2) of the Cylindrical family."""
+    if gp.CoordSystem == SINHCYL:
+        return sinh_map(gp.AMPLRHO, gp.SINHWRHO, x0), sinh_map(gp.AMPLZ, gp.SINHWZ, x2)
+    x0, x2 = np.asarray(x0, dtype=float), np.asarray(x2, dtype=float)
+    return (x0, np.ones_like(x0)), (x2, np.ones_like(x2))
 
 
 def radial(cs, x0, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
@@ -43,20 +66,28 @@ def radial(cs, x0, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
 
 class GridParams:
     def __init__(self, CoordSystem, Nxx, NGHOSTS, FD_order=4, AMPL=10.0, SINHW=0.2, RMAX=10.0,
-                 domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, const_dr=0.0625):
+                 domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, const_dr=0.0625, RHOMAX=10.0,
+                 ZMIN=-10.0, ZMAX=10.0, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2):
         cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
         self.CoordSystem = cs
         self.FD_order = FD_order
         self.NGHOSTS = NGHOSTS
         self.AMPL, self.SINHW, self.RMAX = AMPL, SINHW, RMAX
         self.const_dr = const_dr
+        self.RHOMAX, self.ZMIN, self.ZMAX = RHOMAX, ZMIN, ZMAX
+        self.AMPLRHO, self.SINHWRHO, self.AMPLZ, self.SINHWZ = AMPLRHO, SINHWRHO, AMPLZ, SINHWZ
         self.eta, self.wavespeed = eta, wavespeed
         self.Nxx = [int(n) for n in Nxx]
         self.np = [n + 2 * NGHOSTS for n in self.Nxx]
         ecs = SPH if (EigenCoord and cs in (SINHSPH, SINHSPHV2)) else cs
+        ecs = CYL if (EigenCoord and cs == SINHCYL) else ecs
         if ecs == CART:
             lo, hi = domain
             self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
+        elif ecs == CYL:
+            self.xxmin, self.xxmax = [0.0, -np.pi, ZMIN], [RHOMAX, np.pi, ZMAX]
+        elif ecs == SINHCYL:
+            self.xxmin, self.xxmax = [0.0, -np.pi, -1.0], [1.0, np.pi, 1.0]
         else:
             self.xxmin = [0.0, 0.0, -np.pi]
             self.xxmax = [RMAX if ecs == SPH else 1.0, np.pi, np.pi]
@@ -73,15 +104,28 @@ class GridParams:
         return f[..., g:-g, g:-g, g:-g]
 
 
-def scale_factors(gp, xx0, xx1):
-    """s[i], ds[i][k], dds[i][k][l] as arrays broadcast over (xx1, xx0)."""
-    x0, x1 = np.meshgrid(xx0, xx1)  # shape (n1, n0)
+def scale_factors(gp, xx0, xxB):
+    """s[i], ds[i][k], dds[i][k][l] as arrays broadcast over (xxB, xx0), xxB
+    the second coordinate the metric depends on: xx1 (Spherical family) or
+    xx2 (Cylindrical family)."""
+    x0, x1 = np.meshgrid(xx0, xxB)  # shape (nB, n0)
     z = np.zeros_like(x0)
     one = np.ones_like(x0)
     s = [one.copy(), one.copy(), one.copy()]
     ds = [[z.copy() for _ in range(3)] for _ in range(3)]
     dds = [[[z.copy() for _ in range(3)] for _ in range(3)] for _ in range(3)]
     if gp.CoordSystem == CART:
+        return s, ds, dds
+    if cylindrical(gp.CoordSystem):
+        (rho, rho1), (zz, z1) = cylinder_maps(gp, x0, x1)
+        if gp.CoordSystem == SINHCYL:
+            rho2, rho3 = rho / gp.SINHWRHO ** 2, rho1 / gp.SINHWRHO ** 2
+            z2, z3 = zz / gp.SINHWZ ** 2, z1 / gp.SINHWZ ** 2
+        else:
+            rho2 = rho3 = z2 = z3 = z
+        s = [rho1, rho, z1]
+        ds[0][0], ds[1][0], ds[2][2] = rho2, rho1, z2
+        dds[0][0][0], dds[1][0][0], dds[2][2][2] = rho3, rho2, z3
         return s, ds, dds
     if gp.CoordSystem in (SINHSPH, SINHSPHV2):
         A, w = gp.AMPL, gp.SINHW
@@ -110,20 +154,42 @@ def scale_factors(gp, xx0, xx1):
 
 
 def hatted(gp):
-    """Hatted quantities on the (n1, n0) plane; tensors indexed first."""
-    return hatted_from_scale_factors(*scale_factors(gp, gp.xx[0], gp.xx[1]))
+    """Hatted quantities on the (nB, n0) plane of the metric's coordinates
+    (nB = n1, or n2 for the Cylindrical family); tensors indexed first."""
+    xxB = gp.xx[2] if cylindrical(gp.CoordSystem) else gp.xx[1]
+    return hatted_from_scale_factors(*scale_factors(gp, gp.xx[0], xxB))
+
+
+def hatted_grid(gp, interior=False):
+    """Hatted quantities broadcastable over (n2, n1, n0) grid arrays (or,
+    with interior=True, over interior arrays): shape (tensor..., 1, n1, n0),
+    or (tensor..., n2, 1, n0) for the Cylindrical family."""
+    g = gp.NGHOSTS
+    cyl = cylindrical(gp.CoordSystem)
+    out = {}
+    for k, a in hatted(gp).items():
+        a = a[..., :, None, :] if cyl else a[..., None, :, :]
+        if interior:
+            a = a[..., g:-g, :, g:-g] if cyl else a[..., :, g:-g, g:-g]
+        out[k] = a
+    return out
 
 
 class _PointParams:
-    def __init__(self, cs, AMPL, SINHW, const_dr):
-        self.CoordSystem, self.AMPL, self.SINHW, self.const_dr = cs, AMPL, SINHW, const_dr
+    def __init__(self, cs, **kw):
+        self.CoordSystem = cs
+        for k, v in dict(AMPL=10.0, SINHW=0.2, const_dr=0.0625, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0,
+                         SINHWZ=0.2).items():
+            setattr(self, k, kw.get(k, v))
 
 
-def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
-    """Hatted quantities at one point (xx0, xx1): arrays with point shape (1, 1)."""
+def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2, const_dr=0.0625, xx2=0.0, **cyl):
+    """Hatted quantities at one point (xx0, xx1, xx2): arrays with point shape
+    (1, 1).  cyl: AMPLRHO, SINHWRHO, AMPLZ, SINHWZ of SinhCylindrical."""
     cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else CoordSystem
-    return hatted_from_scale_factors(*scale_factors(_PointParams(cs, AMPL, SINHW, const_dr),
-                                                    np.array([xx0]), np.array([xx1])))
+    xxB = xx2 if cylindrical(cs) else xx1
+    return hatted_from_scale_factors(*scale_factors(_PointParams(cs, AMPL=AMPL, SINHW=SINHW, const_dr=const_dr,
+                                                                 **cyl), np.array([xx0]), np.array([xxB])))
 
 
 def hatted_from_scale_factors(s, ds, dds):
@@ -184,6 +250,7 @@ def hatted_from_scale_factors(s, ds, dds):
 def find_timestep(gp, CFL_FACTOR):
     """CFL * min over interior points of dxx_i * s_i / wavespeed."""
     g = gp.NGHOSTS
-    s, _, _ = scale_factors(gp, gp.xx[0][g:-g], gp.xx[1][g:-g])
+    xxB = gp.xx[2] if cylindrical(gp.CoordSystem) else gp.xx[1]
+    s, _, _ = scale_factors(gp, gp.xx[0][g:-g], xxB[g:-g])
     dsmin = min(float(np.min(gp.dxx[d] * s[d])) for d in range(3))
     return dsmin * CFL_FACTOR / gp.wavespeed

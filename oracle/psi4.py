@@ -30,7 +30,7 @@ import numpy as np
 
 from .bssn import GF, R3, SYM, inv3
 from .fd import Stencils
-from .grid import CART, SPH, hatted, radial
+from .grid import CART, SPH, cylinder_maps, cylindrical, hatted_grid, radial
 
 ISQRT2 = 0.707106781186547524400844362104849039
 
@@ -150,15 +150,23 @@ def psi4_parts(adm, n4U, mre4U, mim4U):
     return re, im
 
 
-def cart_and_jacobian(cs, xx0, xx1, xx2, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
+def cart_and_jacobian(cs, xx0, xx1, xx2, AMPL=10.0, SINHW=0.2, const_dr=0.0625, cyl=None):
     """xx_to_Cart (reference_metric.py: Spherical :159-161, SinhSpherical
-    and SinhSphericalv2 :210-212 with their r(xx0), Cartesian identity) and
-    the Jacobian d x_Cart^i / d xx^j."""
+    and SinhSphericalv2 :210-212 with their r(xx0), the Cylindrical family
+    :296-298 (cyl: a GridParams carrying its parameters), Cartesian identity)
+    and the Jacobian d x_Cart^i / d xx^j."""
     xx0, xx1, xx2 = np.broadcast_arrays(*(np.asarray(a, dtype=float) for a in (xx0, xx1, xx2)))
     if cs == CART:
         one, zero = np.ones_like(xx0), np.zeros_like(xx0)
         J = np.array([[one, zero, zero], [zero, one, zero], [zero, zero, one]])
         return np.array([xx0, xx1, xx2]), J
+    if cylindrical(cs):  # (rho cos phi, rho sin phi, z), reference_metric.py:296-298
+        (rho, drho), (z, dz) = cylinder_maps(cyl, xx0, xx2)
+        sp_, cp = np.sin(xx1), np.cos(xx1)
+        zero = np.zeros_like(rho)
+        x = np.array([rho * cp, rho * sp_, z])
+        J = np.array([[drho * cp, -rho * sp_, zero], [drho * sp_, rho * cp, zero], [zero, zero, dz]])
+        return x, J
     r, drdx = radial(cs, xx0, AMPL, SINHW, const_dr)
     st, ct, sp_, cp = np.sin(xx1), np.cos(xx1), np.sin(xx2), np.cos(xx2)
     x = np.array([r * st * cp, r * st * sp_, r * ct])
@@ -184,10 +192,10 @@ def _inv_general(J):
     return c / det
 
 
-def tetrad(gammaDD, cs, xx0, xx1, xx2, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
+def tetrad(gammaDD, cs, xx0, xx1, xx2, AMPL=10.0, SINHW=0.2, const_dr=0.0625, cyl=None):
     """Psi4_tetrads.py:50-193 (QuasiKinnersley, UseCorrectUnitNormal False):
     returns l4U, n4U, mre4U, mim4U (lists of 4 arrays)."""
-    x, J = cart_and_jacobian(cs, xx0, xx1, xx2, AMPL, SINHW, const_dr)
+    x, J = cart_and_jacobian(cs, xx0, xx1, xx2, AMPL, SINHW, const_dr, cyl)
     Ji = _inv_general(J)
     gUU, detg = inv3(gammaDD)
     v1C = [-x[1], x[0], np.zeros_like(x[0])]
@@ -240,8 +248,7 @@ def psi4_grid(gp, gfs, i0_range=None):
     S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
     g = gp.NGHOSTS
     f = {n: gfs[GF[n]] for n in GF}
-    qf = hatted(gp)
-    q = {k: a[..., None, g:-g, g:-g] for k, a in qf.items()}
+    q = hatted_grid(gp, interior=True)
     shp = (gp.Nxx[2], gp.Nxx[1], gp.Nxx[0])
     v = {}
 
@@ -271,7 +278,7 @@ def psi4_grid(gp, gfs, i0_range=None):
         v["cf_dDD"][k, l] = v["cf_dDD"][l, k] = S.d11(f["cf"], k, l)
     adm = adm_from_bssn(v, q)
     X2, X1, X0 = np.meshgrid(gp.xx[2][g:-g], gp.xx[1][g:-g], gp.xx[0][g:-g], indexing="ij")
-    _, n4, mre, mim = tetrad(adm["gammaDD"], gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW, gp.const_dr)
+    _, n4, mre, mim = tetrad(adm["gammaDD"], gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW, gp.const_dr, gp)
     re, im = psi4_parts(adm, n4, mre, mim)
     out = np.zeros((2,) + gp.shape)
     gp.interior(out[0])[...] = re[0] + re[1] + re[2]

@@ -10,7 +10,7 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 import numpy as np
 
 from .fd import Stencils
-from .grid import CART, hatted, radial
+from .grid import CART, hatted_grid, radial
 
 
 def scalarwave_rhs_grid(gp, gfs):
@@ -23,7 +23,7 @@ def scalarwave_rhs_grid(gp, gfs):
         rhs_v = c2 * lap
     else:
         g = gp.NGHOSTS
-        q = {k: a[..., None, g:-g, g:-g] for k, a in hatted(gp).items()}
+        q = hatted_grid(gp, interior=True)
         gUU, G = q["ghatUU"], q["GammahatUDD"]
         contracted = np.einsum("ij...,kij...->k...", gUU, G)
         acc = 0.0
@@ -149,6 +149,9 @@ def scalarwave_id_grid(gp, kind, t=0.0, k=(1.0, 1.0, 1.0), sigma=3.0):
     X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
     if gp.CoordSystem == 0:
         x, y, z = X0, X1, X2
+    elif gp.CoordSystem in (4, 5):  # Cylindrical family
+        from .psi4 import cart_and_jacobian
+        (x, y, z), _ = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, cyl=gp)
     else:
         r, _ = radial(gp.CoordSystem, X0, gp.AMPL, gp.SINHW, gp.const_dr)
         x, y, z = r * np.sin(X1) * np.cos(X2), r * np.sin(X1) * np.sin(X2), r * np.cos(X1)
@@ -210,7 +213,7 @@ def maxwell_curvi_pointwise(v, q):
 def _mc_symbols(gp, gfs):
     S = Stencils(gp.FD_order, gp.NGHOSTS, gp.invdx)
     g = gp.NGHOSTS
-    q = {k: a[..., None, g:-g, g:-g] for k, a in hatted(gp).items()}
+    q = hatted_grid(gp, interior=True)
     f = {n: gfs[i] for i, n in enumerate(MC_GFS)}
     v = {"aU": np.array([S.interior(f["aU%d" % i]) for i in range(3)]),
          "eU": np.array([S.interior(f["eU%d" % i]) for i in range(3)]),
@@ -255,7 +258,7 @@ def maxwell_curvi_toroidal_dipole(gp, t, amp=1.0, lam=1.0):
     xx_to_Cart and divided by ReU."""
     from .psi4 import _inv_general, cart_and_jacobian
     X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
-    xyz, J = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW, gp.const_dr)
+    xyz, J = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, gp.AMPL, gp.SINHW, gp.const_dr, gp)
     x, y, z = xyz
     r = np.sqrt(x * x + y * y + z * z)
     u, vv = t + r, t - r
@@ -266,8 +269,7 @@ def maxwell_curvi_toroidal_dipole(gp, t, amp=1.0, lam=1.0):
     Ac = [-y * F, x * F, 0.0 * x]
     Ec = [y * dF, -x * dF, 0.0 * x]
     Ji = _inv_general(J)
-    qf = hatted(gp)
-    ReU = qf["ReU"][:, None]  # (3, 1, n1, n0)
+    ReU = hatted_grid(gp)["ReU"]  # (3, 1, n1, n0), or (3, n2, 1, n0) for the Cylindrical family
     out = np.zeros((8,) + gp.shape)
     for i in range(3):
         out[1 + i] = sum(Ji[i, j] * Ac[j] for j in range(3)) / ReU[i]

@@ -70,6 +70,9 @@ FIXTURE_GRIDS = {
     "bssn_ko_cart_fd2": ("Cartesian", (6, 6, 6), 2, 2, 25),
     "bssn_ko_cart_fd8": ("Cartesian", (6, 6, 6), 8, 5, 26),
     "bssn_sinhv2_fd4": ("SinhSphericalv2", (8, 6, 4), 4, 3, 27),
+    "bssn_sinhcyl_fd4": ("SinhCylindrical", (8, 6, 6), 4, 3, 28),
+    "maxwell_curvi_sinhcyl_fd4": ("SinhCylindrical", (8, 6, 6), 4, 3, 29),
+    "sw_sinhcyl_fd4": ("SinhCylindrical", (8, 6, 6), 4, 2, 30),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -322,7 +325,7 @@ TRUSTED += [
      _RFM_INIT, "M.BSSN_source_terms_for_BSSN_RHSs()",
      ["sourceterm_trK_rhs", "sourceterm_a_rhsDD", "sourceterm_lambda_rhsU", "sourceterm_Lambdabar_rhsU"]),
 ]
-for cs in ("Spherical", "SinhSpherical", "SinhSphericalv2", "Cartesian"):
+for cs in ("Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical", "Cartesian"):
     TRUSTED.append(("rfm_" + cs, "tests", "rfm_%s__reference_metric__True__globals" % cs,
                     "import NRPy_param_funcs as par\n"
                     "import reference_metric as M\n"

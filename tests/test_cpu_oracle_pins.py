@@ -279,11 +279,13 @@ def test_trusted_maxwell_system_I():
     assert close(float(C[0]), ex["C"], 1e-13)
 
 
-@pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cartesian"])
+@pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
+                                "Cartesian"])
 def test_trusted_reference_metric(cs):
     inp = TV["rfm_" + cs]["inputs"]
+    cyl = {k: inp[k] for k in ("AMPLRHO", "SINHWRHO", "AMPLZ", "SINHWZ") if k in inp}
     q = og.hatted_at(cs, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("AMPL", 10.0), inp.get("SINHW", 0.2),
-                     inp.get("const_dr", 0.0625))
+                     inp.get("const_dr", 0.0625), xx2=inp.get("xx2", 0.0), **cyl)
     n = 0
     for k, want in expect("rfm_" + cs).items():
         base, _, rest = k.partition("[")
@@ -298,7 +300,7 @@ def test_trusted_reference_metric(cs):
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
         "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical",
-        "bssn_sinhv2_fd4": "SinhSphericalv2"}
+        "bssn_sinhv2_fd4": "SinhSphericalv2", "bssn_sinhcyl_fd4": "SinhCylindrical"}
 
 
 @pytest.mark.parametrize("cfg", sorted(CFGS))
@@ -396,6 +398,9 @@ def test_oracle_swsh_matches_reference_generated_c():
                                           ("sw_sinhsph_fd4", "SinhSpherical", ow.scalarwave_rhs_grid, 2),
                                           ("maxwell_cart_fd4", "Cartesian", ow.maxwell_rhs_grid, 7),
                                           ("maxwell_curvi_sinhsph_fd4", "SinhSpherical", ow.maxwell_curvi_rhs_grid,
+                                           8),
+                                          ("sw_sinhcyl_fd4", "SinhCylindrical", ow.scalarwave_rhs_grid, 2),
+                                          ("maxwell_curvi_sinhcyl_fd4", "SinhCylindrical", ow.maxwell_curvi_rhs_grid,
                                            8)])
 def test_oracle_matches_reference_generated_wave_maxwell(cfg, cs, fn, ngf):
     z = np.load(os.path.join(GOLD, "ref_%s.npz" % cfg))

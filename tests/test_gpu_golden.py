@@ -16,7 +16,7 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
         "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical",
-        "bssn_sinhv2_fd4": "SinhSphericalv2"}
+        "bssn_sinhv2_fd4": "SinhSphericalv2", "bssn_sinhcyl_fd4": "SinhCylindrical"}
 TOL = 1e-12
 
 
@@ -131,7 +131,10 @@ def test_brill_lindquist_matches_reference_initial_data(cuda, cfg):
 
 @pytest.mark.parametrize("cfg,cs,system,ngf", [("sw_cart_fd4", "Cartesian", "ScalarWave", 2),
                                               ("sw_sinhsph_fd4", "SinhSpherical", "ScalarWave", 2),
-                                              ("maxwell_cart_fd4", "Cartesian", "Maxwell", 7)])
+                                              ("maxwell_cart_fd4", "Cartesian", "Maxwell", 7),
+                                              ("sw_sinhcyl_fd4", "SinhCylindrical", "ScalarWave", 2),
+                                              ("maxwell_curvi_sinhcyl_fd4", "SinhCylindrical", "MaxwellCurvilinear",
+                                               8)])
 def test_wave_maxwell_match_reference_generated_c(cuda, cfg, cs, system, ngf):
     import torch
     from nrpytutorial_gb300 import Evolution

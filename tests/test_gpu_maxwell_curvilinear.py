@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0))
 CASES = [("Cartesian", (8, 8, 8), 4), ("Spherical", (10, 8, 6), 2), ("Spherical", (10, 8, 6), 4),
-         ("SinhSpherical", (10, 8, 8), 4), ("SinhSphericalv2", (10, 8, 8), 4)]
+         ("SinhSpherical", (10, 8, 8), 4), ("SinhSphericalv2", (10, 8, 8), 4), ("SinhCylindrical", (10, 8, 8), 4),
+         ("Cylindrical", (8, 6, 8), 2)]
 PARITY = [0, 1, 2, 3, 1, 2, 3, 0]
 
 
@@ -71,7 +72,8 @@ def test_constraints_match_oracle(cuda, coord, Nxx, order):
     assert per_gf_rel(got, ow.maxwell_curvi_constraints_grid(gp, f), gp.NGHOSTS) < 1e-12
 
 
-@pytest.mark.parametrize("coord", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2"])
+@pytest.mark.parametrize("coord", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical",
+                                   "SinhCylindrical"])
 def test_toroidal_dipole_data_match_oracle(cuda, coord):
     ev, gp = _evo(cuda, coord, (10, 8, 6), 4)
     ev.initial_data_toroidal_dipole(1.2, 0.9, 0.3)
