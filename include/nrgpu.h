@@ -55,6 +55,8 @@ extern "C" {
 #define NRGPU_COORD_CYLINDRICAL      4  /* rho = xx0, z = xx2                                 */
 #define NRGPU_COORD_SINHCYLINDRICAL  5  /* rho = AMPLRHO sinh(xx0/SINHWRHO)/sinh(1/SINHWRHO),
                                            z = AMPLZ sinh(xx2/SINHWZ)/sinh(1/SINHWZ)       */
+#define NRGPU_COORD_SINHCYLINDRICALV2 6 /* adds AMPLRHO const_drho xx0 to rho and
+                                           AMPLZ const_dz xx2 to z (:265-275)               */
 
 /* ------------------------------------------------------------- systems */
 #define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
@@ -101,6 +103,7 @@ typedef struct paramstruct {
   double const_dr;                    /* SinhSphericalv2 (reference_metric.py:141) */
   double RHOMAX, ZMIN, ZMAX;          /* Cylindrical (reference_metric.py:233)     */
   double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  /* SinhCylindrical (:249-251)          */
+  double const_drho, const_dz;        /* SinhCylindricalv2 (reference_metric.py:271) */
 } paramstruct;
 
 /*

@@ -281,9 +281,10 @@ __global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gf
   } else if (cylindrical_family(p.CoordSystem)) {
     // (rho cos phi, rho sin phi, z) (reference_metric.py:296-298)
     Dual rho = X0, drho = dconst(1.0), z = X2, dz = dconst(1.0);
-    if (p.CoordSystem == NRGPU_COORD_SINHCYLINDRICAL) {
-      dsinh_map(p.AMPLRHO, p.SINHWRHO, 0.0, X0, rho, drho);
-      dsinh_map(p.AMPLZ, p.SINHWZ, 0.0, X2, z, dz);
+    if (p.CoordSystem != NRGPU_COORD_CYLINDRICAL) {
+      const bool v2 = p.CoordSystem == NRGPU_COORD_SINHCYLINDRICALV2;
+      dsinh_map(p.AMPLRHO, p.SINHWRHO, v2 ? p.const_drho : 0.0, X0, rho, drho);
+      dsinh_map(p.AMPLZ, p.SINHWZ, v2 ? p.const_dz : 0.0, X2, z, dz);
     }
     const Dual sp = dsin(X1), cp = dcos(X1);
     xc[0] = rho * cp; xc[1] = rho * sp; xc[2] = z;
@@ -595,6 +596,7 @@ int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *
       break;
     case NRGPU_COORD_CYLINDRICAL:
     case NRGPU_COORD_SINHCYLINDRICAL:
+    case NRGPU_COORD_SINHCYLINDRICALV2:
       constraint_sources_kernel<NRGPU_COORD_SINHCYLINDRICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU,
                                                                                               H, MU);
       break;

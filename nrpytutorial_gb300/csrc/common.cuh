@@ -63,8 +63,8 @@ struct Grid {
 // the runtime CoordSystem carry the values.
 inline int dispatch_cs(int cs) {
   return cs == NRGPU_COORD_SINHSPHERICALV2 ? NRGPU_COORD_SINHSPHERICAL
-         : cs == NRGPU_COORD_CYLINDRICAL   ? NRGPU_COORD_SINHCYLINDRICAL
-                                           : cs;
+         : (cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICALV2) ? NRGPU_COORD_SINHCYLINDRICAL
+                                                                                   : cs;
 }
 
 inline Grid make_grid(const paramstruct *p) {

@@ -29,7 +29,7 @@ void count_launch(int n) { g_launches += n; }
 
 int check_params(const paramstruct *p) {
   NRGPU_REQUIRE(p != nullptr, "params is NULL");
-  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 5, "unknown CoordSystem %d", p->CoordSystem);
+  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 6, "unknown CoordSystem %d", p->CoordSystem);
   NRGPU_REQUIRE(p->FD_order == 2 || p->FD_order == 4 || p->FD_order == 6 || p->FD_order == 8,
                 "FD_order %d not in {2,4,6,8}", p->FD_order);
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 && p->NGHOSTS <= NRGPU_MAX_GHOSTS,

@@ -44,7 +44,7 @@ constexpr int NQ = 403;
 
 // ------------------------------------------------------- dependency masks
 __host__ __device__ constexpr bool cylindrical_family(int cs) {
-  return cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICAL;
+  return cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICALV2;
 }
 
 // dep(CS, i, k): does scale factor s_i depend on xx_k?
@@ -162,10 +162,12 @@ struct CoordParams {
   int cs;
   double AMPL, SINHW, const_dr;             // Spherical family
   double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  // SinhCylindrical
+  double const_drho, const_dz;              // SinhCylindricalv2
 };
 
 __host__ __device__ inline CoordParams coord_params(const paramstruct &p) {
-  return CoordParams{p.CoordSystem, p.AMPL, p.SINHW, p.const_dr, p.AMPLRHO, p.SINHWRHO, p.AMPLZ, p.SINHWZ};
+  return CoordParams{p.CoordSystem, p.AMPL,  p.SINHW,  p.const_dr,   p.AMPLRHO,
+                     p.SINHWRHO,    p.AMPLZ, p.SINHWZ, p.const_drho, p.const_dz};
 }
 
 __host__ __device__ inline bool spherical_family(int cs) {
@@ -199,12 +201,13 @@ __host__ __device__ inline void radial_map(const CoordParams &c, double x, doubl
 
 // Cylindrical family: rho(xx0) and z(xx2) with three derivatives each
 // (Cylindrical: the identity, reference_metric.py:237-239; SinhCylindrical:
-// sinh maps, :255-258).
+// sinh maps, :255-258; SinhCylindricalv2 adds the linear terms, :273-275).
 __host__ __device__ inline void cylinder_maps(const CoordParams &c, double x0, double x2, double rho[4],
                                               double z[4]) {
-  if (c.cs == NRGPU_COORD_SINHCYLINDRICAL) {
-    sinh_map(c.AMPLRHO, c.SINHWRHO, 0.0, x0, rho);
-    sinh_map(c.AMPLZ, c.SINHWZ, 0.0, x2, z);
+  if (c.cs == NRGPU_COORD_SINHCYLINDRICAL || c.cs == NRGPU_COORD_SINHCYLINDRICALV2) {
+    const bool v2 = c.cs == NRGPU_COORD_SINHCYLINDRICALV2;
+    sinh_map(c.AMPLRHO, c.SINHWRHO, v2 ? c.const_drho : 0.0, x0, rho);
+    sinh_map(c.AMPLZ, c.SINHWZ, v2 ? c.const_dz : 0.0, x2, z);
   } else {
     rho[0] = x0; rho[1] = 1.0; rho[2] = rho[3] = 0.0;
     z[0] = x2; z[1] = 1.0; z[2] = z[3] = 0.0;

@@ -20,13 +20,13 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 """
 import numpy as np
 
-CART, SPH, SINHSPH, SINHSPHV2, CYL, SINHCYL = 0, 1, 2, 3, 4, 5
+CART, SPH, SINHSPH, SINHSPHV2, CYL, SINHCYL, SINHCYLV2 = 0, 1, 2, 3, 4, 5, 6
 NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH, "SinhSphericalv2": SINHSPHV2,
-         "Cylindrical": CYL, "SinhCylindrical": SINHCYL}
+         "Cylindrical": CYL, "SinhCylindrical": SINHCYL, "SinhCylindricalv2": SINHCYLV2}
 
 
 def cylindrical(cs):
-    return cs in (CYL, SINHCYL)
+    return cs in (CYL, SINHCYL, SINHCYLV2)
 
 
 def sinh_map(A, w, x):
@@ -38,9 +38,15 @@ def sinh_map(A, w, x):
 
 
 def cylinder_maps(gp, x0, x2):
-    """(rho, drho/dxx0), (z, dz/dxx2) of the Cylindrical family."""
-    if gp.CoordSystem == SINHCYL:
-        return sinh_map(gp.AMPLRHO, gp.SINHWRHO, x0), sinh_map(gp.AMPLZ, gp.SINHWZ, x2)
+    """(rho, drho/dxx0), (z, dz/dxx2) of the Cylindrical family
+    (SinhCylindricalv2 adds AMPLRHO const_drho xx0 and AMPLZ const_dz xx2,
+    reference_metric.py:273-275)."""
+    if gp.CoordSystem in (SINHCYL, SINHCYLV2):
+        (r, dr), (z, dz) = sinh_map(gp.AMPLRHO, gp.SINHWRHO, x0), sinh_map(gp.AMPLZ, gp.SINHWZ, x2)
+        if gp.CoordSystem == SINHCYLV2:
+            r, dr = r + gp.AMPLRHO * gp.const_drho * np.asarray(x0), dr + gp.AMPLRHO * gp.const_drho
+            z, dz = z + gp.AMPLZ * gp.const_dz * np.asarray(x2), dz + gp.AMPLZ * gp.const_dz
+        return (r, dr), (z, dz)
     x0, x2 = np.asarray(x0, dtype=float), np.asarray(x2, dtype=float)
     return (x0, np.ones_like(x0)), (x2, np.ones_like(x2))
 
@@ -67,7 +73,8 @@ def radial(cs, x0, AMPL=10.0, SINHW=0.2, const_dr=0.0625):
 class GridParams:
     def __init__(self, CoordSystem, Nxx, NGHOSTS, FD_order=4, AMPL=10.0, SINHW=0.2, RMAX=10.0,
                  domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, const_dr=0.0625, RHOMAX=10.0,
-                 ZMIN=-10.0, ZMAX=10.0, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2):
+                 ZMIN=-10.0, ZMAX=10.0, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2, const_drho=0.0625,
+                 const_dz=0.0625):
         cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
         self.CoordSystem = cs
         self.FD_order = FD_order
@@ -76,17 +83,18 @@ class GridParams:
         self.const_dr = const_dr
         self.RHOMAX, self.ZMIN, self.ZMAX = RHOMAX, ZMIN, ZMAX
         self.AMPLRHO, self.SINHWRHO, self.AMPLZ, self.SINHWZ = AMPLRHO, SINHWRHO, AMPLZ, SINHWZ
+        self.const_drho, self.const_dz = const_drho, const_dz
         self.eta, self.wavespeed = eta, wavespeed
         self.Nxx = [int(n) for n in Nxx]
         self.np = [n + 2 * NGHOSTS for n in self.Nxx]
         ecs = SPH if (EigenCoord and cs in (SINHSPH, SINHSPHV2)) else cs
-        ecs = CYL if (EigenCoord and cs == SINHCYL) else ecs
+        ecs = CYL if (EigenCoord and cs in (SINHCYL, SINHCYLV2)) else ecs
         if ecs == CART:
             lo, hi = domain
             self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
         elif ecs == CYL:
             self.xxmin, self.xxmax = [0.0, -np.pi, ZMIN], [RHOMAX, np.pi, ZMAX]
-        elif ecs == SINHCYL:
+        elif ecs in (SINHCYL, SINHCYLV2):
             self.xxmin, self.xxmax = [0.0, -np.pi, -1.0], [1.0, np.pi, 1.0]
         else:
             self.xxmin = [0.0, 0.0, -np.pi]
@@ -118,9 +126,11 @@ def scale_factors(gp, xx0, xxB):
         return s, ds, dds
     if cylindrical(gp.CoordSystem):
         (rho, rho1), (zz, z1) = cylinder_maps(gp, x0, x1)
-        if gp.CoordSystem == SINHCYL:
-            rho2, rho3 = rho / gp.SINHWRHO ** 2, rho1 / gp.SINHWRHO ** 2
-            z2, z3 = zz / gp.SINHWZ ** 2, z1 / gp.SINHWZ ** 2
+        if gp.CoordSystem in (SINHCYL, SINHCYLV2):
+            # second and third derivatives come from the sinh part alone
+            (sh, ch), (shz, chz) = sinh_map(gp.AMPLRHO, gp.SINHWRHO, x0), sinh_map(gp.AMPLZ, gp.SINHWZ, x1)
+            rho2, rho3 = sh / gp.SINHWRHO ** 2, ch / gp.SINHWRHO ** 2
+            z2, z3 = shz / gp.SINHWZ ** 2, chz / gp.SINHWZ ** 2
         else:
             rho2 = rho3 = z2 = z3 = z
         s = [rho1, rho, z1]
@@ -179,7 +189,7 @@ class _PointParams:
     def __init__(self, cs, **kw):
         self.CoordSystem = cs
         for k, v in dict(AMPL=10.0, SINHW=0.2, const_dr=0.0625, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0,
-                         SINHWZ=0.2).items():
+                         SINHWZ=0.2, const_drho=0.0625, const_dz=0.0625).items():
             setattr(self, k, kw.get(k, v))
 
 

@@ -18,7 +18,7 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0))
 CASES = [("Cartesian", (8, 8, 8), 4), ("Spherical", (10, 8, 6), 2), ("Spherical", (10, 8, 6), 4),
          ("SinhSpherical", (10, 8, 8), 4), ("SinhSphericalv2", (10, 8, 8), 4), ("SinhCylindrical", (10, 8, 8), 4),
-         ("Cylindrical", (8, 6, 8), 2)]
+         ("Cylindrical", (8, 6, 8), 2), ("SinhCylindricalv2", (8, 8, 6), 4)]
 PARITY = [0, 1, 2, 3, 1, 2, 3, 0]
 
 

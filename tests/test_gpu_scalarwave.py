@@ -35,7 +35,8 @@ def test_cartesian_rhs_matches_oracle(cuda, order):
     assert float(out[:, :gp.NGHOSTS].abs().max()) == 0.0
 
 
-@pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical"])
+@pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
+                                   "SinhCylindricalv2"])
 @pytest.mark.parametrize("order", [2, 4])
 def test_curvilinear_rhs_matches_oracle(cuda, coord, order):
     import torch
