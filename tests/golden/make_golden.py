@@ -25,6 +25,10 @@ Writes:
       run (Spherical 72x12x2 and 96x16x2, Brill-Lindquist, CFL 1, to
       t = 7.5) through the reference's generated kernels: the 72x12x2
       state and H of both runs at t_final (`evolve`).
+  ref_sw_planewave_sinhsph.npz  the reference's curvilinear ScalarWave
+      validation run (SinhSpherical 16x8x16 and 24x12x24, plane wave, CFL 1,
+      to t = 7) through the reference's generated rhs_eval: the 16x8x16
+      state and both runs' error norms at t_final (`evolve_sw`).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -189,6 +193,55 @@ def evolution():
             out["state_" + tag] = y[:, g:-g, g:-g, g:-g]
         print("evolved", tag, n_final, "steps, dt", dt)
     np.savez_compressed(os.path.join(HERE, "ref_bssn_bl_spherical_axisym.npz"), **out)
+
+
+# The reference's curvilinear ScalarWave validation run (Tutorial-Start_to_
+# Finish-ScalarWaveCurvilinear.ipynb:160-203, 641-648, 781-786): SinhSpherical
+# with domain_size 10 and sinh_width 0.4, FD4, RK4, CFL 1.0, quadratic-
+# extrapolation BCs, PlaneWave data (wavespeed 1, k = (1, 1, 1)), grids
+# 16x8x16 and 24x12x24 evolved to t_final = 0.7 domain_size.
+SW_EVOLVE = dict(AMPL=10.0, SINHW=0.4, CFL=1.0, t_final=7.0, grids=((16, 8, 16), (24, 12, 24)))
+
+
+def evolution_scalarwave():
+    """ref_sw_planewave_sinhsph.npz: the reference's generated rhs_eval
+    (strict build of sw_sinhsph_fd4) driven through the RK4 step and the
+    curvilinear BCs (oracle/bcs.py) from the PlaneWave data (oracle,
+    pinned to the reference's trusted values) for N_final =
+    int(t_final/dt + 0.5) steps: the 16x8x16 interior state at t_final and,
+    for both grids, the notebook's error norm sqrt(mean (u - u_exact)^2)
+    over interior points with r < 0.3 domain_size."""
+    import oracle.bcs as ob
+    import oracle.grid as og
+    import oracle.wave_maxwell as ow
+    from oracle.ref import RefKernels
+    out = {}
+    for N in SW_EVOLVE["grids"]:
+        gp = og.GridParams("SinhSpherical", N, 2, 4, AMPL=SW_EVOLVE["AMPL"], SINHW=SW_EVOLVE["SINHW"])
+        R = RefKernels("sw_sinhsph_fd4", gp, "strict", extra=dict(wavespeed=1.0))
+        layers = ob.build_bcstruct(gp)
+        y = ow.scalarwave_id_grid(gp, "PlaneWave", 0.0)
+        dt = og.find_timestep(gp, SW_EVOLVE["CFL"])
+        n_final = int(SW_EVOLVE["t_final"] / dt + 0.5)
+        k_odd = k_even = None
+        for _ in range(n_final):
+            y, k_odd, k_even = ob.rk4_step(y, dt, R.rhs_eval, lambda f: ob.apply_bcs(layers, f, [0, 0]),
+                                           gp.NGHOSTS, k_odd, k_even)
+        g = gp.NGHOSTS
+        tag = "%dx%dx%d" % N
+        exact = ow.scalarwave_id_grid(gp, "PlaneWave", n_final * dt)
+        X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
+        r = og.radial(gp.CoordSystem, X0, gp.AMPL, gp.SINHW)[0]
+        m = np.zeros(gp.shape, dtype=bool)
+        m[g:-g, g:-g, g:-g] = True
+        m &= r < 0.3 * SW_EVOLVE["AMPL"]
+        out["n_final_" + tag] = n_final
+        out["dt_" + tag] = dt
+        out["l2_error_" + tag] = float(np.sqrt(np.mean((y[0][m] - exact[0][m]) ** 2)))
+        if N == SW_EVOLVE["grids"][0]:
+            out["state_" + tag] = y[:, g:-g, g:-g, g:-g]
+        print("evolved", tag, n_final, "steps, dt", dt, "L2 error", out["l2_error_" + tag])
+    np.savez_compressed(os.path.join(HERE, "ref_sw_planewave_sinhsph.npz"), **out)
 
 
 FD_WORKER = r'''
@@ -396,7 +449,7 @@ def trusted(only=None):
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted", "evolve"]
+    what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted", "evolve", "evolve_sw"]
     if "senr" in what:
         senr_bc()
     if "ref" in what:
@@ -409,6 +462,8 @@ if __name__ == "__main__":
         trusted()
     if "evolve" in what:
         evolution()
+    if "evolve_sw" in what:
+        evolution_scalarwave()
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)
