@@ -141,3 +141,53 @@ def test_scalarwave_validation_run_matches_reference_generated_c(cuda, prec):
             assert rel < (1e-11 if prec == "fp64" else 1e-6)
     order = np.log(errs[0] / errs[1]) / np.log(1.5)
     assert 3.7 < order < 4.3, (errs, order)
+
+
+def test_maxwell_curvilinear_validation_run_converges(cuda):
+    """The reference's curvilinear Maxwell validation run
+    (Tutorial-Start_to_Finish-Solving_Maxwells_Equations_in_Vacuum-
+    Curvilinear.ipynb:153-194, 752-753, 819-823, 1342-1353): System II on
+    SinhCylindrical with AMPLRHO = AMPLZ = 10 (domain_size) and SINHWRHO =
+    SINHWZ = 0.4, FD4, RK4, CFL 0.5, Sommerfeld boundaries (FD4 d_r, falloff
+    power 3, speed 1), toroidal dipole amp = lam = 1, grids 50x4x100 and
+    80x4x160 to t = 0.5 domain_size.  The notebook validates convergence of
+    E^i and A^i to the exact solution; here the error in r < 4 (the pulse
+    has not reached the boundary region) falls at 4th order."""
+    import oracle.grid as og
+    from nrpytutorial_gb300 import Evolution, Grid, sommerfeld_params
+    sommerfeld_params(4, speed=[1.0] * 8, f_inf=[0.0] * 8, radial_falloff_power=[3.0] * 8)
+    try:
+        errs = _maxwell_runs(cuda, og, Evolution, Grid)
+    finally:
+        sommerfeld_params()  # the library's defaults again, for whatever runs next
+    order = np.log(errs[0] / errs[1]) / np.log(1.6)
+    print("Maxwell SinhCylindrical errors", errs, "order", order)
+    assert 3.5 < order < 4.6, (errs, order)
+
+
+def _maxwell_runs(cuda, og, Evolution, Grid):
+    import torch
+    kw = dict(AMPLRHO=10.0, SINHWRHO=0.4, AMPLZ=10.0, SINHWZ=0.4)
+    errs = []
+    for N in ((50, 4, 100), (80, 4, 160)):
+        G = Grid("SinhCylindrical", N, FD_order=4, NGHOSTS=3, **kw)
+        gp = og.GridParams("SinhCylindrical", N, 3, 4, **kw)
+        ev = Evolution("MaxwellCurvilinear", G, device=cuda, boundary="sommerfeld")
+        ev.initial_data_toroidal_dipole(1.0, 1.0, 0.0)
+        dt = G.find_timestep(0.5)
+        n = int(5.0 / dt + 0.5)
+        ev.capture(dt, n_steps=n)()
+        exact = torch.zeros_like(ev.y_n)
+        ev.initial_data_toroidal_dipole(1.0, 1.0, n * dt, gfs=exact)
+        torch.cuda.synchronize()
+        got, want = ev.y_n.cpu().numpy(), exact.cpu().numpy()
+        X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
+        (rho, _), (z, _) = og.cylinder_maps(gp, X0, X2)
+        g = 3
+        m = np.zeros(gp.shape, dtype=bool)
+        m[g:-g, g:-g, g:-g] = True
+        m &= np.sqrt(rho ** 2 + z ** 2) < 4.0
+        # a^i and e^i (gridfunctions 1-6), rescaled components
+        d = sum(np.mean((got[k][m] - want[k][m]) ** 2) for k in range(1, 7))
+        errs.append(float(np.sqrt(d)))
+    return errs
