@@ -227,20 +227,6 @@ __global__ void sw_batch_bc_levels_kernel(const BatchInstance *__restrict__ inst
   }
 }
 
-// Start of an FP32-stage step over all packed points: y_n split in place
-// into (hi, lo) pairs (the float-float accumulation state, and the
-// compensated substep-0 input), and for plain FP32 stages also y_n rounded
-// to FP32 into `f` (substep 0's input).
-template <bool ROUND>
-__global__ void sw_batch_prep_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const float2 p = split_pair_fast(y[i]);
-    if (ROUND) f[i] = p.x;
-    ((float2 *)y)[i] = p;
-  }
-}
-
 }  // namespace nrgpu
 
 using namespace nrgpu;
@@ -727,9 +713,9 @@ int nrgpu_batch_step(nrgpu_batch *b, MoL_gridfunctions *gfs) {
   if (!f64) {  // y_n -> pairs in place (+ FP32 copy in k_even for plain FP32 stages)
     const int blocks = (int)std::min<long long>((b->total_points + 255) / 256, 152LL * 16);
     if (pair)
-      sw_batch_prep_kernel<false><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs, nullptr);
+      split_state_kernel<false><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs, nullptr);
     else
-      sw_batch_prep_kernel<true><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs,
+      split_state_kernel<true><<<blocks, 256, 0, stream()>>>(b->total_points, gfs->y_n_gfs,
                                                                (float *)gfs->k_even_gfs);
     NRGPU_LAUNCH_CHECK();
   }

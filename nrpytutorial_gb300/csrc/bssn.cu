@@ -94,9 +94,9 @@ __global__ void enforce_kernel(Grid g, const double *__restrict__ tab, T *__rest
 // h'_ij = (f - 1) delta_ij + f h_ij.  About 48 significant bits.
 template <typename T>
 __global__ void enforce_ff_kernel(Grid g, T *__restrict__ gfs) {
-  const int i0 = blockIdx.x * blockDim.x + threadIdx.x, i1 = blockIdx.y, i2 = blockIdx.z;
-  if (i0 >= g.n0) return;
-  const long long idx = (long long)i0 + (long long)g.n0 * ((long long)i1 + (long long)g.n1 * i2);
+  // pointwise and coordinate-free: one thread per point of the flat grid
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= g.ntot) return;
   float2 h[6];
 #pragma unroll
   for (int s = 0; s < 6; s++) {
@@ -444,9 +444,10 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   Grid g = make_grid(p);
   dim3 block(64), grid((g.n0 + 63) / 64, g.n1, g.n2);
   if (!is_f64 || ff_f64) {  // FP32 storage (or the FP32-stage steps' FP64 state): float-float rescale
-    if (is_f64) enforce_ff_kernel<double><<<grid, block, 0, stream()>>>(g, (double *)gfs);
-    else if (pair) enforce_ff_kernel<float2><<<grid, block, 0, stream()>>>(g, (float2 *)gfs);
-    else enforce_ff_kernel<float><<<grid, block, 0, stream()>>>(g, (float *)gfs);
+    const dim3 fb(256), fg((unsigned)((g.ntot + 255) / 256));
+    if (is_f64) enforce_ff_kernel<double><<<fg, fb, 0, stream()>>>(g, (double *)gfs);
+    else if (pair) enforce_ff_kernel<float2><<<fg, fb, 0, stream()>>>(g, (float2 *)gfs);
+    else enforce_ff_kernel<float><<<fg, fb, 0, stream()>>>(g, (float *)gfs);
     NRGPU_LAUNCH_CHECK();
     return NRGPU_OK;
   }

@@ -136,4 +136,18 @@ __device__ __forceinline__ bool interior_point(const Grid &g, int &i0, int &i1, 
   return true;
 }
 
+// Start of an FP32-stage step (single grid or batch): the n doubles of y_n
+// split in place into (hi, lo) pairs (the float-float accumulation state of
+// the epilogue, and the compensated substep-0 input); for plain FP32 stages
+// also y_n rounded to FP32 into f (substep 0's input).
+template <bool ROUND>
+__global__ void split_state_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 p = split_pair_fast(y[i]);
+    if (ROUND) f[i] = p.x;
+    ((float2 *)y)[i] = p;
+  }
+}
+
 }  // namespace nrgpu

@@ -148,27 +148,14 @@ static long long state_len(int system, const paramstruct *p) {
          p->Nxx_plus_2NGHOSTS2;
 }
 
-// Start of a fused FP32-stage step: y_n split in place into (hi, lo) pairs
-// (the float-float accumulation state of the epilogue, and the compensated
-// substep-0 input); plain FP32 stages also get y_n rounded to FP32 in
-// k_even_gfs (their substep-0 input).
-template <bool ROUND>
-__global__ void prep_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const float2 p = split_pair_fast(y[i]);
-    if (ROUND) f[i] = p.x;
-    ((float2 *)y)[i] = p;
-  }
-}
 static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
   const long long n = state_len(system, p);
   const int threads = 256;
   const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 8);
   if (gfs->precision == NRGPU_PREC_COMPENSATED)
-    prep_kernel<false><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, nullptr);
+    split_state_kernel<false><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, nullptr);
   else
-    prep_kernel<true><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float *)gfs->k_even_gfs);
+    split_state_kernel<true><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float *)gfs->k_even_gfs);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
