@@ -47,6 +47,12 @@ UNIT = "gridpoint-RHS/s"
 #   compensated: 24 x 8 (pairs) + 6 x 4 + 24 x 8 + 24 x 16 + 24 x 8 = 984 B
 #   FP64:        24 x 8 + 6 x 8 + 24 x 8 + 24 x 16 + 24 x 8 = 1008 B
 RHS_BYTES_COMP = 24 * 8 + 6 * 4 + 24 * 8 + 24 * 16 + 24 * 8
+# DRAM bytes (read + write) of that launch, L2 flushed before it as in the
+# timing: one ncu capture of the launches inside the "roofline_rhs" range
+# (profiles/bssn_rhs_compensated_roofline_traffic.md), mean of two launches:
+# 118.1 MB read + 129.1 MB written, 1.9x the 129.0 MB algorithmic (register
+# spill lines evicted to DRAM and ghost-zone stencil reads).
+RHS_TRAFFIC_COMP = 247.2e6
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 
@@ -276,7 +282,9 @@ def run_gpu(args):
     evc.y_n.copy_(y0)
     evc.step(dt)
     t_ric_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 1))
+    torch.cuda.nvtx.range_push("roofline_rhs")  # the launches the roofline's traffic capture selects
     t_rhs_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 2))
+    torch.cuda.nvtx.range_pop()
     ev.y_n.copy_(y0)
     ev.step(dt)
     t_ric_64 = kernel_time(lambda: ev.substep_rhs(dt, 1, 1))
@@ -335,10 +343,11 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": "bssn rhs_kernel, compensated (FP32 pairs in/out, fused RK4 "
                                                "substep 1)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": None, "bytes_per_point": RHS_BYTES_COMP,
+                     "peak_source": src, "traffic": RHS_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
+                     "bytes_per_point": RHS_BYTES_COMP,
                      "launch_ms": t_rhs_c * 1e3,
-                     "note": "the kernel is load-latency bound (128 registers with spills to L1, 4 blocks "
-                             "of 128 threads per SM); HBM fraction reported as asked"},
+                     "note": "the kernel is load-latency bound (128 registers, 4 blocks of 128 threads per "
+                             "SM, ~1 KB spill frame per thread); HBM fraction reported as asked"},
         "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3},
                        "fp64": {"ricci": t_ric_64 * 1e3, "rhs": t_rhs_64 * 1e3}},
         "fp64": {"value": world * K * nint * 4 / t64, "unit": UNIT, "ms_per_step": t64 / K * 1e3,
