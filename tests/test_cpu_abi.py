@@ -60,7 +60,8 @@ def test_kreiss_oliger_coefficients_match_oracle(order):
     assert np.array_equal(np.array(list(out)), np.array([float(x) for x in w])), order
 
 
-@pytest.mark.parametrize("cs", ["Cartesian", "Spherical", "SinhSpherical"])
+@pytest.mark.parametrize("cs", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical",
+                                "SinhCylindrical", "SinhCylindricalv2"])
 def test_grid_setup_and_timestep_match_oracle(cs):
     from nrpytutorial_gb300 import Grid
     kw = dict(AMPL=64.0, SINHW=0.2, RMAX=10.0)
@@ -94,6 +95,19 @@ def test_bad_arguments_return_status_not_abort():
     bad3.diss_strength = float("nan")
     assert lib.rfm_struct__malloc(C.byref(bad3), C.byref(L.rfm_struct())) == 1
     assert b"diss_strength" in lib.nrgpu_last_error()
+
+
+def test_mode_decomposition_refuses_non_spherical_grids():
+    """The s = -2 decomposition integrates over a spherical shell; Cartesian
+    and Cylindrical-family grids get an argument error, before any device
+    access."""
+    L, lib = _lib()
+    from nrpytutorial_gb300 import Grid
+    buf = (C.c_double * 4)()
+    for cs in ("Cartesian", "Cylindrical", "SinhCylindrical"):
+        G = Grid(cs, (8, 8, 8), FD_order=4, NGHOSTS=3)
+        st = lib.BSSN_psi4_spinweightm2_decomposition(C.byref(G.params), buf, 4, 2, buf)
+        assert st == 1 and b"spherical" in lib.nrgpu_last_error(), cs
 
 
 def test_batch_create_validates_before_touching_the_device():
