@@ -57,6 +57,10 @@ extern "C" {
                                            z = AMPLZ sinh(xx2/SINHWZ)/sinh(1/SINHWZ)       */
 #define NRGPU_COORD_SINHCYLINDRICALV2 6 /* adds AMPLRHO const_drho xx0 to rho and
                                            AMPLZ const_dz xx2 to z (:265-275)               */
+/* reference_metric.py:306-383: symmetric TP coordinates, foci at z = +-bScale;
+   every scale factor depends on xx0 and xx1 (tables per (i0, i1) column) */
+#define NRGPU_COORD_SYMTP            7  /* AA = xx0                                          */
+#define NRGPU_COORD_SINHSYMTP        8  /* AA = AMAX sinh(xx0/SINHWAA)/sinh(1/SINHWAA)      */
 
 /* ------------------------------------------------------------- systems */
 #define NRGPU_SYS_SCALARWAVE  0   /* uu, vv                                   */
@@ -104,6 +108,7 @@ typedef struct paramstruct {
   double RHOMAX, ZMIN, ZMAX;          /* Cylindrical (reference_metric.py:233)     */
   double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  /* SinhCylindrical (:249-251)          */
   double const_drho, const_dz;        /* SinhCylindricalv2 (reference_metric.py:271) */
+  double bScale, SINHWAA, AMAX;       /* SymTP, SinhSymTP (reference_metric.py:308-310) */
 } paramstruct;
 
 /*

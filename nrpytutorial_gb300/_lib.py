@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libnrgpu.so")
 
 COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 3, "Cylindrical": 4,
-         "SinhCylindrical": 5, "SinhCylindricalv2": 6}
+         "SinhCylindrical": 5, "SinhCylindricalv2": 6, "SymTP": 7, "SinhSymTP": 8}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
 MAX_GHOSTS = 8
@@ -39,6 +39,7 @@ class paramstruct(C.Structure):
         ("RHOMAX", C.c_double), ("ZMIN", C.c_double), ("ZMAX", C.c_double),
         ("AMPLRHO", C.c_double), ("SINHWRHO", C.c_double), ("AMPLZ", C.c_double), ("SINHWZ", C.c_double),
         ("const_drho", C.c_double), ("const_dz", C.c_double),
+        ("bScale", C.c_double), ("SINHWAA", C.c_double), ("AMAX", C.c_double),
     ]
 
 

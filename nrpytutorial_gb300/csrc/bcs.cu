@@ -30,9 +30,16 @@
 
 namespace nrgpu {
 
-static void eigen_xx_to_cart(int cs, double x0, double x1, double x2, double out[3]) {
+// b: bScale of the SymTP eigen-coordinates (unused by the others).
+static void eigen_xx_to_cart(int cs, double b, double x0, double x1, double x2, double out[3]) {
   if (cs == NRGPU_COORD_CARTESIAN) {
     out[0] = x0; out[1] = x1; out[2] = x2;
+    return;
+  }
+  if (cs == NRGPU_COORD_SYMTP) {  // reference_metric.py:334-336 with AA = xx0
+    out[0] = x0 * sin(x1) * cos(x2);
+    out[1] = x0 * sin(x1) * sin(x2);
+    out[2] = sqrt(x0 * x0 + b * b) * cos(x1);
     return;
   }
   if (cs == NRGPU_COORD_CYLINDRICAL) {  // reference_metric.py:296-298
@@ -47,9 +54,19 @@ static void eigen_xx_to_cart(int cs, double x0, double x1, double x2, double out
   out[2] = x0 * cos(x1);
 }
 
-static void eigen_cart_to_xx(int cs, const double c[3], double out[3]) {
+static void eigen_cart_to_xx(int cs, double b, const double c[3], double out[3]) {
   if (cs == NRGPU_COORD_CARTESIAN) {
     out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+    return;
+  }
+  if (cs == NRGPU_COORD_SYMTP) {  // reference_metric.py:348-366
+    const double r = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    const double cth = c[2] / r, b2 = b * b, r2 = r * r;
+    const double root = sqrt(b2 * b2 + 2.0 * b2 * r2 + r2 * r2 - 4.0 * b2 * r2 * cth * cth);
+    const double sgn = c[2] > 0.0 ? 1.0 : (c[2] < 0.0 ? -1.0 : 0.0);
+    out[0] = sqrt(-b2 + r2 + root) * M_SQRT1_2;
+    out[1] = acos(sgn * sqrt(1.0 + r2 / b2 - root / b2) * M_SQRT1_2);
+    out[2] = atan2(c[1], c[0]);
     return;
   }
   if (cs == NRGPU_COORD_CYLINDRICAL) {  // reference_metric.py:240-242
@@ -67,11 +84,19 @@ static void eigen_cart_to_xx(int cs, const double c[3], double out[3]) {
 
 // Unit vectors (rows) of the eigen-coordinate basis at (x0,x1,x2)
 // (reference_metric.py:180-182 for the Spherical family, :300-302 for the
-// Cylindrical family with phi = x1; identity otherwise).
-static void unit_vectors(int cs, double x1, double x2, double U[3][3]) {
+// Cylindrical family with phi = x1, :373-379 for SymTP; identity otherwise).
+static void unit_vectors(int cs, double b, double x0, double x1, double x2, double U[3][3]) {
   if (cs == NRGPU_COORD_CARTESIAN) {
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) U[i][j] = (i == j) ? 1.0 : 0.0;
+    return;
+  }
+  if (cs == NRGPU_COORD_SYMTP) {
+    const double st = sin(x1), ct = cos(x1), sp = sin(x2), cp = cos(x2);
+    const double v1 = sqrt(x0 * x0 + b * b * st * st), v2 = sqrt(x0 * x0 + b * b);
+    U[0][0] = st * cp * v2 / v1; U[0][1] = st * sp * v2 / v1; U[0][2] = x0 * ct / v1;
+    U[1][0] = x0 * ct * cp / v1; U[1][1] = x0 * ct * sp / v1; U[1][2] = -st * v2 / v1;
+    U[2][0] = -sp;               U[2][1] = cp;               U[2][2] = 0.0;
     return;
   }
   if (cs == NRGPU_COORD_CYLINDRICAL) {
@@ -109,10 +134,12 @@ static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
   if (!(e.RMAX > 0.0)) e.RMAX = 1.0;
   if (!(e.RHOMAX > 0.0)) e.RHOMAX = 1.0;
   if (!(e.ZMAX > e.ZMIN)) e.ZMIN = -1.0, e.ZMAX = 1.0;
+  if (!(e.AMAX > 0.0)) e.AMAX = 1.0;
   int st = set_Nxx_dxx_invdx_params__and__xx(1, Nxx, &e, xxp);
   if (st) return st;
   const int cs = p->CoordSystem == NRGPU_COORD_CARTESIAN     ? NRGPU_COORD_CARTESIAN
                  : cylindrical_family(p->CoordSystem) ? NRGPU_COORD_CYLINDRICAL
+                 : symtp_family(p->CoordSystem)       ? NRGPU_COORD_SYMTP
                                                       : NRGPU_COORD_SPHERICAL;
   const int ng = p->NGHOSTS;
   const double dxx[3] = {e.dxx0, e.dxx1, e.dxx2};
@@ -124,8 +151,8 @@ static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
     for (int i1 = 0; i1 < np[1]; i1++)
       for (int i0 = 0; i0 < np[0]; i0++) {
         double c[3], xin[3], c2[3];
-        eigen_xx_to_cart(cs, xs[0][i0], xs[1][i1], xs[2][i2], c);
-        eigen_cart_to_xx(cs, c, xin);
+        eigen_xx_to_cart(cs, e.bScale, xs[0][i0], xs[1][i1], xs[2][i2], c);
+        eigen_cart_to_xx(cs, e.bScale, c, xin);
         int ib[3];
         for (int d = 0; d < 3; d++)
           ib[d] = (int)((xin[d] - xxmin[d] - (1.0 / 2.0) * dxx[d] + ((double)ng) * dxx[d]) / dxx[d] + 0.5);
@@ -134,7 +161,7 @@ static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
             set_error("ghost-zone map: point (%d,%d,%d) maps outside the grid", i0, i1, i2);
             return NRGPU_ERR_BCMAP;
           }
-        eigen_xx_to_cart(cs, xs[0][ib[0]], xs[1][ib[1]], xs[2][ib[2]], c2);
+        eigen_xx_to_cart(cs, e.bScale, xs[0][ib[0]], xs[1][ib[1]], xs[2][ib[2]], c2);
         for (int d = 0; d < 3; d++)
           if (fabs(c[d] - c2[d]) > 1e-8) {
             set_error("Cartesian disagreement at (%d,%d,%d): (%.15e %.15e %.15e) != (%.15e %.15e %.15e)",
@@ -144,8 +171,8 @@ static int build_gz_map(const paramstruct *p, std::vector<GzMap> &map) {
         const size_t idx = (size_t)i0 + (size_t)np[0] * ((size_t)i1 + (size_t)np[1] * i2);
         if (ib[0] == i0 && ib[1] == i1 && ib[2] == i2) continue;
         double U[3][3], Ui[3][3], par[10];
-        unit_vectors(cs, xs[1][i1], xs[2][i2], U);
-        unit_vectors(cs, xs[1][ib[1]], xs[2][ib[2]], Ui);
+        unit_vectors(cs, e.bScale, xs[0][i0], xs[1][i1], xs[2][i2], U);
+        unit_vectors(cs, e.bScale, xs[0][ib[0]], xs[1][ib[1]], xs[2][ib[2]], Ui);
         par[0] = 1.0;
         for (int t = 1; t <= 3; t++) {
           par[t] = 0.0;
@@ -516,6 +543,13 @@ __device__ __forceinline__ void somm_contraction(const SommerfeldGeom &G, const 
     r = x0;
     J[0] = 1.0;
     J[1] = J[2] = 0.0;
+  } else if (symtp_family(G.cs)) {
+    // dxx^i/dr along the radial direction x/r: (J^-1 x / r)^i
+    double X[3], Jm[3][3], Ji[3][3];
+    cart_jacobian(G.c, x0, somm_xx(G, 1, idx3[1]), somm_xx(G, 2, idx3[2]), X, Jm);
+    inverse3(Jm, Ji);
+    r = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+    for (int i = 0; i < 3; i++) J[i] = (Ji[i][0] * X[0] + Ji[i][1] * X[1] + Ji[i][2] * X[2]) / r;
   } else if (cylindrical_family(G.cs)) {
     // r = sqrt(rho^2 + z^2); dxx0/dr = (rho/r) / (drho/dxx0), dxx2/dr = (z/r) / (dz/dxx2)
     double rho[4], z[4];

@@ -13,6 +13,7 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 6)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_CARTESIAN, 8)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHCYLINDRICAL, 4)
+NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSYMTP, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
@@ -23,6 +24,7 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
     case NRGPU_COORD_CARTESIAN * 16 + 8: return CALL(NRGPU_COORD_CARTESIAN, 8);               \
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SINHSPHERICAL, 4);       \
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: return CALL(NRGPU_COORD_SINHCYLINDRICAL, 4);   \
+    case NRGPU_COORD_SINHSYMTP * 16 + 4: return CALL(NRGPU_COORD_SINHSYMTP, 4);               \
     case NRGPU_COORD_SPHERICAL * 16 + 4: return CALL(NRGPU_COORD_SPHERICAL, 4);               \
   }                                                                                           \
   set_error("BSSN: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order); \
@@ -278,6 +280,19 @@ __global__ void bl_id_kernel(paramstruct p, BLParams bl, double *__restrict__ gf
       s[a] = dconst(1.0);
       for (int b = 0; b < 3; b++) J[a][b] = dconst(a == b ? 1.0 : 0.0);
     }
+  } else if (symtp_family(p.CoordSystem)) {
+    // (AA sin xx1 cos xx2, AA sin xx1 sin xx2, var2 cos xx1) (reference_metric.py:334-336)
+    Dual A = X0, dA = dconst(1.0);
+    if (p.CoordSystem == NRGPU_COORD_SINHSYMTP) dsinh_map(p.AMAX, p.SINHWAA, 0.0, X0, A, dA);
+    const Dual st = dsin(X1), ct = dcos(X1), sp = dsin(X2), cp = dcos(X2);
+    const Dual b2 = dconst(p.bScale * p.bScale);
+    const Dual v1 = dsqrt(A * A + b2 * st * st), v2 = dsqrt(A * A + b2);
+    const Dual dv2 = (A * dA) / v2;
+    xc[0] = A * st * cp; xc[1] = A * st * sp; xc[2] = v2 * ct;
+    J[0][0] = dA * st * cp; J[0][1] = A * ct * cp; J[0][2] = -(A * st * sp);
+    J[1][0] = dA * st * sp; J[1][1] = A * ct * sp; J[1][2] = A * st * cp;
+    J[2][0] = dv2 * ct;     J[2][1] = -(v2 * st);  J[2][2] = dconst(0.0);
+    s[0] = dA * v1 / v2; s[1] = v1; s[2] = A * st;
   } else if (cylindrical_family(p.CoordSystem)) {
     // (rho cos phi, rho sin phi, z) (reference_metric.py:296-298)
     Dual rho = X0, drho = dconst(1.0), z = X2, dz = dconst(1.0);
@@ -459,6 +474,8 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
     enforce_kernel<NRGPU_COORD_SPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
   else if (cylindrical_family(p->CoordSystem))                                                            \
     enforce_kernel<NRGPU_COORD_SINHCYLINDRICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);      \
+  else if (symtp_family(p->CoordSystem))                                                                  \
+    enforce_kernel<NRGPU_COORD_SINHSYMTP, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
   else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
   NRGPU_REQUIRE(!pair, "pair gridfunctions are FP32");
   ENF(double)
@@ -523,6 +540,8 @@ int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *p, con
       hamiltonian_kernel<NRGPU_COORD_SINHSPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_SINHCYLINDRICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
+    case NRGPU_COORD_SINHSYMTP * 16 + 4:
+      hamiltonian_kernel<NRGPU_COORD_SINHSYMTP, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4:
       hamiltonian_kernel<NRGPU_COORD_SPHERICAL, 4><<<L.grid, L.block, 0, stream()>>>(g, in, tab, aux); break;
     default:
@@ -571,6 +590,7 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *p, const 
     case NRGPU_COORD_CARTESIAN * 16 + 8: MOM(NRGPU_COORD_CARTESIAN, 8); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MOM(NRGPU_COORD_SINHSPHERICAL, 4); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: MOM(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
+    case NRGPU_COORD_SINHSYMTP * 16 + 4: MOM(NRGPU_COORD_SINHSYMTP, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4: MOM(NRGPU_COORD_SPHERICAL, 4); break;
     default:
       set_error("momentum constraint: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);
@@ -600,6 +620,10 @@ int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *
     case NRGPU_COORD_SINHCYLINDRICALV2:
       constraint_sources_kernel<NRGPU_COORD_SINHCYLINDRICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU,
                                                                                               H, MU);
+      break;
+    case NRGPU_COORD_SYMTP:
+    case NRGPU_COORD_SINHSYMTP:
+      constraint_sources_kernel<NRGPU_COORD_SINHSYMTP><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H, MU);
       break;
     default:
       constraint_sources_kernel<NRGPU_COORD_SINHSPHERICAL><<<L.grid, L.block, 0, stream()>>>(g, in, tab, T4UU, H,

@@ -59,12 +59,13 @@ struct Grid {
 // on the structure of the reference metric (which scale factor depends on
 // which coordinate, RfmMask) and read its values from the rfm tables;
 // SinhSphericalv2 has SinhSpherical's structure and differs only in r(xx0),
-// Cylindrical has SinhCylindrical's with the identity maps; the tables and
-// the runtime CoordSystem carry the values.
+// Cylindrical has SinhCylindrical's with the identity maps, SymTP
+// SinhSymTP's; the tables and the runtime CoordSystem carry the values.
 inline int dispatch_cs(int cs) {
   return cs == NRGPU_COORD_SINHSPHERICALV2 ? NRGPU_COORD_SINHSPHERICAL
          : (cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICALV2) ? NRGPU_COORD_SINHCYLINDRICAL
-                                                                                   : cs;
+         : cs == NRGPU_COORD_SYMTP ? NRGPU_COORD_SINHSYMTP
+                                   : cs;
 }
 
 inline Grid make_grid(const paramstruct *p) {

@@ -29,7 +29,7 @@ void count_launch(int n) { g_launches += n; }
 
 int check_params(const paramstruct *p) {
   NRGPU_REQUIRE(p != nullptr, "params is NULL");
-  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 6, "unknown CoordSystem %d", p->CoordSystem);
+  NRGPU_REQUIRE(p->CoordSystem >= 0 && p->CoordSystem <= 8, "unknown CoordSystem %d", p->CoordSystem);
   NRGPU_REQUIRE(p->FD_order == 2 || p->FD_order == 4 || p->FD_order == 6 || p->FD_order == 8,
                 "FD_order %d not in {2,4,6,8}", p->FD_order);
   NRGPU_REQUIRE(p->NGHOSTS >= p->FD_order / 2 && p->NGHOSTS <= NRGPU_MAX_GHOSTS,
@@ -127,10 +127,15 @@ int set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3], paramstr
   // family Cylindrical (reference_metric.py:946-952).
   if (EigenCoord && spherical_family(cs)) cs = NRGPU_COORD_SPHERICAL;
   if (EigenCoord && cylindrical_family(cs)) cs = NRGPU_COORD_CYLINDRICAL;
+  if (EigenCoord && symtp_family(cs)) cs = NRGPU_COORD_SYMTP;
   if (cs == NRGPU_COORD_CARTESIAN) {
     xmin[0] = p->xmin; xmax[0] = p->xmax;
     xmin[1] = p->ymin; xmax[1] = p->ymax;
     xmin[2] = p->zmin; xmax[2] = p->zmax;
+  } else if (symtp_family(cs)) {  // reference_metric.py:317-322
+    xmin[0] = 0.0;   xmax[0] = cs == NRGPU_COORD_SYMTP ? p->AMAX : 1.0;
+    xmin[1] = 0.0;   xmax[1] = M_PI;
+    xmin[2] = -M_PI; xmax[2] = M_PI;
   } else if (cylindrical_family(cs)) {
     // Cylindrical :233-234; SinhCylindrical :246-247
     const bool plain = cs == NRGPU_COORD_CYLINDRICAL;

@@ -221,6 +221,7 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
   MC_CASE(NRGPU_COORD_SPHERICAL, 2) MC_CASE(NRGPU_COORD_SPHERICAL, 4)
   MC_CASE(NRGPU_COORD_SINHSPHERICAL, 2) MC_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
   MC_CASE(NRGPU_COORD_SINHCYLINDRICAL, 2) MC_CASE(NRGPU_COORD_SINHCYLINDRICAL, 4)
+  MC_CASE(NRGPU_COORD_SINHSYMTP, 2) MC_CASE(NRGPU_COORD_SINHSYMTP, 4)
 #undef MC_CASE
   set_error("curvilinear Maxwell: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order);
   return NRGPU_ERR_UNSUPPORTED;
@@ -290,6 +291,8 @@ int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const paramstruct *p, 
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: MCC(NRGPU_COORD_SINHSPHERICAL, 4); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 2: MCC(NRGPU_COORD_SINHCYLINDRICAL, 2); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: MCC(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
+    case NRGPU_COORD_SINHSYMTP * 16 + 2: MCC(NRGPU_COORD_SINHSYMTP, 2); break;
+    case NRGPU_COORD_SINHSYMTP * 16 + 4: MCC(NRGPU_COORD_SINHSYMTP, 4); break;
     default: set_error("curvilinear Maxwell constraints: FD_order %d not built", p->FD_order); return NRGPU_ERR_UNSUPPORTED;
   }
 #undef MCC

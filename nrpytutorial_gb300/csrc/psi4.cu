@@ -409,6 +409,7 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
     case NRGPU_COORD_CARTESIAN * 16 + 6: P4(NRGPU_COORD_CARTESIAN, 6); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: P4(NRGPU_COORD_SINHSPHERICAL, 4); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: P4(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
+    case NRGPU_COORD_SINHSYMTP * 16 + 4: P4(NRGPU_COORD_SINHSYMTP, 4); break;
     case NRGPU_COORD_SPHERICAL * 16 + 4: P4(NRGPU_COORD_SPHERICAL, 4); break;
     default:
       set_error("psi4: CoordSystem %d FD_order %d not built", p->CoordSystem, p->FD_order);

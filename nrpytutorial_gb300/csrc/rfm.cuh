@@ -47,9 +47,15 @@ __host__ __device__ constexpr bool cylindrical_family(int cs) {
   return cs == NRGPU_COORD_CYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICAL || cs == NRGPU_COORD_SINHCYLINDRICALV2;
 }
 
+__host__ __device__ constexpr bool symtp_family(int cs) {
+  return cs == NRGPU_COORD_SYMTP || cs == NRGPU_COORD_SINHSYMTP;
+}
+
 // dep(CS, i, k): does scale factor s_i depend on xx_k?
 __host__ __device__ constexpr bool dep(int cs, int i, int k) {
   return cs == NRGPU_COORD_CARTESIAN ? false
+         // SymTP family: s0 = AA' var1/var2, s1 = var1, s2 = AA sin(xx1), all of (xx0, xx1)
+         : symtp_family(cs) ? k <= 1
          // Cylindrical family: s0 = drho/dxx0, s1 = rho(xx0), s2 = dz/dxx2
          : cylindrical_family(cs) ? ((k == 0 && i <= 1) || (k == 2 && i == 2))
          // Spherical family: s0 = dr/dxx0, s1 = r(xx0), s2 = r(xx0) sin(xx1)
@@ -163,11 +169,12 @@ struct CoordParams {
   double AMPL, SINHW, const_dr;             // Spherical family
   double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  // SinhCylindrical
   double const_drho, const_dz;              // SinhCylindricalv2
+  double bScale, SINHWAA, AMAX;             // SymTP family
 };
 
 __host__ __device__ inline CoordParams coord_params(const paramstruct &p) {
-  return CoordParams{p.CoordSystem, p.AMPL,  p.SINHW,  p.const_dr,   p.AMPLRHO,
-                     p.SINHWRHO,    p.AMPLZ, p.SINHWZ, p.const_drho, p.const_dz};
+  return CoordParams{p.CoordSystem, p.AMPL,      p.SINHW,    p.const_dr, p.AMPLRHO, p.SINHWRHO, p.AMPLZ,
+                     p.SINHWZ,      p.const_drho, p.const_dz, p.bScale,   p.SINHWAA, p.AMAX};
 }
 
 __host__ __device__ inline bool spherical_family(int cs) {
@@ -214,6 +221,19 @@ __host__ __device__ inline void cylinder_maps(const CoordParams &c, double x0, d
   }
 }
 
+// SymTP family (reference_metric.py:320-383): AA(xx0) with three derivatives
+// (SymTP: AA = xx0; SinhSymTP: the sinh map of AMAX, SINHWAA), var1 =
+// sqrt(AA^2 + (bScale sin xx1)^2), var2 = sqrt(AA^2 + bScale^2).
+__host__ __device__ inline void symtp_aa(const CoordParams &c, double x0, double A[4]) {
+  if (c.cs == NRGPU_COORD_SINHSYMTP) {
+    sinh_map(c.AMAX, c.SINHWAA, 0.0, x0, A);
+  } else {
+    A[0] = x0;
+    A[1] = 1.0;
+    A[2] = A[3] = 0.0;
+  }
+}
+
 // s[i], ds[i][k] = d s_i / d xx_k, dds[i][k][l] at uniform coordinates
 // (xx0, xx1, xx2) (reference_metric.py:168-175 Spherical family: s0 = dr/dxx0,
 // s1 = r, s2 = r sin(xx1); :289-291 Cylindrical family: s0 = drho/dxx0,
@@ -232,6 +252,45 @@ __host__ __device__ inline void scale_factors(const CoordParams &c, double xx0, 
     }
   }
   if (c.cs == NRGPU_COORD_CARTESIAN) return;
+  if (symtp_family(c.cs)) {
+    // s0 = AA' q with q = var1/var2, s1 = var1, s2 = AA sin(xx1); derivatives
+    // in (xx0, xx1) by the chain rule (none depends on xx2)
+    double A[4];
+    symtp_aa(c, xx0, A);
+    const double b2 = c.bScale * c.bScale, sn = sin(xx1), cn = cos(xx1);
+    const double v1 = sqrt(A[0] * A[0] + b2 * sn * sn), v2 = sqrt(A[0] * A[0] + b2);
+    const double du[2] = {2.0 * A[0] * A[1], 2.0 * b2 * sn * cn};
+    const double ddu[2][2] = {{2.0 * (A[1] * A[1] + A[0] * A[2]), 0.0}, {0.0, 2.0 * b2 * (cn * cn - sn * sn)}};
+    double dv1[2], ddv1[2][2], dv2[2] = {du[0] / (2.0 * v2), 0.0}, ddv2[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    ddv2[0][0] = ddu[0][0] / (2.0 * v2) - du[0] * du[0] / (4.0 * v2 * v2 * v2);
+    for (int k = 0; k < 2; k++) {
+      dv1[k] = du[k] / (2.0 * v1);
+      for (int l = 0; l < 2; l++) ddv1[k][l] = ddu[k][l] / (2.0 * v1) - du[k] * du[l] / (4.0 * v1 * v1 * v1);
+    }
+    const double q = v1 / v2;
+    double dq[2], ddq[2][2];
+    for (int k = 0; k < 2; k++) dq[k] = dv1[k] / v2 - v1 * dv2[k] / (v2 * v2);
+    for (int k = 0; k < 2; k++)
+      for (int l = 0; l < 2; l++)
+        ddq[k][l] = ddv1[k][l] / v2 - (dv1[k] * dv2[l] + dv1[l] * dv2[k]) / (v2 * v2) -
+                    v1 * ddv2[k][l] / (v2 * v2) + 2.0 * v1 * dv2[k] * dv2[l] / (v2 * v2 * v2);
+    const double dA1[2] = {A[2], 0.0}, ddA1[2][2] = {{A[3], 0.0}, {0.0, 0.0}};
+    const double ds2[2] = {A[1] * sn, A[0] * cn}, dds2[2][2] = {{A[2] * sn, A[1] * cn}, {A[1] * cn, -A[0] * sn}};
+    S->s[0] = A[1] * q;
+    S->s[1] = v1;
+    S->s[2] = A[0] * sn;
+    for (int k = 0; k < 2; k++) {
+      S->ds[0][k] = dA1[k] * q + A[1] * dq[k];
+      S->ds[1][k] = dv1[k];
+      S->ds[2][k] = ds2[k];
+      for (int l = 0; l < 2; l++) {
+        S->dds[0][k][l] = ddA1[k][l] * q + dA1[k] * dq[l] + dA1[l] * dq[k] + A[1] * ddq[k][l];
+        S->dds[1][k][l] = ddv1[k][l];
+        S->dds[2][k][l] = dds2[k][l];
+      }
+    }
+    return;
+  }
   if (cylindrical_family(c.cs)) {
     double rho[4], z[4];
     cylinder_maps(c, xx0, xx2, rho, z);
@@ -337,6 +396,24 @@ __host__ __device__ inline void cart_jacobian(const CoordParams &c, double xx0, 
     x[2] = xx2;
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) J[i][j] = i == j ? 1.0 : 0.0;
+  } else if (symtp_family(c.cs)) {
+    // (AA sin xx1 cos xx2, AA sin xx1 sin xx2, var2 cos xx1) (reference_metric.py:334-336)
+    double A[4];
+    symtp_aa(c, xx0, A);
+    const double b2 = c.bScale * c.bScale, v2 = sqrt(A[0] * A[0] + b2), dv2 = A[0] * A[1] / v2;
+    const double st = sin(xx1), ct = cos(xx1), sp = sin(xx2), cp = cos(xx2);
+    x[0] = A[0] * st * cp;
+    x[1] = A[0] * st * sp;
+    x[2] = v2 * ct;
+    J[0][0] = A[1] * st * cp;
+    J[0][1] = A[0] * ct * cp;
+    J[0][2] = -A[0] * st * sp;
+    J[1][0] = A[1] * st * sp;
+    J[1][1] = A[0] * ct * sp;
+    J[1][2] = A[0] * st * cp;
+    J[2][0] = dv2 * ct;
+    J[2][1] = -v2 * st;
+    J[2][2] = 0.0;
   } else if (cylindrical_family(c.cs)) {
     double rho[4], z[4];
     cylinder_maps(c, xx0, xx2, rho, z);

@@ -81,6 +81,7 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
   SW_CASE(NRGPU_COORD_SPHERICAL, 2) SW_CASE(NRGPU_COORD_SPHERICAL, 4)
   SW_CASE(NRGPU_COORD_SINHSPHERICAL, 2) SW_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
   SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 2) SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 4)
+  SW_CASE(NRGPU_COORD_SINHSYMTP, 2) SW_CASE(NRGPU_COORD_SINHSYMTP, 4)
 #undef SW_CASE
   set_error("ScalarWave: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order);
   return NRGPU_ERR_UNSUPPORTED;

@@ -42,7 +42,8 @@ class Grid:
     def __init__(self, CoordSystem, Nxx, FD_order=4, NGHOSTS=2, *, AMPL=10.0, SINHW=0.2,
                  RMAX=10.0, domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, diss_strength=0.0,
                  stress_energy_source_terms=False, const_dr=0.0625, RHOMAX=10.0, ZMIN=-10.0, ZMAX=10.0,
-                 AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2, const_drho=0.0625, const_dz=0.0625):
+                 AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2, const_drho=0.0625, const_dz=0.0625,
+                 bScale=0.5, SINHWAA=0.2, AMAX=10.0):
         lib = _lib.load()
         p = _lib.paramstruct()
         p.CoordSystem = _lib.COORD[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
@@ -53,6 +54,7 @@ class Grid:
         p.RHOMAX, p.ZMIN, p.ZMAX = RHOMAX, ZMIN, ZMAX  # Cylindrical domain (reference defaults)
         p.AMPLRHO, p.SINHWRHO, p.AMPLZ, p.SINHWZ = AMPLRHO, SINHWRHO, AMPLZ, SINHWZ  # SinhCylindrical
         p.const_drho, p.const_dz = const_drho, const_dz  # SinhCylindricalv2
+        p.bScale, p.SINHWAA, p.AMAX = bScale, SINHWAA, AMAX  # SymTP family (reference defaults)
         lo, hi = domain
         p.xmin = p.ymin = p.zmin = lo
         p.xmax = p.ymax = p.zmax = hi

@@ -19,7 +19,7 @@ then the post-RHS calls (BCs, then the det(gammabar) rescale for BSSN).
 """
 import numpy as np
 
-from .grid import CART, GridParams, cylinder_maps, cylindrical, radial
+from .grid import CART, GridParams, cylinder_maps, cylindrical, radial, symtp
 
 
 def build_bcstruct(gp):
@@ -27,15 +27,26 @@ def build_bcstruct(gp):
     outer = list of (idx3, step) in application order (grouped per face dir:
     list of 3 arrays), inner = (dest idx3, src idx3, parity (n,10) ints)."""
     eg = GridParams(gp.CoordSystem, gp.Nxx, gp.NGHOSTS, gp.FD_order, gp.AMPL, gp.SINHW, gp.RMAX,
-                    EigenCoord=1, RHOMAX=gp.RHOMAX, ZMIN=gp.ZMIN, ZMAX=gp.ZMAX)
+                    EigenCoord=1, RHOMAX=gp.RHOMAX, ZMIN=gp.ZMIN, ZMAX=gp.ZMAX, bScale=gp.bScale, AMAX=gp.AMAX)
     n0, n1, n2 = eg.np
     ng = gp.NGHOSTS
     cart = gp.CoordSystem == CART
     cyl = cylindrical(gp.CoordSystem)
+    stp = symtp(gp.CoordSystem)
+    b = gp.bScale
     X2, X1, X0 = np.meshgrid(eg.xx[2], eg.xx[1], eg.xx[0], indexing="ij")
     if cart:
         xc = [X0, X1, X2]
         xin = [X0, X1, X2]
+    elif stp:
+        # SymTP eigen-coordinates (reference_metric.py:334-336, 348-366)
+        xc = [X0 * np.sin(X1) * np.cos(X2), X0 * np.sin(X1) * np.sin(X2), np.sqrt(X0 ** 2 + b * b) * np.cos(X1)]
+        r = np.sqrt(xc[0] ** 2 + xc[1] ** 2 + xc[2] ** 2)
+        cth = xc[2] / r
+        root = np.sqrt(b ** 4 + 2 * b * b * r * r + r ** 4 - 4 * b * b * r * r * cth * cth)
+        xin = [np.sqrt(-b * b + r * r + root) * np.sqrt(0.5),
+               np.arccos(np.sign(xc[2]) * np.sqrt(1 + r * r / (b * b) - root / (b * b)) * np.sqrt(0.5)),
+               np.arctan2(xc[1], xc[0])]
     elif cyl:
         # Cylindrical eigen-coordinates (reference_metric.py:240-242, 296-298)
         xc = [X0 * np.cos(X1), X0 * np.sin(X1), X2]
@@ -50,21 +61,26 @@ def build_bcstruct(gp):
     I2, I1, I0 = np.meshgrid(np.arange(n2), np.arange(n1), np.arange(n0), indexing="ij")
     inner = (ib[0] != I0) | (ib[1] != I1) | (ib[2] != I2)
 
-    def unit(x1, x2):
+    def unit(x1, x2, x0=None):
         if cart:
             e = np.zeros((3, 3) + np.shape(x1))
             for i in range(3):
                 e[i, i] = 1.0
             return e
+        if stp:  # reference_metric.py:373-379
+            st, ct, sp, cp = np.sin(x1), np.cos(x1), np.sin(x2), np.cos(x2)
+            v1, v2 = np.sqrt(x0 ** 2 + b * b * st * st), np.sqrt(x0 ** 2 + b * b)
+            return np.array([[st * cp * v2 / v1, st * sp * v2 / v1, x0 * ct / v1],
+                             [x0 * ct * cp / v1, x0 * ct * sp / v1, -st * v2 / v1], [-sp, cp, 0 * st]])
         if cyl:  # reference_metric.py:300-302, phi = xx1
             sp, cp, z0 = np.sin(x1), np.cos(x1), 0 * np.asarray(x1, dtype=float)
             return np.array([[cp, sp, z0], [-sp, cp, z0], [z0, z0, z0 + 1.0]])
         st, ct, sp, cp = np.sin(x1), np.cos(x1), np.sin(x2), np.cos(x2)
         return np.array([[st * cp, st * sp, ct], [ct * cp, ct * sp, -st], [-sp, cp, 0 * st]])
 
-    U = unit(X1, X2)
+    U = unit(X1, X2, X0)
     ibc = [np.clip(ib[d], 0, eg.np[d] - 1) for d in range(3)]
-    Ui = unit(eg.xx[1][ibc[1]], eg.xx[2][ibc[2]])
+    Ui = unit(eg.xx[1][ibc[1]], eg.xx[2][ibc[2]], eg.xx[0][ibc[0]])
     par = np.ones((10,) + X0.shape)
     for t in range(1, 4):
         par[t] = (U[t - 1] * Ui[t - 1]).sum(axis=0)
@@ -207,6 +223,12 @@ def _radial_geometry(gp, i0, i1, i2):
         return r, (x0 / r, x1 / r, x2 / r)
     if gp.CoordSystem == 1:  # Spherical: xx0 = r
         return x0, (1.0, 0.0, 0.0)
+    if symtp(gp.CoordSystem):  # dxx^i/dr = (J^-1 x / r)^i
+        from .psi4 import _inv_general, cart_and_jacobian
+        x, Jm = cart_and_jacobian(gp.CoordSystem, x0, x1, x2, cyl=gp)
+        r = float(np.sqrt((np.asarray(x) ** 2).sum()))
+        Ji = _inv_general(np.asarray(Jm, dtype=float))
+        return r, tuple(float(sum(Ji[i, j] * x[j] for j in range(3)) / r) for i in range(3))
     if cylindrical(gp.CoordSystem):  # r = sqrt(rho^2 + z^2)
         (rho, drho), (z, dz) = cylinder_maps(gp, x0, x2)
         r = float(np.sqrt(rho * rho + z * z))

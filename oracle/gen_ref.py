@@ -44,6 +44,7 @@ CONFIGS = {
     "bssn_sinhv2_fd4": ("BSSN", "SinhSphericalv2", 4, 3),
     "bssn_sinhcyl_fd4": ("BSSN", "SinhCylindrical", 4, 3),
     "bssn_sinhcylv2_fd4": ("BSSN", "SinhCylindricalv2", 4, 3),
+    "bssn_sinhsymtp_fd4": ("BSSN", "SinhSymTP", 4, 3),
     "bssn_cart_fd4": ("BSSN", "Cartesian", 4, 3),
     "bssn_cart_fd6": ("BSSN", "Cartesian", 6, 4),
     "bssn_cart_fd2": ("BSSN", "Cartesian", 2, 2),

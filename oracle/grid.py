@@ -20,9 +20,59 @@ TEST INFRASTRUCTURE (see oracle/__init__.py).
 """
 import numpy as np
 
-CART, SPH, SINHSPH, SINHSPHV2, CYL, SINHCYL, SINHCYLV2 = 0, 1, 2, 3, 4, 5, 6
+CART, SPH, SINHSPH, SINHSPHV2, CYL, SINHCYL, SINHCYLV2, SYMTP, SINHSYMTP = 0, 1, 2, 3, 4, 5, 6, 7, 8
 NAMES = {"Cartesian": CART, "Spherical": SPH, "SinhSpherical": SINHSPH, "SinhSphericalv2": SINHSPHV2,
-         "Cylindrical": CYL, "SinhCylindrical": SINHCYL, "SinhCylindricalv2": SINHCYLV2}
+         "Cylindrical": CYL, "SinhCylindrical": SINHCYL, "SinhCylindricalv2": SINHCYLV2, "SymTP": SYMTP,
+         "SinhSymTP": SINHSYMTP}
+
+
+def symtp(cs):
+    return cs in (SYMTP, SINHSYMTP)
+
+
+def symtp_scale_factors(gp, x0, x1):
+    """SymTP family (reference_metric.py:306-383): AA(xx0) (xx0, or the sinh
+    map of AMAX/SINHWAA), var1 = sqrt(AA^2 + (bScale sin xx1)^2), var2 =
+    sqrt(AA^2 + bScale^2); s0 = AA' var1/var2, s1 = var1, s2 = AA sin xx1,
+    with first and second derivatives in xx0, xx1 by the chain rule."""
+    b = gp.bScale
+    z = np.zeros_like(x0)
+    if gp.CoordSystem == SINHSYMTP:
+        A, A1 = sinh_map(gp.AMAX, gp.SINHWAA, x0)
+        A2, A3 = A / gp.SINHWAA ** 2, A1 / gp.SINHWAA ** 2
+    else:
+        A, A1, A2, A3 = x0, np.ones_like(x0), z, z
+    S, Cs = np.sin(x1), np.cos(x1)
+    u = A * A + b * b * S * S
+    v1 = np.sqrt(u)
+    du = [2 * A * A1, 2 * b * b * S * Cs]
+    ddu = [[2 * (A1 * A1 + A * A2), z], [z, 2 * b * b * (Cs * Cs - S * S)]]
+    dv1 = [du[k] / (2 * v1) for k in range(2)]
+    ddv1 = [[ddu[k][l] / (2 * v1) - du[k] * du[l] / (4 * v1 ** 3) for l in range(2)] for k in range(2)]
+    w = A * A + b * b
+    v2 = np.sqrt(w)
+    dv2 = [2 * A * A1 / (2 * v2), z]
+    ddv2 = [[2 * (A1 * A1 + A * A2) / (2 * v2) - (2 * A * A1) ** 2 / (4 * v2 ** 3), z], [z, z]]
+    q = v1 / v2
+    dq = [dv1[k] / v2 - v1 * dv2[k] / v2 ** 2 for k in range(2)]
+    ddq = [[ddv1[k][l] / v2 - (dv1[k] * dv2[l] + dv1[l] * dv2[k]) / v2 ** 2 - v1 * ddv2[k][l] / v2 ** 2
+            + 2 * v1 * dv2[k] * dv2[l] / v2 ** 3 for l in range(2)] for k in range(2)]
+    dA1 = [A2, z]
+    ddA1 = [[A3, z], [z, z]]
+    s = [A1 * q, v1, A * S]
+    ds = [[z.copy() for _ in range(3)] for _ in range(3)]
+    dds = [[[z.copy() for _ in range(3)] for _ in range(3)] for _ in range(3)]
+    ds2 = [A1 * S, A * Cs]
+    dds2 = [[A2 * S, A1 * Cs], [A1 * Cs, -A * S]]
+    for k in range(2):
+        ds[0][k] = dA1[k] * q + A1 * dq[k]
+        ds[1][k] = dv1[k]
+        ds[2][k] = ds2[k]
+        for l in range(2):
+            dds[0][k][l] = ddA1[k][l] * q + dA1[k] * dq[l] + dA1[l] * dq[k] + A1 * ddq[k][l]
+            dds[1][k][l] = ddv1[k][l]
+            dds[2][k][l] = dds2[k][l]
+    return s, ds, dds
 
 
 def cylindrical(cs):
@@ -74,7 +124,7 @@ class GridParams:
     def __init__(self, CoordSystem, Nxx, NGHOSTS, FD_order=4, AMPL=10.0, SINHW=0.2, RMAX=10.0,
                  domain=(-10.0, 10.0), eta=2.0, wavespeed=1.0, EigenCoord=0, const_dr=0.0625, RHOMAX=10.0,
                  ZMIN=-10.0, ZMAX=10.0, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0, SINHWZ=0.2, const_drho=0.0625,
-                 const_dz=0.0625):
+                 const_dz=0.0625, bScale=0.5, SINHWAA=0.2, AMAX=10.0):
         cs = NAMES[CoordSystem] if isinstance(CoordSystem, str) else int(CoordSystem)
         self.CoordSystem = cs
         self.FD_order = FD_order
@@ -84,16 +134,20 @@ class GridParams:
         self.RHOMAX, self.ZMIN, self.ZMAX = RHOMAX, ZMIN, ZMAX
         self.AMPLRHO, self.SINHWRHO, self.AMPLZ, self.SINHWZ = AMPLRHO, SINHWRHO, AMPLZ, SINHWZ
         self.const_drho, self.const_dz = const_drho, const_dz
+        self.bScale, self.SINHWAA, self.AMAX = bScale, SINHWAA, AMAX
         self.eta, self.wavespeed = eta, wavespeed
         self.Nxx = [int(n) for n in Nxx]
         self.np = [n + 2 * NGHOSTS for n in self.Nxx]
         ecs = SPH if (EigenCoord and cs in (SINHSPH, SINHSPHV2)) else cs
         ecs = CYL if (EigenCoord and cs in (SINHCYL, SINHCYLV2)) else ecs
+        ecs = SYMTP if (EigenCoord and cs == SINHSYMTP) else ecs
         if ecs == CART:
             lo, hi = domain
             self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
         elif ecs == CYL:
             self.xxmin, self.xxmax = [0.0, -np.pi, ZMIN], [RHOMAX, np.pi, ZMAX]
+        elif symtp(ecs):  # :317-322
+            self.xxmin, self.xxmax = [0.0, 0.0, -np.pi], [AMAX if ecs == SYMTP else 1.0, np.pi, np.pi]
         elif ecs in (SINHCYL, SINHCYLV2):
             self.xxmin, self.xxmax = [0.0, -np.pi, -1.0], [1.0, np.pi, 1.0]
         else:
@@ -124,6 +178,8 @@ def scale_factors(gp, xx0, xxB):
     dds = [[[z.copy() for _ in range(3)] for _ in range(3)] for _ in range(3)]
     if gp.CoordSystem == CART:
         return s, ds, dds
+    if symtp(gp.CoordSystem):
+        return symtp_scale_factors(gp, x0, x1)
     if cylindrical(gp.CoordSystem):
         (rho, rho1), (zz, z1) = cylinder_maps(gp, x0, x1)
         if gp.CoordSystem in (SINHCYL, SINHCYLV2):
@@ -189,7 +245,8 @@ class _PointParams:
     def __init__(self, cs, **kw):
         self.CoordSystem = cs
         for k, v in dict(AMPL=10.0, SINHW=0.2, const_dr=0.0625, AMPLRHO=10.0, SINHWRHO=0.2, AMPLZ=10.0,
-                         SINHWZ=0.2, const_drho=0.0625, const_dz=0.0625).items():
+                         SINHWZ=0.2, const_drho=0.0625, const_dz=0.0625, bScale=0.5, SINHWAA=0.2,
+                         AMAX=10.0).items():
             setattr(self, k, kw.get(k, v))
 
 

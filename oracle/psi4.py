@@ -160,6 +160,20 @@ def cart_and_jacobian(cs, xx0, xx1, xx2, AMPL=10.0, SINHW=0.2, const_dr=0.0625, 
         one, zero = np.ones_like(xx0), np.zeros_like(xx0)
         J = np.array([[one, zero, zero], [zero, one, zero], [zero, zero, one]])
         return np.array([xx0, xx1, xx2]), J
+    if cs in (7, 8):  # SymTP family, reference_metric.py:334-336
+        b = cyl.bScale
+        if cs == 8:
+            from .grid import sinh_map
+            A, dA = sinh_map(cyl.AMAX, cyl.SINHWAA, xx0)
+        else:
+            A, dA = xx0, np.ones_like(xx0)
+        st, ct, sp_, cp = np.sin(xx1), np.cos(xx1), np.sin(xx2), np.cos(xx2)
+        v2 = np.sqrt(A * A + b * b)
+        zero = np.zeros_like(A)
+        x = np.array([A * st * cp, A * st * sp_, v2 * ct])
+        J = np.array([[dA * st * cp, A * ct * cp, -A * st * sp_], [dA * st * sp_, A * ct * sp_, A * st * cp],
+                      [A * dA / v2 * ct, -v2 * st, zero]])
+        return x, J
     if cylindrical(cs):  # (rho cos phi, rho sin phi, z), reference_metric.py:296-298
         (rho, drho), (z, dz) = cylinder_maps(cyl, xx0, xx2)
         sp_, cp = np.sin(xx1), np.cos(xx1)

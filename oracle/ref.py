@@ -36,7 +36,8 @@ class RefKernels:
                 "invdx0": gp.invdx[0], "invdx1": gp.invdx[1], "invdx2": gp.invdx[2],
                 "AMPL": gp.AMPL, "SINHW": gp.SINHW, "RMAX": gp.RMAX, "eta": gp.eta, "wavespeed": gp.wavespeed,
                 "const_dr": getattr(gp, "const_dr", 0.0625)}
-        for k in ("RHOMAX", "ZMIN", "ZMAX", "AMPLRHO", "SINHWRHO", "AMPLZ", "SINHWZ", "const_drho", "const_dz"):
+        for k in ("RHOMAX", "ZMIN", "ZMAX", "AMPLRHO", "SINHWRHO", "AMPLZ", "SINHWZ", "const_drho", "const_dz",
+                  "bScale", "SINHWAA", "AMAX"):
             if hasattr(gp, k):
                 vals[k] = getattr(gp, k)
         vals.update(extra or {})

@@ -149,7 +149,7 @@ def scalarwave_id_grid(gp, kind, t=0.0, k=(1.0, 1.0, 1.0), sigma=3.0):
     X2, X1, X0 = np.meshgrid(gp.xx[2], gp.xx[1], gp.xx[0], indexing="ij")
     if gp.CoordSystem == 0:
         x, y, z = X0, X1, X2
-    elif gp.CoordSystem in (4, 5):  # Cylindrical family
+    elif gp.CoordSystem in (4, 5, 6, 7, 8):  # Cylindrical and SymTP families
         from .psi4 import cart_and_jacobian
         (x, y, z), _ = cart_and_jacobian(gp.CoordSystem, X0, X1, X2, cyl=gp)
     else:

@@ -78,6 +78,7 @@ FIXTURE_GRIDS = {
     "maxwell_curvi_sinhcyl_fd4": ("SinhCylindrical", (8, 6, 6), 4, 3, 29),
     "sw_sinhcyl_fd4": ("SinhCylindrical", (8, 6, 6), 4, 2, 30),
     "bssn_sinhcylv2_fd4": ("SinhCylindricalv2", (8, 6, 6), 4, 3, 31),
+    "bssn_sinhsymtp_fd4": ("SinhSymTP", (8, 6, 4), 4, 3, 32),
 }
 KO_DISS_STRENGTH = 0.3
 
@@ -380,7 +381,7 @@ TRUSTED += [
      ["sourceterm_trK_rhs", "sourceterm_a_rhsDD", "sourceterm_lambda_rhsU", "sourceterm_Lambdabar_rhsU"]),
 ]
 for cs in ("Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical", "SinhCylindricalv2",
-           "Cartesian"):
+           "SymTP", "SinhSymTP", "Cartesian"):
     TRUSTED.append(("rfm_" + cs, "tests", "rfm_%s__reference_metric__True__globals" % cs,
                     "import NRPy_param_funcs as par\n"
                     "import reference_metric as M\n"

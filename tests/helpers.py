@@ -32,7 +32,8 @@ def grids(system, coord, Nxx, fd_order, ng=None, **kw):
     from nrpytutorial_gb300 import Grid, default_nghosts
     ng = ng if ng is not None else default_nghosts(system, fd_order)
     G = Grid(coord, Nxx, FD_order=fd_order, NGHOSTS=ng, **kw)
-    okw = {k: v for k, v in kw.items() if k in ("AMPL", "SINHW", "RMAX", "domain", "eta", "wavespeed", "const_dr")}
+    okw = {k: v for k, v in kw.items() if k in ("AMPL", "SINHW", "RMAX", "domain", "eta", "wavespeed", "const_dr",
+                                                "bScale", "SINHWAA", "AMAX")}
     gp = og.GridParams(coord, Nxx, ng, fd_order, **okw)
     return G, gp
 

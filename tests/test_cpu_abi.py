@@ -61,7 +61,7 @@ def test_kreiss_oliger_coefficients_match_oracle(order):
 
 
 @pytest.mark.parametrize("cs", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical",
-                                "SinhCylindrical", "SinhCylindricalv2"])
+                                "SinhCylindrical", "SinhCylindricalv2", "SymTP", "SinhSymTP"])
 def test_grid_setup_and_timestep_match_oracle(cs):
     from nrpytutorial_gb300 import Grid
     kw = dict(AMPL=64.0, SINHW=0.2, RMAX=10.0)

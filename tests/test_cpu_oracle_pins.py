@@ -280,10 +280,11 @@ def test_trusted_maxwell_system_I():
 
 
 @pytest.mark.parametrize("cs", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
-                                "SinhCylindricalv2", "Cartesian"])
+                                "SinhCylindricalv2", "SymTP", "SinhSymTP", "Cartesian"])
 def test_trusted_reference_metric(cs):
     inp = TV["rfm_" + cs]["inputs"]
-    cyl = {k: inp[k] for k in ("AMPLRHO", "SINHWRHO", "AMPLZ", "SINHWZ", "const_drho", "const_dz") if k in inp}
+    cyl = {k: inp[k] for k in ("AMPLRHO", "SINHWRHO", "AMPLZ", "SINHWZ", "const_drho", "const_dz", "bScale",
+                                "SINHWAA", "AMAX") if k in inp}
     q = og.hatted_at(cs, inp.get("xx0", 0.0), inp.get("xx1", 0.0), inp.get("AMPL", 10.0), inp.get("SINHW", 0.2),
                      inp.get("const_dr", 0.0625), xx2=inp.get("xx2", 0.0), **cyl)
     n = 0
@@ -301,7 +302,7 @@ KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
         "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical",
         "bssn_sinhv2_fd4": "SinhSphericalv2", "bssn_sinhcyl_fd4": "SinhCylindrical",
-        "bssn_sinhcylv2_fd4": "SinhCylindricalv2"}
+        "bssn_sinhcylv2_fd4": "SinhCylindricalv2", "bssn_sinhsymtp_fd4": "SinhSymTP"}
 
 
 @pytest.mark.parametrize("cfg", sorted(CFGS))

@@ -11,7 +11,8 @@ pytestmark = pytest.mark.gpu
 
 CASES = [("Spherical", (4, 4, 4), 3), ("SinhSpherical", (8, 6, 4), 3), ("Cartesian", (6, 5, 7), 2),
          ("Spherical", (6, 4, 8), 2), ("SinhSpherical", (10, 8, 6), 4), ("SinhSphericalv2", (10, 8, 6), 3),
-         ("Cylindrical", (6, 6, 6), 3), ("SinhCylindrical", (8, 6, 8), 3), ("SinhCylindricalv2", (8, 6, 8), 3)]
+         ("Cylindrical", (6, 6, 6), 3), ("SinhCylindrical", (8, 6, 8), 3), ("SinhCylindricalv2", (8, 6, 8), 3),
+         ("SymTP", (8, 6, 4), 3), ("SinhSymTP", (8, 6, 8), 3)]
 
 
 @pytest.mark.parametrize("coord,Nxx,ng", CASES)

@@ -17,7 +17,8 @@ FP32_TOL = 5e-5
 CASES = [("Cartesian", (8, 8, 8), 4), ("Cartesian", (8, 6, 10), 6),
          ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4),
          ("Cartesian", (8, 6, 6), 2), ("Cartesian", (6, 8, 6), 8), ("SinhSphericalv2", (10, 8, 8), 4),
-         ("SinhCylindrical", (10, 8, 8), 4), ("Cylindrical", (8, 6, 8), 4), ("SinhCylindricalv2", (8, 8, 6), 4)]
+         ("SinhCylindrical", (10, 8, 8), 4), ("Cylindrical", (8, 6, 8), 4), ("SinhCylindricalv2", (8, 8, 6), 4),
+         ("SymTP", (8, 6, 6), 4), ("SinhSymTP", (10, 8, 6), 4)]
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 
 
@@ -28,7 +29,7 @@ def _setup(cuda, coord, Nxx, order, prec="fp64"):
 
 
 @pytest.mark.parametrize("coord", ["SinhSpherical", "Spherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
-                                   "SinhCylindricalv2"])
+                                   "SinhCylindricalv2", "SymTP", "SinhSymTP"])
 def test_rfm_tables_match_oracle(cuda, coord):
     ev, gp = _setup(cuda, coord, (10, 8, 6), 4)
     tab = ev.rfm_table()

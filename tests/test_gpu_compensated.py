@@ -46,7 +46,8 @@ CASES = [("ScalarWave", "SinhSpherical", (16, 12, 8), 4),
          ("BSSN", "Cartesian", (12, 12, 12), 4),
          ("BSSN", "SinhSpherical", (12, 10, 8), 4),
          ("BSSN", "SinhSphericalv2", (12, 10, 8), 4),
-         ("BSSN", "SinhCylindrical", (12, 10, 8), 4)]
+         ("BSSN", "SinhCylindrical", (12, 10, 8), 4),
+         ("BSSN", "SinhSymTP", (12, 10, 8), 4)]
 
 
 @pytest.mark.parametrize("system,coord,Nxx,order", CASES)

@@ -17,7 +17,7 @@ KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 CFGS = {"bssn_cart_fd2": "Cartesian", "bssn_cart_fd4": "Cartesian", "bssn_cart_fd6": "Cartesian",
         "bssn_cart_fd8": "Cartesian", "bssn_sinhsph_fd4": "SinhSpherical", "bssn_sph_fd4": "Spherical",
         "bssn_sinhv2_fd4": "SinhSphericalv2", "bssn_sinhcyl_fd4": "SinhCylindrical",
-        "bssn_sinhcylv2_fd4": "SinhCylindricalv2"}
+        "bssn_sinhcylv2_fd4": "SinhCylindricalv2", "bssn_sinhsymtp_fd4": "SinhSymTP"}
 TOL = 1e-12
 
 

@@ -18,7 +18,8 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0))
 CASES = [("Cartesian", (8, 8, 8), 4), ("Spherical", (10, 8, 6), 2), ("Spherical", (10, 8, 6), 4),
          ("SinhSpherical", (10, 8, 8), 4), ("SinhSphericalv2", (10, 8, 8), 4), ("SinhCylindrical", (10, 8, 8), 4),
-         ("Cylindrical", (8, 6, 8), 2), ("SinhCylindricalv2", (8, 8, 6), 4)]
+         ("Cylindrical", (8, 6, 8), 2), ("SinhCylindricalv2", (8, 8, 6), 4), ("SinhSymTP", (10, 8, 6), 4),
+         ("SymTP", (8, 6, 6), 2)]
 PARITY = [0, 1, 2, 3, 1, 2, 3, 0]
 
 
@@ -73,7 +74,7 @@ def test_constraints_match_oracle(cuda, coord, Nxx, order):
 
 
 @pytest.mark.parametrize("coord", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical",
-                                   "SinhCylindrical"])
+                                   "SinhCylindrical", "SymTP", "SinhSymTP"])
 def test_toroidal_dipole_data_match_oracle(cuda, coord):
     ev, gp = _evo(cuda, coord, (10, 8, 6), 4)
     ev.initial_data_toroidal_dipole(1.2, 0.9, 0.3)

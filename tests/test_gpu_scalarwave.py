@@ -36,7 +36,7 @@ def test_cartesian_rhs_matches_oracle(cuda, order):
 
 
 @pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
-                                   "SinhCylindricalv2"])
+                                   "SinhCylindricalv2", "SymTP", "SinhSymTP"])
 @pytest.mark.parametrize("order", [2, 4])
 def test_curvilinear_rhs_matches_oracle(cuda, coord, order):
     import torch
@@ -112,7 +112,7 @@ def test_plane_wave_fourth_order_convergence(cuda, prec):
 
 
 @pytest.mark.parametrize("coord", ["Cartesian", "Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical",
-                                   "SinhCylindrical"])
+                                   "SinhCylindrical", "SymTP", "SinhSymTP"])
 @pytest.mark.parametrize("kind", ["PlaneWave", "SphericalGaussian"])
 def test_initial_data_matches_oracle(cuda, coord, kind):
     G, gp = grids("ScalarWave", coord, (10, 8, 6), 4, AMPL=5.0, SINHW=0.3, RMAX=5.0, wavespeed=0.7)

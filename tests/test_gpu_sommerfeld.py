@@ -29,6 +29,8 @@ def _set(fd, ngf, falloff=3.0):
     ("ScalarWave", "SinhCylindrical", (10, 8, 8), 4, 4),
     ("ScalarWave", "Cylindrical", (8, 6, 8), 4, 2),
     ("ScalarWave", "SinhCylindricalv2", (8, 6, 8), 4, 4),
+    ("ScalarWave", "SinhSymTP", (10, 8, 6), 4, 4),
+    ("ScalarWave", "SymTP", (8, 6, 6), 4, 2),
 ])
 def test_sommerfeld_rhs_matches_oracle(cuda, system, coord, Nxx, order, fd):
     import torch
