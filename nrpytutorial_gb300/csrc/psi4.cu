@@ -405,8 +405,10 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *p, const double *in_gfs,
   double *re = psi4_gfs, *im = psi4_gfs + g.ntot;
 #define P4(CS, ORD) psi4_kernel<CS, ORD><<<grid, block, 0, stream()>>>(g, in_gfs, tab, *p, i0_min, i0_max, re, im)
   switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {
+    case NRGPU_COORD_CARTESIAN * 16 + 2: P4(NRGPU_COORD_CARTESIAN, 2); break;
     case NRGPU_COORD_CARTESIAN * 16 + 4: P4(NRGPU_COORD_CARTESIAN, 4); break;
     case NRGPU_COORD_CARTESIAN * 16 + 6: P4(NRGPU_COORD_CARTESIAN, 6); break;
+    case NRGPU_COORD_CARTESIAN * 16 + 8: P4(NRGPU_COORD_CARTESIAN, 8); break;
     case NRGPU_COORD_SINHSPHERICAL * 16 + 4: P4(NRGPU_COORD_SINHSPHERICAL, 4); break;
     case NRGPU_COORD_SINHCYLINDRICAL * 16 + 4: P4(NRGPU_COORD_SINHCYLINDRICAL, 4); break;
     case NRGPU_COORD_SINHSYMTP * 16 + 4: P4(NRGPU_COORD_SINHSYMTP, 4); break;

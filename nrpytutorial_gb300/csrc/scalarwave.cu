@@ -79,9 +79,13 @@ static int dispatch(const paramstruct *p, const Grid &g, typename InRef<Tin>::ty
   SW_CASE(NRGPU_COORD_CARTESIAN, 2) SW_CASE(NRGPU_COORD_CARTESIAN, 4)
   SW_CASE(NRGPU_COORD_CARTESIAN, 6) SW_CASE(NRGPU_COORD_CARTESIAN, 8)
   SW_CASE(NRGPU_COORD_SPHERICAL, 2) SW_CASE(NRGPU_COORD_SPHERICAL, 4)
+  SW_CASE(NRGPU_COORD_SPHERICAL, 6) SW_CASE(NRGPU_COORD_SPHERICAL, 8)
   SW_CASE(NRGPU_COORD_SINHSPHERICAL, 2) SW_CASE(NRGPU_COORD_SINHSPHERICAL, 4)
+  SW_CASE(NRGPU_COORD_SINHSPHERICAL, 6) SW_CASE(NRGPU_COORD_SINHSPHERICAL, 8)
   SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 2) SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 4)
+  SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 6) SW_CASE(NRGPU_COORD_SINHCYLINDRICAL, 8)
   SW_CASE(NRGPU_COORD_SINHSYMTP, 2) SW_CASE(NRGPU_COORD_SINHSYMTP, 4)
+  SW_CASE(NRGPU_COORD_SINHSYMTP, 6) SW_CASE(NRGPU_COORD_SINHSYMTP, 8)
 #undef SW_CASE
   set_error("ScalarWave: CoordSystem %d with FD_order %d not built", p->CoordSystem, p->FD_order);
   return NRGPU_ERR_UNSUPPORTED;

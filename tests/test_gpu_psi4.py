@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
-CASES = [("Cartesian", (8, 6, 10), 4), ("Cartesian", (8, 8, 6), 6),
+CASES = [("Cartesian", (8, 6, 10), 4), ("Cartesian", (8, 8, 6), 6), ("Cartesian", (8, 6, 6), 2),
+         ("Cartesian", (10, 8, 8), 8),
          ("SinhSpherical", (10, 8, 8), 4), ("Spherical", (8, 8, 6), 4), ("SinhSphericalv2", (10, 8, 8), 4),
          ("SinhCylindrical", (10, 8, 8), 4), ("SinhCylindricalv2", (8, 8, 6), 4), ("SinhSymTP", (10, 8, 6), 4),
          ("SymTP", (8, 6, 6), 4)]

@@ -37,7 +37,7 @@ def test_cartesian_rhs_matches_oracle(cuda, order):
 
 @pytest.mark.parametrize("coord", ["Spherical", "SinhSpherical", "SinhSphericalv2", "Cylindrical", "SinhCylindrical",
                                    "SinhCylindricalv2", "SymTP", "SinhSymTP"])
-@pytest.mark.parametrize("order", [2, 4])
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
 def test_curvilinear_rhs_matches_oracle(cuda, coord, order):
     import torch
     G, gp = grids("ScalarWave", coord, (10, 8, 6), order, AMPL=5.0, SINHW=0.3, RMAX=5.0)
