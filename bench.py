@@ -197,9 +197,11 @@ def run_gpu(args):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in zip(ev_s, ev_e)) / 1e3
 
-    def run(e):
+    def run(e, label=None):
         """K graph-replayed RK4 steps from y0 after Wm warm-up steps; returns
-        (seconds, kernel launches per step)."""
+        (seconds, kernel launches per step).  With a label, one more warm-up
+        replay runs inside an NVTX range of that name (for per-kernel
+        profiles of one step; outside the timed region)."""
         e.y_n.copy_(y0)
         for _ in range(Wm):
             e.step(dt)
@@ -210,6 +212,10 @@ def run_gpu(args):
         replay = e.capture(dt, n_steps=1)
         for _ in range(Wm):
             replay()
+        if label:
+            torch.cuda.nvtx.range_push(label)
+            replay()
+            torch.cuda.nvtx.range_pop()
         e.y_n.copy_(y0)
         barrier()
         t = timed_replays(replay, K)
@@ -235,7 +241,7 @@ def run_gpu(args):
         return float(np.mean(ts))
 
     # ---- FP64 (parity mode)
-    t64, lps64 = run(ev)
+    t64, lps64 = run(ev, "headline_step_fp64")
     y64 = ev.y_n.clone()
     H64 = ev.l2_norm(ev.hamiltonian(y64))
     g = W["ng"]
@@ -243,7 +249,7 @@ def run_gpu(args):
 
     # ---- headline: compensated mixed precision
     evc = Evolution("BSSN", G, precision="compensated", device=dev)
-    tc, lps = run(evc)
+    tc, lps = run(evc, "headline_step_compensated")
     finite = bool(torch.isfinite(evc.y_n).all().item())
     comp_err = state_errors(evc.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names)
     Hc = ev.l2_norm(ev.hamiltonian(evc.y_n))
