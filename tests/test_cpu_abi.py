@@ -145,3 +145,38 @@ def test_oracle_mixed_derivative_is_product_of_first():
     assert np.allclose(d01, (2 * X0 * 3 * X1 ** 2)[3:-3, 3:-3, 3:-3], atol=1e-10)
     assert np.allclose(S2.dup(poly, 2), X0[3:-3, 3:-3, 3:-3], atol=1e-12)
     assert np.allclose(S2.ddn(poly, 2), X0[3:-3, 3:-3, 3:-3], atol=1e-12)
+
+
+def test_struct_layouts_match_the_c_header(tmp_path):
+    """The ctypes mirrors of paramstruct, rfm_struct, bc_struct and
+    MoL_gridfunctions have the C header's size and field offsets (a C
+    program compiled against include/nrgpu.h prints them)."""
+    import shutil
+    import subprocess
+    L, _ = _lib()
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    structs = {"paramstruct": L.paramstruct, "rfm_struct": L.rfm_struct}
+    for name in ("bc_struct", "MoL_gridfunctions"):
+        if hasattr(L, name):
+            structs[name] = getattr(L, name)
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "nrgpu.h"', "int main(void) {"]
+    for sname, cls in structs.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (sname, sname))
+        for f in cls._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (sname, f[0], sname, f[0]))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I" + inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    for sname, cls in structs.items():
+        assert got[(sname, "sizeof")] == C.sizeof(cls), sname
+        for f in cls._fields_:
+            assert got[(sname, f[0])] == getattr(cls, f[0]).offset, (sname, f[0])
