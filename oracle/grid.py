@@ -260,6 +260,13 @@ def hatted_at(CoordSystem, xx0, xx1, AMPL=10.0, SINHW=0.2, const_dr=0.0625, xx2=
 
 
 def hatted_from_scale_factors(s, ds, dds):
+    # the formulas hold wherever asked; on a coordinate singularity (r = 0)
+    # they give inf/nan entries as the reference's expressions do
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return _hatted(s, ds, dds)
+
+
+def _hatted(s, ds, dds):
     s = np.array(s)
     ds = np.array(ds)
     dds = np.array(dds)
