@@ -194,6 +194,32 @@ void       *nrgpu_get_stream(void);
 const char *nrgpu_last_error(void);
 /* Number of kernels this library has launched in this process. */
 long long   nrgpu_kernel_launch_count(void);
+/* Device status word of the current device: nonzero once a kernel's bounded
+ * wait for one of its own asynchronous copies gave up (that kernel stored
+ * nothing).  Synchronises the library stream; clear != 0 resets the word.
+ * Returns the word, or -NRGPU_ERR_CUDA.  No reference counterpart. */
+int         nrgpu_device_status(int clear);
+/* Which kernels evaluate BSSN Ricci_eval / rhs_eval (no reference
+ * counterpart: the reference has one generated loop per function).
+ *   POINT:  one thread per point, every stencil tap read from global memory;
+ *   STAGED: a block per 16x4x2 brick (16x4x1 in FP64); each gridfunction's
+ *           brick-plus-halo box staged in shared memory by TMA, finite
+ *           differences evaluated there, then the algebra;
+ *   FUSED:  STAGED with Ricci computed inside the RHS kernel of a MoL step
+ *           (auxevol is neither written nor read by the step);
+ *   AUTO:   STAGED for FP32 arithmetic (mixed and compensated precision)
+ *           where the grid allows it (NGHOSTS = FD_order/2 + 1, 16-byte-
+ *           aligned stage arrays and rows), POINT otherwise and for FP64 --
+ *           the faster of the two on GB300 in each case.
+ * Kreiss-Oliger dissipation, T^{mu nu} sources, the no-precompute _xx
+ * functions and FP32 arithmetic on FP64 input always run on POINT.
+ * Process-wide setting. */
+#define NRGPU_BSSN_KERNELS_AUTO   0
+#define NRGPU_BSSN_KERNELS_POINT  1
+#define NRGPU_BSSN_KERNELS_STAGED 2
+#define NRGPU_BSSN_KERNELS_FUSED  3
+int         nrgpu_set_bssn_kernels(int mode);
+int         nrgpu_get_bssn_kernels(void);
 /* FD coefficients the kernels use: kind 0 = centred 1st, 1 = centred 2nd,
  * 2 = upwind (+1 shifted) 1st, 3 = Kreiss-Oliger.  Writes order+1 doubles
  * (offsets -order/2 ... +order/2, shifted by +1 for kind 2), order+3 for
@@ -504,8 +530,11 @@ int nrgpu_l2_norm_sq(const paramstruct *params, const double *gfs, int gf,
  * by every GPU that loads it until the process exits; a call that would need
  * more partials fails with NRGPU_ERR_SIZE.  The first call on a device looks
  * up that array's device address (cudaGetSymbolAddress) with the device
- * current, so make the first call before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU race; no cudaMalloc/cudaFree. */
+ * current, so make the first call before any stream capture.  The cached
+ * address is that context's: after cudaDeviceReset (or any teardown of the
+ * device's primary context) it is stale, so do not call this entry point
+ * again in that process.  All calls share the array, so calls that overlap
+ * on the GPU race; no cudaMalloc/cudaFree. */
 int nrgpu_l2_norm_sq_static(const paramstruct *params, const double *gfs, int gf, double *result);
 
 #ifdef __cplusplus

@@ -13,6 +13,7 @@ COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 
          "SinhCylindrical": 5, "SinhCylindricalv2": 6, "SymTP": 7, "SinhSymTP": 8}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
 PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
+BSSN_KERNELS = {"auto": 0, "point": 1, "staged": 2, "fused": 3}
 MAX_GHOSTS = 8
 MAX_BC_LEVELS = 32
 
@@ -77,6 +78,9 @@ _PROTOS = {
     "nrgpu_get_stream": (vp, []),
     "nrgpu_last_error": (C.c_char_p, []),
     "nrgpu_kernel_launch_count": (C.c_longlong, []),
+    "nrgpu_device_status": (C.c_int, [C.c_int]),
+    "nrgpu_set_bssn_kernels": (C.c_int, [C.c_int]),
+    "nrgpu_get_bssn_kernels": (C.c_int, []),
     "nrgpu_fd_coeffs": (C.c_int, [C.c_int, C.c_int, P(C.c_double)]),
     "set_Nxx_dxx_invdx_params__and__xx": (C.c_int, [C.c_int, P(C.c_int), P(paramstruct), P(P(C.c_double))]),
     "find_timestep": (C.c_double, [P(paramstruct), C.c_double]),

@@ -39,11 +39,22 @@ def _newest_header():
 
 
 def build(verbose=False, ptxas_verbose=False, jobs=None):
+    """Compiles what changed.  $NRGPU_DEFINES (e.g. "-DNRGPU_STAGED_NBUF=3")
+    adds preprocessor settings of the kernels' tunables; a change of them
+    rebuilds everything."""
     os.makedirs(BUILD, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    defines = [d for d in os.environ.get("NRGPU_DEFINES", "").split() if d.startswith("-D")]
+    stamp = os.path.join(BUILD, "defines.txt")
+    old = open(stamp).read() if os.path.exists(stamp) else ""
+    if old != " ".join(defines):
+        for o in glob.glob(os.path.join(BUILD, "*.o")):
+            os.remove(o)
+        with open(stamp, "w") as f:
+            f.write(" ".join(defines))
     hdr_t = _newest_header()
     nv = nvcc()
-    extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    extra = (["-Xptxas", "-v"] if ptxas_verbose else []) + defines
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")

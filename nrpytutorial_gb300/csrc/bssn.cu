@@ -3,6 +3,7 @@
 #include <math.h>
 
 #include "bssn_kernels.cuh"
+#include "bssn_staged.cuh"
 
 namespace nrgpu {
 namespace bssn {
@@ -15,6 +16,25 @@ NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHCYLINDRICAL, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SINHSYMTP, 4)
 NRGPU_BSSN_DECLARE(NRGPU_COORD_SPHERICAL, 4)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_CARTESIAN, 2)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_CARTESIAN, 4)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_CARTESIAN, 6)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_CARTESIAN, 8)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SINHSPHERICAL, 4)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SINHCYLINDRICAL, 4)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SINHSYMTP, 4)
+NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SPHERICAL, 4)
+
+// Which BSSN Ricci/RHS kernels run (nrgpu_set_bssn_kernels).
+static int g_kernels = NRGPU_BSSN_KERNELS_AUTO;
+// AUTO takes the staged kernels for FP32 arithmetic and the point kernels
+// for FP64, whichever measured faster on GB300 at the headline grid (the
+// FP64 kernels are FP64-pipe bound; the staged FP64 form's slot arrays halve
+// its occupancy).
+static bool staged_for(int prec) {
+  return g_kernels == NRGPU_BSSN_KERNELS_STAGED || g_kernels == NRGPU_BSSN_KERNELS_FUSED ||
+         (g_kernels == NRGPU_BSSN_KERNELS_AUTO && prec != NRGPU_PREC_FP64);
+}
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
   switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {                                   \
@@ -433,11 +453,20 @@ __global__ void constraint_sources_kernel(Grid g, const double *__restrict__ in,
 using namespace bssn;
 
 #define RICCI_CALL(CS, ORD) ricci_launch_t<CS, ORD>(rfm, p, in, in_is_f64, prec, auxevol)
+#define STAGED_RICCI_CALL(CS, ORD) staged_ricci_launch_t<CS, ORD>(rfm, p, in, in_is_f64, prec, auxevol)
+static int staged_ricci(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64, int prec,
+                        void *auxevol) {
+  NRGPU_BSSN_SWITCH(STAGED_RICCI_CALL)
+}
 int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64, int prec,
                       void *auxevol) {
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(in && auxevol, "NULL gridfunctions");
+  if (staged_for(prec)) {
+    st = staged_ricci(rfm, p, in, in_is_f64, prec, auxevol);
+    if (st != NRGPU_ERR_UNSUPPORTED) return st;
+  }
   NRGPU_BSSN_SWITCH(RICCI_CALL)
 }
 static bool extras_on(const paramstruct *p) {
@@ -445,11 +474,34 @@ static bool extras_on(const paramstruct *p) {
 }
 #define RHS_CALL(CS, ORD) \
   (extras_on(p) ? rhs_launch_t<CS, ORD, true>(rfm, p, a) : rhs_launch_t<CS, ORD, false>(rfm, p, a))
+#define STAGED_RHS_CALL(CS, ORD) staged_rhs_launch_t<CS, ORD>(rfm, p, a, fused)
+static int staged_rhs(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a, bool fused) {
+  NRGPU_BSSN_SWITCH(STAGED_RHS_CALL)
+}
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
+  // Kreiss-Oliger dissipation and T^{mu nu} sources run on the point kernels.
+  if (staged_for(a.prec) && !extras_on(p)) {
+    st = staged_rhs(rfm, p, a, false);
+    if (st != NRGPU_ERR_UNSUPPORTED) return st;
+  }
   NRGPU_BSSN_SWITCH(RHS_CALL)
+}
+// One MoL substep's Ricci + RHS: the fused staged kernel when selected,
+// else Ricci_eval then rhs_eval.
+int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a) {
+  int st = check_bssn(rfm, p);
+  if (st) return st;
+  NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
+  if (g_kernels == NRGPU_BSSN_KERNELS_FUSED && !extras_on(p)) {
+    st = staged_rhs(rfm, p, a, true);
+    if (st != NRGPU_ERR_UNSUPPORTED) return st;
+  }
+  st = bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
+  if (st) return st;
+  return bssn_rhs_launch(rfm, p, a);
 }
 
 int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair, bool ff_f64) {
@@ -502,6 +554,13 @@ static int bssn_plain(const rfm_struct *rfm, const paramstruct *p, const void *a
 }
 
 extern "C" {
+int nrgpu_set_bssn_kernels(int mode) {
+  NRGPU_REQUIRE(mode >= NRGPU_BSSN_KERNELS_AUTO && mode <= NRGPU_BSSN_KERNELS_FUSED, "unknown BSSN kernel mode %d",
+                mode);
+  g_kernels = mode;
+  return NRGPU_OK;
+}
+int nrgpu_get_bssn_kernels(void) { return g_kernels; }
 int BSSN_Ricci_eval(const rfm_struct *rfm, const paramstruct *p, const double *in, double *aux) {
   return bssn_ricci_launch(rfm, p, in, true, NRGPU_PREC_FP64, aux);
 }

@@ -57,6 +57,22 @@ template <int ORDER, typename R, typename Tin>
 __device__ __forceinline__ R DUP(const Point<Tin> &P, int g, int d, const R *inv, const bool *pos) {
   return fd_dupwind<ORDER, R>(P.gf(g), P.st[d], pos[d]) * inv[d];
 }
+// Value of gridfunction g at the point.
+template <typename R, typename Tin> __device__ __forceinline__ R pval(const Point<Tin> &P, int g) {
+  return val<R>(P.gf(g));
+}
+// Advection of gridfunction g along the shift, beta^k d_k g with every d_k
+// upwinded by the sign of beta^k.  The reference's RHSs use the upwinded
+// derivatives (dupD symbols) only in these contractions with beta^k
+// (BSSN_RHSs.py:69-318, BSSN_gauge_RHSs.py:61-67, 191-255), so each
+// gridfunction contributes this one scalar.
+template <int ORDER, typename R, typename Tin>
+__device__ __forceinline__ R ADV(const Point<Tin> &P, int g, const R *betaU, const bool *pos, const R *inv) {
+  R s = (R)0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) s += betaU[k] * DUP<ORDER, R>(P, g, k, inv, pos);
+  return s;
+}
 
 // Symmetric 3x3 inverse via the adjugate (indexedexp.py:331, symm_matrix_inverter3x3).
 template <typename R>
@@ -85,8 +101,8 @@ template <int CS, typename R> struct Metric {
   R Gbar[3][3][3];   // Gammabar^i_kl
 };
 
-template <int ORDER, int CS, typename R, typename Tin, bool LOC>
-__device__ __forceinline__ void metric_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf, const R *inv,
+template <int ORDER, int CS, typename R, typename PT, bool LOC>
+__device__ __forceinline__ void metric_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                              Metric<CS, R> &m) {
   using M = RfmMask<CS>;
 #pragma unroll
@@ -94,7 +110,7 @@ __device__ __forceinline__ void metric_point(const Point<Tin> &P, const Rfm<CS, 
 #pragma unroll
     for (int j = i; j < 3; j++) {
       const int g = HDD00 + S6(i, j);
-      const R hij = val<R>(P.gf(g));
+      const R hij = pval<R>(P, g);
       m.h[i][j] = m.h[j][i] = hij;
       const R e = M::trivial ? hij : hij * rf.ReDD(i, j);
       m.eps[i][j] = m.eps[j][i] = e;
@@ -156,8 +172,8 @@ __device__ __forceinline__ void delta_gamma(const Metric<CS, R> &m, const Rfm<CS
 // ------------------------------------------------------------------ Ricci
 // Rbar_ij (BSSN_quantities.py:260-425), needs second derivatives of hDD and
 // first derivatives of lambdaU.
-template <int ORDER, int CS, typename R, typename Tin, bool LOC>
-__device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf, const R *inv,
+template <int ORDER, int CS, typename R, typename PT, bool LOC>
+__device__ __forceinline__ void ricci_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                             const Metric<CS, R> &m, R Rbar[6]) {
   using M = RfmMask<CS>;
   R DG[3][3][3], DGU[3];
@@ -196,7 +212,7 @@ __device__ __forceinline__ void ricci_point(const Point<Tin> &P, const Rfm<CS, R
   // lambda: \hat{D}_j Lambdabar^k (LambarU_dHatD)
   R lam[3], LdH[3][3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) lam[k] = val<R>(P.gf(LAMBDAU0 + k));
+  for (int k = 0; k < 3; k++) lam[k] = pval<R>(P, LAMBDAU0 + k);
 #pragma unroll
   for (int k = 0; k < 3; k++)
 #pragma unroll
@@ -290,13 +306,13 @@ __device__ __forceinline__ void momentum_point(const Point<Tin> &P, const Rfm<CS
   using M = RfmMask<CS>;
   Metric<CS, R> m;
   metric_point<ORDER, CS, R>(P, rf, inv, m);
-  const R cf = val<R>(P.gf(CF));
+  const R cf = pval<R>(P, CF);
   R a[3][3], Abar[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      a[i][j] = a[j][i] = val<R>(P.gf(ADD00 + S6(i, j)));
+      a[i][j] = a[j][i] = pval<R>(P, ADD00 + S6(i, j));
       Abar[i][j] = Abar[j][i] = M::trivial ? a[i][j] : a[i][j] * rf.ReDD(i, j);
     }
   R AUD[3][3], AUU[3][3];
@@ -357,22 +373,22 @@ __device__ __forceinline__ void momentum_point(const Point<Tin> &P, const Rfm<CS
 
 // -------------------------------------------------------------------- RHS
 // All 24 right-hand sides at one interior point, in gridfunction order.
-template <int ORDER, int CS, typename R, typename Tin, bool LOC>
-__device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf, const R *inv,
+template <int ORDER, int CS, typename R, typename PT, bool LOC>
+__device__ __forceinline__ void rhs_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                           const R Rbar[6], R eta, R out[NUM_EVOL_GFS]) {
   using M = RfmMask<CS>;
   Metric<CS, R> m;
   metric_point<ORDER, CS, R>(P, rf, inv, m);
 
-  const R alpha = val<R>(P.gf(ALPHA));
-  const R cf = val<R>(P.gf(CF));
-  const R trK = val<R>(P.gf(TRK));
+  const R alpha = pval<R>(P, ALPHA);
+  const R cf = pval<R>(P, CF);
+  const R trK = pval<R>(P, TRK);
   R vet[3], bet[3], lam[3], betaU[3], BU[3], LambdabarU[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    vet[i] = val<R>(P.gf(VETU0 + i));
-    bet[i] = val<R>(P.gf(BETU0 + i));
-    lam[i] = val<R>(P.gf(LAMBDAU0 + i));
+    vet[i] = pval<R>(P, VETU0 + i);
+    bet[i] = pval<R>(P, BETU0 + i);
+    lam[i] = pval<R>(P, LAMBDAU0 + i);
     betaU[i] = M::trivial ? vet[i] : vet[i] * rf.ReU(i);
     BU[i] = M::trivial ? bet[i] : bet[i] * rf.ReU(i);
     LambdabarU[i] = M::trivial ? lam[i] : lam[i] * rf.ReU(i);
@@ -382,8 +398,19 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
 #pragma unroll
   for (int d = 0; d < 3; d++) pos[d] = betaU[d] > (R)0;
 
-  // beta^i_{,j}, beta^i_{,jk}, upwinded beta^i_{,j} (BSSN_quantities.py:431-456)
-  R vetd[3][3], betad[3][3], betadup[3][3], betadd[3][3][3];
+  // beta^j d_j (f^i ReU^i) for a rescaled vector f (upwinded): ReU^i times
+  // the advection of f^i, plus f^i beta^j d_j ReU^i.
+  auto vec_adv = [&](int g0, int i, R fi) -> R {
+    R u = ADV<ORDER, R>(P, g0 + i, betaU, pos, inv);
+    if constexpr (!M::trivial) u *= rf.ReU(i);
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      if (M::ReUdD(i, j)) u += betaU[j] * fi * rf.ReUdD(i, j);
+    return u;
+  };
+
+  // beta^i_{,j}, beta^i_{,jk} (BSSN_quantities.py:431-456)
+  R vetd[3][3], betad[3][3], betadd[3][3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -392,10 +419,6 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
       R v = M::trivial ? vetd[i][j] : vetd[i][j] * rf.ReU(i);
       if (M::ReUdD(i, j)) v += vet[i] * rf.ReUdD(i, j);
       betad[i][j] = v;
-      R u = DUP<ORDER, R>(P, VETU0 + i, j, inv, pos);
-      if constexpr (!M::trivial) u *= rf.ReU(i);
-      if (M::ReUdD(i, j)) u += vet[i] * rf.ReUdD(i, j);
-      betadup[i][j] = u;
     }
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -417,7 +440,7 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      a[i][j] = a[j][i] = val<R>(P.gf(ADD00 + S6(i, j)));
+      a[i][j] = a[j][i] = pval<R>(P, ADD00 + S6(i, j));
       Abar[i][j] = Abar[j][i] = M::trivial ? a[i][j] : a[i][j] * rf.ReDD(i, j);
     }
   R AUD[3][3], AUU[3][3], trAbar = (R)0;
@@ -453,12 +476,11 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
   }
 
   // phi derivatives for W = e^{-2 phi} (BSSN_quantities.py:496-508)
-  R cfd[3], phid[3], phidup[3], phidd[3][3];
+  R cfd[3], phid[3], phidd[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     cfd[i] = D1<ORDER, R>(P, CF, i, inv);
     phid[i] = -cfd[i] / ((R)2 * cf);
-    phidup[i] = -DUP<ORDER, R>(P, CF, i, inv, pos) / ((R)2 * cf);
   }
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -506,21 +528,22 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
 #pragma unroll
     for (int j = i; j < 3; j++) {
       const int gij = S6(i, j);
-      R grhs = (R)0, arhs = (R)0;
+      // upwinded beta^k d_k gammabar_ij and beta^k d_k Abar_ij
+      R grhs = ADV<ORDER, R>(P, HDD00 + gij, betaU, pos, inv);
+      R arhs = ADV<ORDER, R>(P, ADD00 + gij, betaU, pos, inv);
+      if constexpr (!M::trivial) {
+        grhs *= rf.ReDD(i, j);
+        arhs *= rf.ReDD(i, j);
+      }
 #pragma unroll
       for (int k = 0; k < 3; k++) {
-        // upwinded d_k gammabar_ij and d_k Abar_ij
-        R hup = DUP<ORDER, R>(P, HDD00 + gij, k, inv, pos);
-        R aup = DUP<ORDER, R>(P, ADD00 + gij, k, inv, pos);
-        R gdup = M::trivial ? hup : hup * rf.ReDD(i, j);
-        R adup = M::trivial ? aup : aup * rf.ReDD(i, j);
         if (M::ReDDdD(i, j, k)) {
-          gdup += m.h[i][j] * rf.ReDDdD(i, j, k);
-          adup += rf.ReDDdD(i, j, k) * a[i][j];
+          grhs += betaU[k] * (m.h[i][j] * rf.ReDDdD(i, j, k));
+          arhs += betaU[k] * (rf.ReDDdD(i, j, k) * a[i][j]);
         }
-        if (M::ghatDDdD(i, j, k)) gdup += rf.ghatDDdD(i, j, k);
-        grhs += betaU[k] * gdup + betad[k][i] * m.gbar[k][j] + betad[k][j] * m.gbar[i][k];
-        arhs += betaU[k] * adup + betad[k][i] * Abar[k][j] + betad[k][j] * Abar[i][k];
+        if (M::ghatDDdD(i, j, k)) grhs += betaU[k] * rf.ghatDDdD(i, j, k);
+        grhs += betad[k][i] * m.gbar[k][j] + betad[k][j] * m.gbar[i][k];
+        arhs += betad[k][i] * Abar[k][j] + betad[k][j] * Abar[i][k];
       }
       grhs += (R)(2.0 / 3.0) * m.gbar[i][j] * (alpha * trAbar - Dbarbeta);
       grhs += (R)-2 * alpha * Abar[i][j];
@@ -540,9 +563,9 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
 
   // ---- cf RHS for W (BSSN_RHSs.py:167-194)
   {
+    // beta^k d_k phi upwinded: -beta^k d_k cf / (2 cf)
     R phirhs = (R)(1.0 / 6.0) * (Dbarbeta - alpha * trK);
-#pragma unroll
-    for (int k = 0; k < 3; k++) phirhs += betaU[k] * phidup[k];
+    phirhs += -ADV<ORDER, R>(P, CF, betaU, pos, inv) / ((R)2 * cf);
     out[CF] = phirhs * ((R)-2 * cf);
   }
 
@@ -550,7 +573,7 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
   {
     R r = (R)(1.0 / 3.0) * alpha * trK * trK;
 #pragma unroll
-    for (int i = 0; i < 3; i++) r += betaU[i] * DUP<ORDER, R>(P, TRK, i, inv, pos);
+    r += ADV<ORDER, R>(P, TRK, betaU, pos, inv);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -566,16 +589,10 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
   // ---- Lambdabar^i RHS (BSSN_RHSs.py:225-318)
   R DG[3][3][3], DGU[3];
   delta_gamma<CS, R>(m, rf, DG, DGU);
-  R LdUp[3][3];  // LambdabarU_dupD
+  // beta^k LambdabarU_dupD[i][k], upwinded
+  R LAdv[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      R v = DUP<ORDER, R>(P, LAMBDAU0 + i, j, inv, pos);
-      if constexpr (!M::trivial) v *= rf.ReU(i);
-      if (M::ReUdD(i, j)) v += lam[i] * rf.ReUdD(i, j);
-      LdUp[i][j] = v;
-    }
+  for (int i = 0; i < 3; i++) LAdv[i] = vec_adv(LAMBDAU0, i, lam[i]);
   R trKd[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) trKd[j] = D1<ORDER, R>(P, TRK, j, inv);
@@ -605,7 +622,8 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
     R r = (R)0;
     // Term 1
 #pragma unroll
-    for (int k = 0; k < 3; k++) r += betaU[k] * LdUp[i][k] - betad[i][k] * LambdabarU[k];
+    for (int k = 0; k < 3; k++) r += -betad[i][k] * LambdabarU[k];
+    r += LAdv[i];
     // Term 2: gammabar^jk (beta^i_{,kj} + hatted pieces)
 #pragma unroll
     for (int j = 0; j < 3; j++)
@@ -658,21 +676,13 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
   // (BSSN_gauge_RHSs.py:61-67, :191-255)
   {
     R r = (R)-2 * alpha * trK;
-#pragma unroll
-    for (int i = 0; i < 3; i++) r += betaU[i] * DUP<ORDER, R>(P, ALPHA, i, inv, pos);
+    r += ADV<ORDER, R>(P, ALPHA, betaU, pos, inv);
     out[ALPHA] = r;
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    R brhs = (R)0, Brhs = (R)0;
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      brhs += betaU[j] * betadup[i][j];
-      R bup = DUP<ORDER, R>(P, BETU0 + i, j, inv, pos);
-      if constexpr (!M::trivial) bup *= rf.ReU(i);
-      if (M::ReUdD(i, j)) bup += bet[i] * rf.ReUdD(i, j);
-      Brhs += betaU[j] * bup;
-    }
+    // upwinded beta^j d_j beta^i and beta^j d_j B^i
+    R brhs = vec_adv(VETU0, i, vet[i]), Brhs = vec_adv(BETU0, i, bet[i]);
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll
@@ -683,8 +693,7 @@ __device__ __forceinline__ void rhs_point(const Point<Tin> &P, const Rfm<CS, R, 
 #pragma unroll
       for (int mm = 0; mm < 3; mm++) Brhs += betaU[j] * m.Gbar[i][mm][j] * BU[mm];
     Brhs += (R)(3.0 / 4.0) * Lrhs[i];
-#pragma unroll
-    for (int j = 0; j < 3; j++) Brhs += (R)(-3.0 / 4.0) * betaU[j] * LdUp[i][j];
+    Brhs += (R)(-3.0 / 4.0) * LAdv[i];
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll

@@ -79,13 +79,13 @@ template <int CS, typename R, typename Tin, bool LOC>
 __device__ __forceinline__ void source_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf,
                                              const R *__restrict__ T4, long long ntot, R *out) {
   using M = RfmMask<CS>;
-  const R alpha = val<R>(P.gf(ALPHA)), cf = val<R>(P.gf(CF));
+  const R alpha = pval<R>(P, ALPHA), cf = pval<R>(P, CF);
   R gbar[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = i; j < 3; j++) {
-      const R h = val<R>(P.gf(HDD00 + S6(i, j)));
+      const R h = pval<R>(P, HDD00 + S6(i, j));
       R v = M::trivial ? h : h * rf.ReDD(i, j);
       if (i == j) v += rf.ghatDD(i);
       gbar[i][j] = gbar[j][i] = v;
@@ -99,7 +99,7 @@ __device__ __forceinline__ void source_point(const Point<Tin> &P, const Rfm<CS, 
     R bD = (R)0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      const R vet = val<R>(P.gf(VETU0 + j));
+      const R vet = pval<R>(P, VETU0 + j);
       bD += e4 * gbar[i][j] * (M::trivial ? vet : vet * rf.ReU(j));
       P4[i][j + 1] = e4 * gbar[i][j];
     }

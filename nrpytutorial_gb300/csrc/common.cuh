@@ -12,6 +12,9 @@ namespace nrgpu {
 void set_error(const char *fmt, ...);
 cudaStream_t stream();
 void count_launch(int n = 1);
+// Device address of the library's status word on the current device (set by
+// a kernel whose bounded wait gave up), or NULL.
+int *device_status_word();
 
 #define NRGPU_CUDA_CHECK(call)                                                   \
   do {                                                                           \

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 
@@ -102,14 +103,25 @@ __global__ void rk4_update_kernel(int stage, double dt, StageConsts kc, long lon
   }
 }
 
+// SM count of the current device, cached per device ordinal (grid sizes of
+// the reductions and update loops depend on the device they run on).
 static int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
   }
+  if (dev >= 0 && dev < 64) {
+    const int c = cached[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = 152;
+  }
+  if (dev >= 0 && dev < 64) cached[dev].store(n, std::memory_order_relaxed);
   return n;
 }
 
@@ -119,9 +131,7 @@ static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, co
     case NRGPU_SYS_MAXWELL: return maxwell_launch(p, a);
     case NRGPU_SYS_MAXWELL_CURVILINEAR: return maxwell_curvi_launch(rfm, p, a);
     case NRGPU_SYS_BSSN: {
-      int st = bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
-      if (st) return st;
-      return bssn_rhs_launch(rfm, p, a);
+      return bssn_stage_launch(rfm, p, a);
     }
   }
   set_error("unknown system %d", system);
@@ -448,6 +458,11 @@ extern "C" int nrgpu_l2_norm_sq_static(const paramstruct *p, const double *gfs, 
   {
     // One-time set-up per device, with that device current: the host-side
     // name of the array is not a device address, so look the address up.
+    // The cached address belongs to the device's current context: after a
+    // cudaDeviceReset (or any teardown of the primary context) the library
+    // module is loaded again, possibly elsewhere, and this cached address
+    // is stale -- callers that reset a device must not use this entry point
+    // afterwards in the same process.
     std::lock_guard<std::mutex> lock(g_l2_static_mutex);
     if (!g_l2_static_ptr[dev]) {
       void *addr = nullptr;

@@ -35,6 +35,7 @@ int maxwell_curvi_launch(const rfm_struct *rfm, const paramstruct *p, const Stag
 int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, bool in_is_f64,
                       int prec, void *auxevol);
 int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
+int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 // is_f64: double array; otherwise float, or float2 pairs when pair is set
 // ff_f64: FP64 data rescaled in float-float arithmetic (the FP32-stage steps' state)
 int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair = false,

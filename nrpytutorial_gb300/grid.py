@@ -55,9 +55,9 @@ class Grid:
         p.AMPLRHO, p.SINHWRHO, p.AMPLZ, p.SINHWZ = AMPLRHO, SINHWRHO, AMPLZ, SINHWZ  # SinhCylindrical
         p.const_drho, p.const_dz = const_drho, const_dz  # SinhCylindricalv2
         p.bScale, p.SINHWAA, p.AMAX = bScale, SINHWAA, AMAX  # SymTP family (reference defaults)
-        lo, hi = domain
-        p.xmin = p.ymin = p.zmin = lo
-        p.xmax = p.ymax = p.zmax = hi
+        # Cartesian extent: (lo, hi) on every axis, or one (lo, hi) per axis
+        ext = [tuple(d) for d in domain] if np.ndim(domain) == 2 else [tuple(domain)] * 3
+        (p.xmin, p.xmax), (p.ymin, p.ymax), (p.zmin, p.zmax) = ext
         p.eta, p.wavespeed, p.time = eta, wavespeed, 0.0
         p.diss_strength = diss_strength  # Kreiss-Oliger dissipation of the BSSN RHSs (0 = off)
         p.enable_stress_energy_source_terms = int(bool(stress_energy_source_terms))  # T4UU in auxevol 6..15

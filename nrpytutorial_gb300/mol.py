@@ -166,6 +166,16 @@ class Evolution:
                                                           _lib.ptr(rhs_gfs))
         _lib.check(st, "rhs_eval")
 
+    def rhs_eval_given_ricci(self, in_gfs, auxevol, rhs_gfs):
+        """BSSN rhs_eval alone, with RbarDD supplied in auxevol (the reference's
+        LeaveRicciSymbolic form: rhs_eval(rfmstruct, params, auxevol_gfs,
+        in_gfs, rhs_gfs) after a separate Ricci_eval)."""
+        self._sync_stream()
+        sfx = "_f32" if in_gfs.dtype == torch.float32 else ""
+        _lib.check(getattr(self.lib, "BSSN_rhs_eval" + sfx)(self._rfm(), C.byref(self.grid.params),
+                                                            _lib.ptr(auxevol), _lib.ptr(in_gfs),
+                                                            _lib.ptr(rhs_gfs)), "BSSN_rhs_eval")
+
     def ricci_eval(self, in_gfs, auxevol):
         self._sync_stream()
         sfx = "_f32" if in_gfs.dtype == torch.float32 else ""

@@ -21,3 +21,18 @@ def cuda():
     from nrpytutorial_gb300 import _lib
     _lib.load()
     return torch.device("cuda:0")
+
+
+@pytest.fixture(params=["point", "staged", "fused"])
+def bssn_kernels(request, cuda):
+    """Runs a BSSN test once per kernel family (nrgpu_set_bssn_kernels): the
+    point kernels, the shared-memory staged kernels, and the staged kernels
+    with Ricci fused into the MoL step's RHS kernel.  Afterwards the library's
+    device status word must be clear (no bounded wait gave up)."""
+    import nrpytutorial_gb300 as pkg
+    prev = pkg.set_bssn_kernels(request.param)
+    try:
+        yield request.param
+    finally:
+        pkg.set_bssn_kernels(prev)
+    assert pkg.device_status() == 0

@@ -46,7 +46,7 @@ def test_rfm_tables_match_oracle(cuda, coord):
 
 
 @pytest.mark.parametrize("coord,Nxx,order", CASES)
-def test_ricci_matches_oracle(cuda, coord, Nxx, order):
+def test_ricci_matches_oracle(cuda, bssn_kernels, coord, Nxx, order):
     import torch
     ev, gp = _setup(cuda, coord, Nxx, order)
     f = bssn_random_state(gp.shape, seed=order)
@@ -58,7 +58,7 @@ def test_ricci_matches_oracle(cuda, coord, Nxx, order):
 
 
 @pytest.mark.parametrize("coord,Nxx,order", CASES)
-def test_rhs_matches_oracle(cuda, coord, Nxx, order):
+def test_rhs_matches_oracle(cuda, bssn_kernels, coord, Nxx, order):
     import torch
     ev, gp = _setup(cuda, coord, Nxx, order)
     f = bssn_random_state(gp.shape, seed=100 + order)
@@ -103,7 +103,7 @@ def test_enforce_detgammabar_matches_oracle(cuda, coord):
 
 
 @pytest.mark.parametrize("coord,Nxx,order", CASES[:3])
-def test_hamiltonian_matches_oracle(cuda, coord, Nxx, order):
+def test_hamiltonian_matches_oracle(cuda, bssn_kernels, coord, Nxx, order):
     ev, gp = _setup(cuda, coord, Nxx, order)
     import torch
     f = bssn_random_state(gp.shape, seed=9)
@@ -151,7 +151,7 @@ def test_momentum_constraint_matches_oracle(cuda, coord, Nxx, order):
 
 @pytest.mark.parametrize("coord,Nxx,order", [CASES[0], CASES[2]])
 @pytest.mark.parametrize("fused", [True, False])
-def test_rk4_step_matches_oracle(cuda, coord, Nxx, order, fused):
+def test_rk4_step_matches_oracle(cuda, bssn_kernels, coord, Nxx, order, fused):
     import torch
     from nrpytutorial_gb300 import SYSTEM_GFS
     ev, gp = _setup(cuda, coord, Nxx, order)
@@ -171,7 +171,7 @@ def test_rk4_step_matches_oracle(cuda, coord, Nxx, order, fused):
     assert per_gf_rel(ev.y_n.cpu().numpy(), yo) < 1e-12
 
 
-def test_cuda_graph_replay_matches_eager_steps(cuda):
+def test_cuda_graph_replay_matches_eager_steps(cuda, bssn_kernels):
     """Three RK4 steps replayed from a captured CUDA graph give the same bits
     as three eager steps."""
     import torch

@@ -26,7 +26,7 @@ def _load(cfg):
 
 
 @pytest.mark.parametrize("cfg", sorted(CFGS))
-def test_bssn_matches_reference_generated_c(cuda, cfg):
+def test_bssn_matches_reference_generated_c(cuda, bssn_kernels, cfg):
     import torch
     from nrpytutorial_gb300 import Evolution
     z = _load(cfg)
@@ -43,8 +43,7 @@ def test_bssn_matches_reference_generated_c(cuda, cfg):
     aux_ref = np.zeros((6,) + gp.shape)
     aux_ref[I] = z["ricci"]
     out = torch.zeros_like(t)
-    from bench import _rhs_only
-    _rhs_only(ev, t, torch.tensor(aux_ref, device=cuda), out)
+    ev.rhs_eval_given_ricci(t, torch.tensor(aux_ref, device=cuda), out)
     assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
     H = ev.hamiltonian(t).cpu().numpy()[0]
     assert per_gf_rel(H[None, g:-g, g:-g, g:-g], z["hamiltonian"][None]) < TOL
@@ -63,7 +62,6 @@ def test_kreiss_oliger_rhs_matches_reference_generated_c(cuda, cfg, cs):
     import ctypes as C
     import torch
     from nrpytutorial_gb300 import Evolution, _lib
-    from bench import _rhs_only
     z = _load(cfg)
     diss = float(z["diss_strength"])
     G, gp = grids("BSSN", cs, tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]), diss_strength=diss, **KW)
@@ -74,7 +72,7 @@ def test_kreiss_oliger_rhs_matches_reference_generated_c(cuda, cfg, cs):
     g = gp.NGHOSTS
     I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
     out = torch.zeros_like(t)
-    _rhs_only(ev, t, aux, out)
+    ev.rhs_eval_given_ricci(t, aux, out)
     assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
     xx = [torch.tensor(np.asarray(G.xx[d]), dtype=torch.float64, device=cuda) for d in range(3)]
     xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
@@ -91,7 +89,6 @@ def test_source_terms_rhs_matches_reference_generated_c(cuda):
     import ctypes as C
     import torch
     from nrpytutorial_gb300 import Evolution, _lib
-    from bench import _rhs_only
     z = _load("bssn_src_sinhsph_fd4")
     G, gp = grids("BSSN", "SinhSpherical", tuple(z["Nxx"]), int(z["fd"]), ng=int(z["ng"]),
                   stress_energy_source_terms=True, **KW)
@@ -101,7 +98,7 @@ def test_source_terms_rhs_matches_reference_generated_c(cuda):
     g = gp.NGHOSTS
     I = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
     out = torch.zeros_like(t)
-    _rhs_only(ev, t, aux, out)
+    ev.rhs_eval_given_ricci(t, aux, out)
     assert per_gf_rel(out.cpu().numpy()[I], z["rhs"]) < TOL
     xx = [torch.tensor(np.asarray(G.xx[d]), dtype=torch.float64, device=cuda) for d in range(3)]
     xxp = (C.c_void_p * 3)(*[x.data_ptr() for x in xx])
