@@ -142,8 +142,8 @@ class GridParams:
         ecs = CYL if (EigenCoord and cs in (SINHCYL, SINHCYLV2)) else ecs
         ecs = SYMTP if (EigenCoord and cs == SINHSYMTP) else ecs
         if ecs == CART:
-            lo, hi = domain
-            self.xxmin, self.xxmax = [lo] * 3, [hi] * 3
+            ext = [tuple(d) for d in domain] if np.ndim(domain) == 2 else [tuple(domain)] * 3
+            self.xxmin, self.xxmax = [e[0] for e in ext], [e[1] for e in ext]
         elif ecs == CYL:
             self.xxmin, self.xxmax = [0.0, -np.pi, ZMIN], [RHOMAX, np.pi, ZMAX]
         elif symtp(ecs):  # :317-322
