@@ -256,6 +256,33 @@ def run_gpu(args):
     value = world * K * nint * 4 / tc
     launches = lps * K
 
+    # ---- the FP64-accumulation form: FP32 RHS on pair stages, RK update and
+    # det(gammabar) rescale in FP64 arithmetic
+    evf = Evolution("BSSN", G, precision="compensated_fp64rk", device=dev)
+    tf, lpsf = run(evf)
+    f_err = state_errors(evf.y_n[:, g:-g, g:-g, g:-g], y64[:, g:-g, g:-g, g:-g], c0, ev.gf_names)
+    Hf = ev.l2_norm(ev.hamiltonian(evf.y_n))
+
+    # ---- error legs over the configuration's 200 steps (untimed), whatever K is
+    def evolve_from_y0(e, n):
+        e.y_n.copy_(y0)
+        e.capture(dt, n_steps=n)()
+        torch.cuda.synchronize()
+        return e.y_n[:, g:-g, g:-g, g:-g].clone()
+
+    N200 = 200
+    y64_200 = evolve_from_y0(ev, N200)
+    H64_200 = ev.l2_norm(ev.hamiltonian(ev.y_n))
+    err200 = {}
+    for name, e in (("compensated", evc), ("compensated_fp64rk", evf)):
+        ye = evolve_from_y0(e, N200)
+        er = state_errors(ye, y64_200, c0, ev.gf_names)
+        err200[name] = {"state_rel_l2": er["state_rel_l2"],
+                        "max_rel_l2_significant_fields": er["max_rel_l2_significant_fields"],
+                        "max_rel_max_significant_fields": er["max_rel_max_significant_fields"],
+                        "H_l2": ev.l2_norm(ev.hamiltonian(e.y_n)), "H_l2_fp64": H64_200}
+    del evf
+
     # ---- plain FP32 stage buffers, for comparison
     evm = Evolution("BSSN", G, precision="mixed", device=dev)
     tm, _ = run(evm)
@@ -337,6 +364,16 @@ def run_gpu(args):
                    "interior_points": nint, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed (256 MB write) before every timed step",
                    "launch": "each step replays a CUDA graph of its %d kernel launches" % lps},
+        "error_vs_fp64_200_steps": err200,
+        "fp64_accumulation_form": {
+            "what": "FP32 RHS on FP32 (hi, lo) pair stages; RK4 accumulation, y_n, running total and the "
+                    "det(gammabar) rescale in FP64 arithmetic (NRGPU_PREC_COMPENSATED_FP64RK)",
+            "value": world * K * nint * 4 / tf, "unit": UNIT, "ms_per_step": tf / K * 1e3,
+            "launches_per_step": lpsf, "speedup_vs_fp64": t64 / tf,
+            "error_vs_fp64": {"after_steps": K, "state_rel_l2": f_err["state_rel_l2"],
+                              "max_rel_l2_significant_fields": f_err["max_rel_l2_significant_fields"],
+                              "max_rel_max_significant_fields": f_err["max_rel_max_significant_fields"],
+                              "H_l2": Hf}},
         "error_vs_fp64": {"after_steps": K, "state_rel_l2": comp_err["state_rel_l2"],
                           "max_rel_l2_significant_fields": comp_err["max_rel_l2_significant_fields"],
                           "max_rel_max_significant_fields": comp_err["max_rel_max_significant_fields"],
@@ -346,14 +383,15 @@ def run_gpu(args):
         "e2e": {"value": world * K * nint * 4 / te2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
                 "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call"},
-        "roofline": {"bound": "hbm", "kernel": "bssn rhs_kernel, compensated (FP32 pairs in/out, fused RK4 "
-                                               "substep 1)",
+        "roofline": {"bound": "hbm", "kernel": "bssn staged_kernel (RHS variant), compensated (FP32 pairs "
+                                               "in/out, fused RK4 substep 1)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "traffic": RHS_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
                      "bytes_per_point": RHS_BYTES_COMP,
                      "launch_ms": t_rhs_c * 1e3,
-                     "note": "the kernel is load-latency bound (128 registers, 4 blocks of 128 threads per "
-                             "SM, ~1 KB spill frame per thread); HBM fraction reported as asked"},
+                     "note": "the staged kernel (TMA-staged shared-memory finite differences, 236 registers, no "
+                             "spills, 8 warps per SM) is issue/latency bound by the BSSN algebra, not by HBM; "
+                             "HBM fraction reported as asked"},
         "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3},
                        "fp64": {"ricci": t_ric_64 * 1e3, "rhs": t_rhs_64 * 1e3}},
         "fp64": {"value": world * K * nint * 4 / t64, "unit": UNIT, "ms_per_step": t64 / K * 1e3,
@@ -372,6 +410,8 @@ def run_gpu(args):
         "clocks": clocks,
     }
     del evc
+    torch.cuda.empty_cache()
+    out["scalarwave_cartesian_64"] = run_config1(dev)
     torch.cuda.empty_cache()
     if args.config3_steps > 0:
         out["mixed_cartesian_256"] = run_config3(dev, args.config3_steps, flush, N=PROFILE_N3 or 256)
@@ -392,6 +432,66 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_config1(dev, N=64, nsteps=100):
+    """Configuration 1: ScalarWave Cartesian [-10,10]^3, 64^3 + 2 ghosts, FD4,
+    RK4, CFL 0.5, 100 steps, plane wave u = sin(k.x - |k|t), k = (2 pi/20)(1,1,1),
+    quadratic-extrapolation outer BCs, FP64 (and compensated precision beside
+    it); errors against the exact solution on the central half of the z
+    midplane (Tutorial-Start_to_Finish-ScalarWave.ipynb:514-520) at t = 2.5
+    (4th-order regime; the 32^3 run gives the order) and at the final
+    t = 15.625, where the extrapolation boundary's growing mode has reached
+    the centre (in the reference's own run too)."""
+    import torch
+    import oracle.grid as og
+    import oracle.wave_maxwell as ow
+    from nrpytutorial_gb300 import Evolution, Grid
+
+    def central(e, n, g):
+        m = n + 2 * g
+        lo, hi = int(m * 0.25) + 1, int(np.ceil(m * 0.75))
+        return float(np.abs(e[m // 2, lo:hi, lo:hi]).max())
+
+    res = {"workload": "ScalarWave Cartesian %d^3 FD4 RK4 CFL 0.5 plane wave k=(2pi/20)(1,1,1), %d steps"
+                       % (N, nsteps)}
+    for prec in ("fp64", "compensated"):
+        errs = {}
+        for n in (N // 2, N):
+            G = Grid("Cartesian", (n, n, n), FD_order=4, NGHOSTS=2)
+            gp = og.GridParams("Cartesian", (n, n, n), 2, 4)
+            ev = Evolution("ScalarWave", G, precision=prec, device=dev)
+            y0 = torch.tensor(ow.plane_wave(gp, 0.0), device=dev)
+            dt = 0.5 * gp.dxx[0]
+            steps = nsteps * n // N
+            n25 = int(round(2.5 / dt))
+            ev.y_n.copy_(y0)
+            ev.capture(dt, n_steps=n25)()
+            e25 = central(ev.y_n[0].cpu().numpy() - ow.plane_wave(gp, n25 * dt)[0], n, 2)
+            rep = ev.capture(dt, n_steps=1)
+            ev.y_n.copy_(y0)
+            for _ in range(3):
+                rep()
+            ev.y_n.copy_(y0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(steps):
+                rep()
+            b.record()
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b) / 1e3
+            ef = central(ev.y_n[0].cpu().numpy() - ow.plane_wave(gp, steps * dt)[0], n, 2)
+            errs[n] = {"err_t2.5": e25, "err_final": ef, "steps": steps, "seconds": t,
+                       "gp_per_s": n ** 3 * 4 * steps / t, "ms_per_step": t / steps * 1e3}
+            del ev
+        r = dict(errs[N])
+        r["convergence_order_t2.5"] = float(np.log2(errs[N // 2]["err_t2.5"] / errs[N]["err_t2.5"]))
+        r["coarse_%d" % (N // 2)] = errs[N // 2]
+        res[prec] = r
+    res["note"] = ("steps are CUDA-graph replays of one RK4 step (launch-bound at this size); L2 not flushed "
+                   "(the 2.5 MB state stays in L2, as it does in a running evolution)")
+    return res
 
 
 def run_config3(dev, K, flush, N=256):
@@ -538,10 +638,10 @@ def run_config4(dev, K, flush, n=512):
 def convergence_orders(dev):
     """|H| in 2 < r < 5 after t = 0.2 of Brill-Lindquist data (m = 0.5 at
     z = +-0.5) on Spherical grids 48x24x4 and 96x48x4 (RMAX 8, FD4): the
-    convergence order log2(|H|_coarse / |H|_fine), FP64 and compensated."""
+    convergence order log2(|H|_coarse / |H|_fine), FP64 and both mixed forms."""
     from nrpytutorial_gb300 import Evolution, Grid
     T, out = 0.2, {}
-    for prec in ("fp64", "compensated"):
+    for prec in ("fp64", "compensated", "compensated_fp64rk"):
         norms = []
         for Nr, Nth in ((48, 24), (96, 48)):
             G = Grid("Spherical", (Nr, Nth, 4), FD_order=4, NGHOSTS=3, RMAX=8.0, eta=2.0)

@@ -73,6 +73,14 @@ extern "C" {
 #define NRGPU_PREC_MIXED  1       /* FP32 stage buffers + FP32 RHS, FP64 y_n  */
 #define NRGPU_PREC_COMPENSATED 2  /* FP32 RHS on FP32 (hi, lo) pair stage
                                      buffers, FP64 y_n and running total    */
+#define NRGPU_PREC_COMPENSATED_FP64RK 3  /* the same FP32 RHS on pair stages, with
+                                     the RK4 accumulation (y_n, running total)
+                                     and the det(gammabar) rescale in FP64
+                                     arithmetic: the mixed-precision form whose
+                                     only FP32 arithmetic is the RHS. COMPENSATED
+                                     carries the accumulation and rescale in
+                                     float-float (48 bits) on the FP32 pipe
+                                     instead. Single-grid MoL steps only. */
 
 /*
  * paramstruct: the runtime parameters the generated kernels read through

@@ -12,7 +12,7 @@ LIBPATH = os.path.join(HERE, "libnrgpu.so")
 COORD = {"Cartesian": 0, "Spherical": 1, "SinhSpherical": 2, "SinhSphericalv2": 3, "Cylindrical": 4,
          "SinhCylindrical": 5, "SinhCylindricalv2": 6, "SymTP": 7, "SinhSymTP": 8}
 SYSTEM = {"ScalarWave": 0, "Maxwell": 1, "BSSN": 2, "MaxwellCurvilinear": 3}
-PREC = {"fp64": 0, "mixed": 1, "compensated": 2}
+PREC = {"fp64": 0, "mixed": 1, "compensated": 2, "compensated_fp64rk": 3}
 BSSN_KERNELS = {"auto": 0, "point": 1, "staged": 2, "fused": 3}
 MAX_GHOSTS = 8
 MAX_BC_LEVELS = 32

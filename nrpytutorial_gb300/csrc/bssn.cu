@@ -504,13 +504,14 @@ int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
   return bssn_rhs_launch(rfm, p, a);
 }
 
-int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair, bool ff_f64) {
+int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair, bool ff_f64,
+                        bool f64_pair) {
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(gfs != nullptr, "NULL gridfunctions");
   Grid g = make_grid(p);
   dim3 block(64), grid((g.n0 + 63) / 64, g.n1, g.n2);
-  if (!is_f64 || ff_f64) {  // FP32 storage (or the FP32-stage steps' FP64 state): float-float rescale
+  if ((!is_f64 || ff_f64) && !(pair && f64_pair)) {  // FP32 storage (or the FP32-stage steps' FP64 state): float-float rescale
     const dim3 fb(256), fg((unsigned)((g.ntot + 255) / 256));
     if (is_f64) enforce_ff_kernel<double><<<fg, fb, 0, stream()>>>(g, (double *)gfs);
     else if (pair) enforce_ff_kernel<float2><<<fg, fb, 0, stream()>>>(g, (float2 *)gfs);
@@ -529,8 +530,11 @@ int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, 
   else if (symtp_family(p->CoordSystem))                                                                  \
     enforce_kernel<NRGPU_COORD_SINHSYMTP, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);            \
   else enforce_kernel<NRGPU_COORD_SINHSPHERICAL, T><<<grid, block, 0, stream()>>>(g, tab, (T *)gfs);
-  NRGPU_REQUIRE(!pair, "pair gridfunctions are FP32");
-  ENF(double)
+  if (pair) {  // pair stage buffers, FP64 arithmetic (COMPENSATED_FP64RK)
+    ENF(float2)
+  } else {
+    ENF(double)
+  }
 #undef ENF
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;

@@ -297,7 +297,7 @@ int ricci_launch_t(const rfm_struct *rfm, const paramstruct *p, const void *in, 
                    void *aux) {
   Grid g = make_grid(p);
   InteriorLaunch L = interior_launch(g, kBlockX, kBlockY);
-  if (prec == NRGPU_PREC_COMPENSATED) {
+  if (pair_precision(prec)) {
     ricci_kernel<float, Pair32, CS, ORDER, float><<<L.grid, L.block, 0, stream()>>>(
         g, (const float2 *)in, table_of<float>(rfm), (float *)aux);
   } else if (prec == NRGPU_PREC_FP64) {
@@ -324,8 +324,9 @@ int rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a
     rhs_kernel<double, double, CS, ORDER, double, EXTRA><<<L.grid, L.block, 0, stream()>>>(
         g, (const double *)a.in, (const double *)a.auxevol, table_of<double>(rfm), p->eta, p->diss_strength,
         t4uu_of<double>(p, a.auxevol, g.ntot), epi);
-  } else if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
+  } else if (pair_precision(a.prec)) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt),
+                           a.prec == NRGPU_PREC_COMPENSATED_FP64RK};
     rhs_kernel<float, Pair32, CS, ORDER, float2, EXTRA><<<L.grid, L.block, 0, stream()>>>(
         g, stage_input<Pair32>(a), (const float *)a.auxevol, table_of<float>(rfm), eta32, diss32,
         t4uu_of<float>(p, a.auxevol, g.ntot), epi);

@@ -465,7 +465,7 @@ int staged_ricci_launch_t(const rfm_struct *rfm, const paramstruct *p, const voi
     return staged_launch<double, double, CS, ORDER, double, stage::RICCI>(rfm, p, in, nullptr, (double *)aux, 0.0,
                                                                         RKEpilogue<double>{});
   if (in_is_f64) return NRGPU_ERR_UNSUPPORTED;
-  if (prec == NRGPU_PREC_COMPENSATED)
+  if (pair_precision(prec))
     return staged_launch<float, Pair32, CS, ORDER, float2, stage::RICCI>(rfm, p, in, nullptr, (float *)aux, 0.f,
                                                                         RKEpilogue<float2>{});
   return staged_launch<float, float, CS, ORDER, float, stage::RICCI>(rfm, p, in, nullptr, (float *)aux, 0.f,
@@ -485,8 +485,9 @@ int staged_rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const Stage
   }
   if (a.in_is_f64) return NRGPU_ERR_UNSUPPORTED;
   const float eta32 = (float)p->eta;
-  if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
+  if (pair_precision(a.prec)) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt),
+                           a.prec == NRGPU_PREC_COMPENSATED_FP64RK};
     return fused ? staged_launch<float, Pair32, CS, ORDER, float2, stage::FUSED>(rfm, p, a.in, nullptr, nullptr,
                                                                                  eta32, epi)
                  : staged_launch<float, Pair32, CS, ORDER, float2, stage::RHS>(

@@ -46,6 +46,11 @@ int *device_status_word();
     }                                                                            \
   } while (0)
 
+// Stage buffers of FP32 (hi, lo) pairs: both compensated precisions.
+__host__ __device__ inline bool pair_precision(int prec) {
+  return prec == NRGPU_PREC_COMPENSATED || prec == NRGPU_PREC_COMPENSATED_FP64RK;
+}
+
 // Validates the parts of a paramstruct every kernel depends on.
 int check_params(const paramstruct *p);
 

@@ -80,6 +80,9 @@ template <typename TStage> struct RKEpilogue {
   TStage *out;        // stage buffer (or rhs buffer for stage -1); float2:
                       // FP32 (hi, lo) pairs of the FP64 stage value
   StageConsts kc;     // FP32 stage buffers: dt*c pairs (stage_consts(dt))
+  bool f64_update;    // FP32 stage buffers: RK update in FP64 arithmetic on the
+                      // FP64 y_n and running total (NRGPU_PREC_COMPENSATED_FP64RK)
+                      // instead of float-float on their pair form
 
   // Stage value (computed in FP64) into the stage buffer.
   __device__ __forceinline__ void put(long long i, double v) const {
@@ -101,9 +104,11 @@ template <typename TStage> struct RKEpilogue {
       return;
     }
     if constexpr (!std::is_same<TStage, double>::value) {
-      const float2 v = ff_rk4_update(stage, (float)value, kc, y_n, rt, i);
-      if (stage < 3) put_pair(i, v);
-      return;
+      if (!f64_update) {
+        const float2 v = ff_rk4_update(stage, (float)value, kc, y_n, rt, i);
+        if (stage < 3) put_pair(i, v);
+        return;
+      }
     }
     const double kdt = dmul((double)value, dt);
     switch (stage) {

@@ -88,8 +88,9 @@ int maxwell_launch(const paramstruct *p, const StageArgs &a) {
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
     return dispatch<double, double, double>(p, g, stage_input<double>(a), epi);
   }
-  if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
+  if (pair_precision(a.prec)) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt),
+                           a.prec == NRGPU_PREC_COMPENSATED_FP64RK};
     return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), epi);
   }
   RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};

@@ -238,8 +238,9 @@ int maxwell_curvi_launch(const rfm_struct *rfm, const paramstruct *p, const Stag
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
     return dispatch<double, double, double>(p, g, stage_input<double>(a), rfm, epi);
   }
-  if (a.prec == NRGPU_PREC_COMPENSATED) {
-    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt)};
+  if (pair_precision(a.prec)) {
+    RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt),
+                           a.prec == NRGPU_PREC_COMPENSATED_FP64RK};
     return dispatch<float, Pair32, float2>(p, g, stage_input<Pair32>(a), rfm, epi);
   }
   RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};

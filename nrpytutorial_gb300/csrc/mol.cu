@@ -65,12 +65,14 @@ template <typename TStage> __device__ __forceinline__ TStage from_double(double 
   else return (TStage)v;
 }
 
+// f64_update: FP32 stage buffers with the update in FP64 arithmetic on the
+// FP64 y_n and running total (NRGPU_PREC_COMPENSATED_FP64RK).
 template <typename TStage>
 __global__ void rk4_update_kernel(int stage, double dt, StageConsts kc, long long n, double *__restrict__ y_n,
-                                  double *__restrict__ rt, TStage *__restrict__ k) {
+                                  double *__restrict__ rt, TStage *__restrict__ k, bool f64_update = false) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    if constexpr (!std::is_same<TStage, double>::value) {
+    if (!std::is_same<TStage, double>::value && !f64_update) {
       // FP32 stages: the fused epilogue's float-float update (y_n, rt hold pairs)
       float kv;
       if constexpr (std::is_same<TStage, float2>::value) kv = k[i].x;  // rhs_eval stored (k, 0)
@@ -141,15 +143,17 @@ static int rhs_stage(int system, const rfm_struct *rfm, const paramstruct *p, co
 // Boundary conditions, then (BSSN) the det(gammabar) rescale, on `gfs`
 // (double, float, or float2 pairs when `pair`).
 // reduced: an FP32-stage step (its FP64 y_n is rescaled in float-float arithmetic)
+// f64_rescale: pair stage buffers rescaled in FP64 arithmetic (COMPENSATED_FP64RK)
 static int post_rhs(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc, void *gfs,
-                    bool is_f64, bool pair = false, bool reduced = false) {
+                    bool is_f64, bool pair = false, bool reduced = false, bool f64_rescale = false) {
   const int ngf = system_num_gfs(system);
   int st;
   if (pair) st = apply_bcs_pair_impl(p, bc, ngf, system_parity(system), (float2 *)gfs);
   else if (is_f64) st = apply_bcs_impl<double>(p, bc, ngf, system_parity(system), (double *)gfs);
   else st = apply_bcs_impl<float>(p, bc, ngf, system_parity(system), (float *)gfs);
   if (st) return st;
-  if (system == NRGPU_SYS_BSSN) return bssn_enforce_launch(rfm, p, gfs, is_f64, pair, reduced && is_f64);
+  if (system == NRGPU_SYS_BSSN)
+    return bssn_enforce_launch(rfm, p, gfs, is_f64, pair, reduced && is_f64, f64_rescale && pair);
   return NRGPU_OK;
 }
 
@@ -158,11 +162,21 @@ static long long state_len(int system, const paramstruct *p) {
          p->Nxx_plus_2NGHOSTS2;
 }
 
+// Start of an NRGPU_PREC_COMPENSATED_FP64RK step: the FP64 y_n stays as it is
+// and its (hi, lo) pairs go to `out`, substep 0's stencil input.
+__global__ void pair_copy_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = split_pair(y[i]);
+}
+
 static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
   const long long n = state_len(system, p);
   const int threads = 256;
   const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 8);
-  if (gfs->precision == NRGPU_PREC_COMPENSATED)
+  if (gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK)
+    pair_copy_kernel<<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
+  else if (gfs->precision == NRGPU_PREC_COMPENSATED)
     split_state_kernel<false><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, nullptr);
   else
     split_state_kernel<true><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float *)gfs->k_even_gfs);
@@ -177,7 +191,7 @@ static int check_step_args(int system, const rfm_struct *rfm, const paramstruct 
   NRGPU_REQUIRE(system_num_gfs(system) > 0, "unknown system %d", system);
   NRGPU_REQUIRE(bc != nullptr && gfs != nullptr, "NULL bcstruct or gridfunctions");
   NRGPU_REQUIRE(gfs->precision == NRGPU_PREC_FP64 || gfs->precision == NRGPU_PREC_MIXED ||
-                    gfs->precision == NRGPU_PREC_COMPENSATED,
+                    pair_precision(gfs->precision),
                 "unknown precision %d", gfs->precision);
   NRGPU_REQUIRE(gfs->y_n_gfs && gfs->y_nplus1_running_total_gfs && gfs->k_odd_gfs && gfs->k_even_gfs,
                 "MoL gridfunction buffer is NULL");
@@ -198,7 +212,8 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
   int st = check_step_args(system, rfm, p, bc, gfs);
   if (st) return st;
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
-  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
+  const bool pair = pair_precision(gfs->precision);
+  const bool acc64 = gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   if (!f64 && (st = prep_state(system, p, gfs))) return st;
   for (int s = 0; s < 4; s++) {
@@ -207,8 +222,8 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
     a.dt = dt;
     a.prec = gfs->precision;
     // substep 0 reads y_n: itself in FP64, its pairs in place when compensated,
-    // its FP32 copy in k_even for plain FP32 stages
-    a.in = (s == 0) ? (f64 || pair ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
+    // its pair copy (COMPENSATED_FP64RK) or FP32 copy (plain FP32 stages) in k_even
+    a.in = (s == 0) ? (f64 || (pair && !acc64) ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
                     : (const void *)kbuf[(s + 1) % 2];
     a.in_is_f64 = f64;
     a.y_n = gfs->y_n_gfs;
@@ -218,7 +233,7 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
     if ((st = rhs_stage(system, rfm, p, a))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64))) return st;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64 && !acc64, acc64))) return st;
   }
   return NRGPU_OK;
 }
@@ -232,7 +247,7 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   NRGPU_REQUIRE(which >= 0 && which <= 2, "which %d not in 0..2", which);
   NRGPU_REQUIRE(which == 0 || system == NRGPU_SYS_BSSN, "which = 1, 2 select BSSN's two kernels");
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
-  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
+  const bool pair = pair_precision(gfs->precision);
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   StageArgs a{};
   a.stage = stage;
@@ -291,7 +306,8 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
   int st = check_step_args(system, rfm, p, bc, gfs);
   if (st) return st;
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
-  const bool pair = gfs->precision == NRGPU_PREC_COMPENSATED;
+  const bool pair = pair_precision(gfs->precision);
+  const bool acc64 = gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK;
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   const long long n = state_len(system, p);
   const int threads = 256;
@@ -303,7 +319,7 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
     a.stage = -1;
     a.dt = dt;
     a.prec = gfs->precision;
-    a.in = (s == 0) ? (f64 || pair ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
+    a.in = (s == 0) ? (f64 || (pair && !acc64) ? (const void *)gfs->y_n_gfs : (const void *)gfs->k_even_gfs)
                     : (const void *)kbuf[(s + 1) % 2];
     a.in_is_f64 = f64;
     a.out = kbuf[s % 2];  // RHS_output: k_odd, k_even, k_odd, k_even
@@ -312,7 +328,7 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
     if (pair)
       rk4_update_kernel<float2><<<blocks, threads, 0, stream()>>>(s, dt, kc, n, gfs->y_n_gfs,
                                                                   gfs->y_nplus1_running_total_gfs,
-                                                                  (float2 *)kbuf[s % 2]);
+                                                                  (float2 *)kbuf[s % 2], acc64);
     else if (!f64)
       rk4_update_kernel<float><<<blocks, threads, 0, stream()>>>(s, dt, kc, n, gfs->y_n_gfs,
                                                                  gfs->y_nplus1_running_total_gfs,
@@ -324,7 +340,7 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
     NRGPU_LAUNCH_CHECK();
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
-    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64))) return st;
+    if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64 && !acc64, acc64))) return st;
   }
   return NRGPU_OK;
 }

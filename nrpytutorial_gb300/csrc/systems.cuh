@@ -38,8 +38,9 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs &a);
 // is_f64: double array; otherwise float, or float2 pairs when pair is set
 // ff_f64: FP64 data rescaled in float-float arithmetic (the FP32-stage steps' state)
+// f64_pair: pair data rescaled in FP64 arithmetic (COMPENSATED_FP64RK stages)
 int bssn_enforce_launch(const rfm_struct *rfm, const paramstruct *p, void *gfs, bool is_f64, bool pair = false,
-                        bool ff_f64 = false);
+                        bool ff_f64 = false, bool f64_pair = false);
 
 // Evolved-gridfunction counts and parity types (alphabetical gf order;
 // parity types from CurviBoundaryConditions.py:122-213).

@@ -42,7 +42,8 @@ class Evolution:
         self.y_n = torch.zeros(shape, dtype=torch.float64, **z)
         self.rt = torch.zeros(shape, dtype=torch.float64, **z)
         # compensated: stage buffers hold FP32 (hi, lo) pairs of the FP64 stage values
-        kshape = shape + (2,) if precision == "compensated" else shape
+        # (both compensated modes; compensated_fp64rk keeps the RK accumulation in FP64)
+        kshape = shape + (2,) if precision.startswith("compensated") else shape
         self.k_odd = torch.zeros(kshape, dtype=stage, **z)
         self.k_even = torch.zeros(kshape, dtype=stage, **z)
         naux = len(AUXEVOL_GFS.get(system, []))

@@ -1,7 +1,7 @@
 """Generate the reference's own C kernels into oracle/_ref/src/ (gitignored).
 
 TEST INFRASTRUCTURE (see oracle/__init__.py).  Needs the reference checkout
-(default /root/reference, or $NRPY_REFERENCE); run it in the container that
+($NRPY_REFERENCE, required); run it in the container that
 has it:
 
     python -m oracle.gen_ref            # all configurations, in parallel
@@ -34,7 +34,7 @@ import textwrap
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("NRPY_REFERENCE", "/root/reference")
+REF = os.environ.get("NRPY_REFERENCE", "")
 OUT = os.path.join(HERE, "_ref", "src")
 
 # name -> (system, CoordSystem, FD order, NGHOSTS)
@@ -338,8 +338,8 @@ def generate(name):
 
 
 def main(names):
-    if not os.path.isdir(REF):
-        raise SystemExit("reference checkout not found at %s" % REF)
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("set NRPY_REFERENCE to the reference checkout (now %r)" % REF)
     names = names or list(CONFIGS)
     with ThreadPoolExecutor(max_workers=min(8, len(names))) as ex:
         for name, funcs in ex.map(generate, names):

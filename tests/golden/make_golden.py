@@ -1,8 +1,7 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference.
 
-Run in a container that has the reference checkout (default /root/reference,
-or $NRPY_REFERENCE) after `python -m oracle.gen_ref` and
-`python -m oracle.ref_build`:
+Run in a container that has the reference checkout ($NRPY_REFERENCE,
+required) after `python -m oracle.gen_ref` and `python -m oracle.ref_build`:
 
     python tests/golden/make_golden.py
     python tests/golden/make_golden.py ref:bssn_cart_fd8     # one fixture
@@ -29,6 +28,11 @@ Writes:
       validation run (SinhSpherical 16x8x16 and 24x12x24, plane wave, CFL 1,
       to t = 7) through the reference's generated rhs_eval: the 16x8x16
       state and both runs' error norms at t_final (`evolve_sw`).
+  ref_sw_config1.npz  configuration 1 (ScalarWave Cartesian 64^3 and 32^3,
+      FD4, CFL 0.5, plane wave, 100 and 50 steps) through the reference's
+      generated rhs_eval: central-midplane errors against the exact solution
+      at t = 2.5, 5, 15.625 and 4096 sampled points of the final 64^3 state
+      (`config1`).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -51,7 +55,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("NRPY_REFERENCE", "/root/reference")
+REF = os.environ.get("NRPY_REFERENCE", "")
 
 KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-2.0, 2.0), eta=2.0)
 BL = dict(BH1_mass=0.5, BH1_posn_x=0.0, BH1_posn_y=0.0, BH1_posn_z=0.5,
@@ -243,6 +247,59 @@ def evolution_scalarwave():
             out["state_" + tag] = y[:, g:-g, g:-g, g:-g]
         print("evolved", tag, n_final, "steps, dt", dt, "L2 error", out["l2_error_" + tag])
     np.savez_compressed(os.path.join(HERE, "ref_sw_planewave_sinhsph.npz"), **out)
+
+
+# Configuration 1: ScalarWave Cartesian [-10,10]^3, FD4, 2 ghosts, CFL 0.5,
+# u = sin(k.x - |k| t), v = -|k| cos(k.x - |k| t), k = (2 pi/20)(1,1,1),
+# quadratic-extrapolation outer BCs; 64^3 for 100 RK4 steps and 32^3 for 50
+# (the same final time 15.625).  Errors against the exact solution are taken
+# the way Tutorial-Start_to_Finish-ScalarWave.ipynb:514-520 takes them: on the
+# central half of the z midplane.
+C1 = dict(grids=((32, 32, 32), (64, 64, 64)), steps=(50, 100), times=(2.5, 5.0, 15.625), nsample=4096)
+
+
+def c1_central(e, N, g):
+    """|e| on the central half of the z midplane (the notebook's region)."""
+    n = N + 2 * g
+    lo, hi = int(n * 0.25) + 1, int(np.ceil(n * 0.75))
+    return e[n // 2, lo:hi, lo:hi]
+
+
+def config1():
+    """ref_sw_config1.npz: the reference's generated ScalarWave rhs_eval
+    (strict build of sw_cart_fd4) through the oracle's RK4 step and face
+    extrapolation: for both grids the central-midplane max error against the
+    exact solution at the C1 times, and for 64^3 the final state at 4096
+    seeded interior sample points."""
+    import oracle.bcs as ob
+    import oracle.grid as og
+    import oracle.wave_maxwell as ow
+    from oracle.ref import RefKernels
+    out = {}
+    for N, nsteps in zip(C1["grids"], C1["steps"]):
+        gp = og.GridParams("Cartesian", N, 2, 4)
+        R = RefKernels("sw_cart_fd4", gp, "strict", extra=dict(wavespeed=1.0))
+        layers = ob.build_bcstruct(gp)
+        y = ow.plane_wave(gp, 0.0)
+        dt = 0.5 * gp.dxx[0]
+        tag = "%d" % N[0]
+        k_odd = k_even = None
+        for s in range(1, nsteps + 1):
+            y, k_odd, k_even = ob.rk4_step(y, dt, R.rhs_eval, lambda f: ob.apply_bcs(layers, f, [0, 0]),
+                                           gp.NGHOSTS, k_odd, k_even)
+            for t in C1["times"]:
+                if abs(s * dt - t) < 1e-9:
+                    ex = ow.plane_wave(gp, s * dt)
+                    out["err_%s_t%g" % (tag, t)] = float(c1_central(np.abs(y[0] - ex[0]), N[0], 2).max())
+        out["dt_" + tag] = dt
+        if N[0] == 64:
+            rng = np.random.default_rng(C1["nsample"])
+            g = gp.NGHOSTS
+            idx = np.stack([rng.integers(g, g + N[d], C1["nsample"]) for d in (2, 1, 0)], axis=1)
+            out["sample_idx"] = idx
+            out["sample_state"] = y[:, idx[:, 0], idx[:, 1], idx[:, 2]]
+        print("config 1", tag, {k: v for k, v in out.items() if k.startswith("err_" + tag)})
+    np.savez_compressed(os.path.join(HERE, "ref_sw_config1.npz"), **out)
 
 
 FD_WORKER = r'''
@@ -450,6 +507,8 @@ def trusted(only=None):
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("set NRPY_REFERENCE to the reference checkout")
     what = sys.argv[1:] or ["senr", "ref", "fd", "swsh", "trusted", "evolve", "evolve_sw"]
     if "senr" in what:
         senr_bc()
@@ -465,6 +524,8 @@ if __name__ == "__main__":
         evolution()
     if "evolve_sw" in what:
         evolution_scalarwave()
+    if "config1" in what:
+        config1()
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)

@@ -1,7 +1,10 @@
 """Compensated mixed precision (NRGPU_PREC_COMPENSATED): FP32 RHS arithmetic
 on split FP32 stage inputs (hi + remainder), FP64 y_n and running total.
 Against the FP64 step it must be far closer than the plain FP32-stage mode,
-fused and unfused steps must agree, and graph replay must match eager steps."""
+fused and unfused steps must agree, and graph replay must match eager steps.
+The same for NRGPU_PREC_COMPENSATED_FP64RK, whose RK accumulation and
+det(gammabar) rescale are FP64 arithmetic: its error against FP64 is that of
+the FP32 RHS alone."""
 import numpy as np
 import pytest
 
@@ -71,24 +74,46 @@ def test_compensated_much_closer_to_fp64_than_plain_fp32(cuda, system, coord, Nx
     assert e_comp < e_plain / 3, (e_comp, e_plain)
 
 
-@pytest.mark.parametrize("system,coord,Nxx,order", [CASES[0], CASES[2], CASES[4]])
-def test_compensated_fused_equals_unfused(cuda, system, coord, Nxx, order):
+@pytest.mark.parametrize("system,coord,Nxx,order", CASES)
+def test_fp64_accumulation_form_close_to_fp64(cuda, system, coord, Nxx, order):
+    """FP32 RHS with FP64 RK accumulation and FP64 rescale: the error against
+    the FP64 step is the FP32 RHS's, at the float-float form's level."""
+    from nrpytutorial_gb300 import default_nghosts
     G, gp = grids(system, coord, Nxx, order, **KW)
     y = _state(system, gp)
     dt = G.find_timestep(0.5)
-    a = _run(cuda, system, coord, Nxx, order, "compensated", y, dt, 3, fused=True)
-    b = _run(cuda, system, coord, Nxx, order, "compensated", y, dt, 3, fused=False)
+    n = 8
+    ref = _run(cuda, system, coord, Nxx, order, "fp64", y, dt, n)
+    comp = _run(cuda, system, coord, Nxx, order, "compensated", y, dt, n)
+    acc = _run(cuda, system, coord, Nxx, order, "compensated_fp64rk", y, dt, n)
+    g = default_nghosts(system, order)
+    sl = (slice(None), slice(g, -g), slice(g, -g), slice(g, -g))
+    e_comp, e_acc = rel_l2(comp[sl], ref[sl]), rel_l2(acc[sl], ref[sl])
+    print("%s %s: state rel_l2 compensated %.3e fp64-accumulation %.3e" % (system, coord, e_comp, e_acc))
+    assert e_acc < 1e-6, e_acc
+    assert e_acc < 2 * e_comp + 1e-14, (e_acc, e_comp)
+
+
+@pytest.mark.parametrize("prec", ["compensated", "compensated_fp64rk"])
+@pytest.mark.parametrize("system,coord,Nxx,order", [CASES[0], CASES[2], CASES[4]])
+def test_compensated_fused_equals_unfused(cuda, system, coord, Nxx, order, prec):
+    G, gp = grids(system, coord, Nxx, order, **KW)
+    y = _state(system, gp)
+    dt = G.find_timestep(0.5)
+    a = _run(cuda, system, coord, Nxx, order, prec, y, dt, 3, fused=True)
+    b = _run(cuda, system, coord, Nxx, order, prec, y, dt, 3, fused=False)
     assert rel_l2(a, b) < 1e-13
 
 
-def test_compensated_graph_replay_matches_eager(cuda):
+@pytest.mark.parametrize("prec", ["compensated", "compensated_fp64rk"])
+def test_compensated_graph_replay_matches_eager(cuda, prec):
     import torch
     system, coord, Nxx, order = CASES[4]
     G, gp = grids(system, coord, Nxx, order, **KW)
     y = _state(system, gp)
     dt = G.find_timestep(0.5)
-    eager = _run(cuda, system, coord, Nxx, order, "compensated", y, dt, 3)
-    ev, _ = _evo(cuda, system, coord, Nxx, order, "compensated")
+    eager = _run(cuda, system, coord, Nxx, order, prec, y, dt, 3)
+    ev, _ = _evo(cuda, system, coord, Nxx, order, prec)
     ev.y_n.copy_(torch.tensor(y, device=cuda))
     ev.apply_bcs(ev.y_n)
     ev.enforce_detgammabar(ev.y_n)

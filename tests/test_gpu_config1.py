@@ -1,0 +1,79 @@
+"""Configuration 1 as specified: ScalarWave Cartesian [-10,10]^3, 64^3
+interior + 2 ghost zones, FD4, RK4, CFL 0.5, 100 steps, plane wave
+u = sin(k.x - |k| t), v = -|k| cos(k.x - |k| t), k = (2 pi/20)(1,1,1),
+quadratic-extrapolation outer BCs, exact solution as the oracle.
+
+* FP64 on the GPU (CUDA graphs of the steps) against the same run through
+  the reference's generated rhs_eval and the oracle's RK4 step and BCs
+  (tests/golden/ref_sw_config1.npz): the final state at 4096 sampled points
+  to 1e-12 normwise, and the central-midplane errors against the exact
+  solution at t = 2.5, 5 and 15.625 (the notebook's measure,
+  Tutorial-Start_to_Finish-ScalarWave.ipynb:514-520).
+* 32^3 for 50 steps: the error at t = 2.5 falls at 4th order (the notebook's
+  convergence check, :738-757).  By t = 5 and beyond, the growing mode of
+  the quadratic-extrapolation outer boundary reaches the centre in the
+  reference's own run as well (error O(1) at t = 15.625 on both grids; the
+  notebook itself stops at t = 0.8 domain_size, :554).
+* compensated precision (FP32 RHS on FP32 pair stages) stays within 1e-6 of
+  the FP64 run after the 100 steps."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle.grid as og
+import oracle.wave_maxwell as ow
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _central(e, N, g):
+    n = N + 2 * g
+    lo, hi = int(n * 0.25) + 1, int(np.ceil(n * 0.75))
+    return e[n // 2, lo:hi, lo:hi]
+
+
+def _run(cuda, N, nsteps, prec, times):
+    import torch
+    from nrpytutorial_gb300 import Evolution, Grid
+    G = Grid("Cartesian", (N, N, N), FD_order=4, NGHOSTS=2)
+    gp = og.GridParams("Cartesian", (N, N, N), 2, 4)
+    ev = Evolution("ScalarWave", G, precision=prec, device=cuda)
+    ev.y_n.copy_(torch.tensor(ow.plane_wave(gp, 0.0), device=cuda))
+    dt = 0.5 * gp.dxx[0]
+    errs, done = {}, 0
+    for t in sorted(times) + [nsteps * dt]:
+        n = int(round(t / dt)) - done
+        if n > 0:
+            ev.capture(dt, n_steps=n)()
+            done += n
+        ex = ow.plane_wave(gp, done * dt)
+        errs[round(done * dt, 6)] = float(_central(np.abs(ev.y_n[0].cpu().numpy() - ex[0]), N, 2).max())
+    return ev.y_n.cpu().numpy(), errs
+
+
+def test_config1_fp64_matches_reference_run_and_converges(cuda):
+    z = np.load(os.path.join(GOLD, "ref_sw_config1.npz"))
+    y64, e64 = _run(cuda, 64, 100, "fp64", (2.5, 5.0))
+    idx = z["sample_idx"]
+    got = y64[:, idx[:, 0], idx[:, 1], idx[:, 2]]
+    for g in range(2):
+        assert rel_l2(got[g], z["sample_state"][g]) < 1e-12
+    for t in (2.5, 5.0, 15.625):
+        assert e64[t] == pytest.approx(float(z["err_64_t%g" % t]), rel=1e-6)
+    _, e32 = _run(cuda, 32, 50, "fp64", (2.5, 5.0))
+    for t in (2.5, 5.0, 15.625):
+        assert e32[t] == pytest.approx(float(z["err_32_t%g" % t]), rel=1e-6)
+    order = np.log2(e32[2.5] / e64[2.5])
+    assert 3.8 < order < 4.2, order
+
+
+def test_config1_compensated_close_to_fp64(cuda):
+    y64, _ = _run(cuda, 64, 100, "fp64", ())
+    yc, _ = _run(cuda, 64, 100, "compensated", ())
+    g = 2
+    for k in range(2):
+        assert rel_l2(yc[k][g:-g, g:-g, g:-g], y64[k][g:-g, g:-g, g:-g]) < 1e-6
