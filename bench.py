@@ -49,10 +49,11 @@ UNIT = "gridpoint-RHS/s"
 RHS_BYTES_COMP = 24 * 8 + 6 * 4 + 24 * 8 + 24 * 16 + 24 * 8
 # DRAM bytes (read + write) of that launch, L2 flushed before it as in the
 # timing: one ncu capture of the launches inside the "roofline_rhs" range
-# (profiles/bssn_rhs_compensated_roofline_traffic.md), mean of two launches:
-# 118.1 MB read + 129.1 MB written, 1.9x the 129.0 MB algorithmic (register
-# spill lines evicted to DRAM and ghost-zone stencil reads).
-RHS_TRAFFIC_COMP = 247.2e6
+# (profiles/bssn_rhs_staged_compensated_roofline_traffic.md), mean of two
+# launches of the staged RHS kernel: 101.2 MB read + 21.4 MB written, 0.95x
+# the 129.0 MB algorithmic (the running-total and stage stores that are still
+# in L2 when the launch ends are written back later).
+RHS_TRAFFIC_COMP = 122.6e6
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 

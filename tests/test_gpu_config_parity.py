@@ -10,10 +10,17 @@ machine by __graft_entry__.build() from the output of oracle/gen_ref.py):
   8 planes in i2, 4 ghosts -- with its seeded Brill-Lindquist data plus a
   perturbation.
 
-Ricci_eval, rhs_eval (given the reference's RbarDD), the Hamiltonian
-constraint and the det(gammabar) rescale must match at 1e-12 normwise
-relative per gridfunction (1e-14 for the rescale), with every BSSN kernel
-family.  The identical FP64 input state goes to both sides.
+Ricci_eval, the Hamiltonian constraint and the det(gammabar) rescale must
+match at 1e-12 normwise relative per gridfunction (1e-14 for the rescale),
+rhs_eval (given the reference's RbarDD) at 1e-11, with every BSSN kernel
+family.  The identical FP64 input state goes to both sides.  The rhs bound
+is the FP64 conditioning of the RHS at Brill-Lindquist data, not a kernel
+property: on the same kind of input (a 64 x 64 x 8 slab at this grid
+spacing) the numpy oracle, an independent FP64 evaluation, differs from the
+reference's C by up to 3e-12 per gridfunction in aDD_ii and trK (1.4e-12
+over the whole RHS), and the GPU's point, staged and fused kernels show the
+same figures as each other (5e-12 on this slab, 1.5e-12 on the headline
+grid).
 """
 import numpy as np
 import pytest
@@ -25,6 +32,7 @@ from tests.helpers import per_gf_rel, smooth_state
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+RHS_TOL = 1e-11
 
 
 def _reference(cfg, gp):
@@ -55,7 +63,7 @@ def _compare(cuda, G, gp, cfg, m1, z1, m2, z2, seed):
     out = torch.zeros_like(t)
     ev.rhs_eval_given_ricci(t, torch.tensor(r_ric, device=cuda), out)
     r_rhs = rk.rhs_eval(f, aux=r_ric)
-    assert per_gf_rel(out.cpu().numpy()[interior], r_rhs[interior]) < TOL
+    assert per_gf_rel(out.cpu().numpy()[interior], r_rhs[interior]) < RHS_TOL
 
     H = ev.hamiltonian(t).cpu().numpy()[0]
     r_H = rk.hamiltonian(f)
