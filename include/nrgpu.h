@@ -82,12 +82,21 @@ extern "C" {
                                      float-float (48 bits) on the FP32 pipe
                                      instead. Single-grid MoL steps only. */
 
+/* The name of the library's parameter struct.  A generated driver whose own
+ * declare_Cparameters_struct.h already defines `paramstruct` defines
+ * NRGPU_PARAMSTRUCT (e.g. nrgpu_paramstruct) before including this header;
+ * nrpytutorial_gb300/params_shim.py then writes the conversion between the
+ * two (nrgpu_params_from_generated). */
+#ifndef NRGPU_PARAMSTRUCT
+#define NRGPU_PARAMSTRUCT paramstruct
+#endif
+
 /*
  * paramstruct: the runtime parameters the generated kernels read through
  * set_Cparameters.h (NRPy_param_funcs.py:216-304 emits the reference's struct).
  * Field names follow the reference's C parameter names.
  */
-typedef struct paramstruct {
+typedef struct nrgpu_paramstruct_s {
   int    CoordSystem;                 /* NRGPU_COORD_*                          */
   int    FD_order;                    /* 2, 4, 6 or 8 (FD_CENTDERIVS_ORDER)     */
   int    NGHOSTS;                     /* ghost zones per side                   */
@@ -117,7 +126,7 @@ typedef struct paramstruct {
   double AMPLRHO, SINHWRHO, AMPLZ, SINHWZ;  /* SinhCylindrical (:249-251)          */
   double const_drho, const_dz;        /* SinhCylindricalv2 (reference_metric.py:271) */
   double bScale, SINHWAA, AMAX;       /* SymTP, SinhSymTP (reference_metric.py:308-310) */
-} paramstruct;
+} NRGPU_PARAMSTRUCT;
 
 /*
  * rfm_struct: FP64 reference-metric precompute tables (the rfm_precompute
@@ -240,19 +249,20 @@ int         nrgpu_fd_coeffs(int order, int kind, double *out);
  * sets Nxx*, Nxx_plus_2NGHOSTS*, dxx*, invdx*, xxmin/xxmax from CoordSystem,
  * NGHOSTS and the coordinate parameters already in *params, and fills the
  * caller-allocated host arrays xx[d][Nxx_plus_2NGHOSTS_d] with cell-centred
- * coordinates.  EigenCoord=1 uses the eigen-coordinate domain (Spherical for
- * the Spherical family), as the reference does before building BC maps. */
+ * coordinates (xx, or any xx[d], may be NULL: nothing is written there).
+ * EigenCoord=1 uses the eigen-coordinate domain (Spherical for the Spherical
+ * family), as the reference does before building BC maps. */
 int    set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3],
-                                         paramstruct *params, double *xx[3]);
+                                         NRGPU_PARAMSTRUCT *params, double *xx[3]);
 /* reference_metric.py:1412-1439 (find_timestep): CFL * min over interior
  * points of the proper spacing dxx_i * scalefactor_i, / wavespeed.  Host. */
-double find_timestep(const paramstruct *params, double CFL_FACTOR);
+double find_timestep(const NRGPU_PARAMSTRUCT *params, double CFL_FACTOR);
 
 /* ----------------------------------------------- reference metric tables */
 /* rfm_struct__malloc.h / rfm_struct__define.h / rfm_struct__freemem.h
  * (reference_metric.py:871-886).  define() runs an FP64 kernel. */
-int rfm_struct__malloc(const paramstruct *params, rfm_struct *rfm);
-int rfm_struct__define(const paramstruct *params, rfm_struct *rfm);
+int rfm_struct__malloc(const NRGPU_PARAMSTRUCT *params, rfm_struct *rfm);
+int rfm_struct__define(const NRGPU_PARAMSTRUCT *params, rfm_struct *rfm);
 int rfm_struct__freemem(rfm_struct *rfm);
 /* Copy the FP64 table back to the host (testing): host buffer of
  * nquant*N0*N1 doubles. */
@@ -261,7 +271,7 @@ int rfm_struct__download(const rfm_struct *rfm, double *host);
 /* ---------------------------------------------------------- boundaries */
 /* boundary_conditions/driver_bcstruct.h:8-44 (set_up__bc_gz_map_and_parity_condns
  * + set_bcstruct), built on the host on the eigen-coordinate grid, uploaded. */
-int driver_bcstruct(const paramstruct *params, bc_struct *bcstruct);
+int driver_bcstruct(const NRGPU_PARAMSTRUCT *params, bc_struct *bcstruct);
 int bcstruct_freemem(bc_struct *bcstruct);
 /* Host copy of the flattened map (testing).  Buffers sized total_outer /
  * total_inner as reported in *bcstruct. */
@@ -270,9 +280,9 @@ int bcstruct_download(const bc_struct *bcstruct, int *outer_dest, int *outer_ste
 /* apply_bcs_curvilinear.h:56-64: per ghost layer, quadratic extrapolation at
  * outer points then parity copy at inner points.  gfs_parity is a HOST array
  * of NUM_GFS parity types (0..9). */
-int apply_bcs_curvilinear(const paramstruct *params, const bc_struct *bcstruct,
+int apply_bcs_curvilinear(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
                           int NUM_GFS, const int8_t *gfs_parity, double *gfs);
-int apply_bcs_curvilinear_f32(const paramstruct *params, const bc_struct *bcstruct,
+int apply_bcs_curvilinear_f32(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
                               int NUM_GFS, const int8_t *gfs_parity, float *gfs);
 
 /* Sommerfeld radiation boundary condition (CurviBoundaryConditions.py:259-658,
@@ -287,26 +297,26 @@ int apply_bcs_curvilinear_f32(const paramstruct *params, const bc_struct *bcstru
  * nrgpu_sommerfeld_params (NULL arrays leave values unchanged). */
 int nrgpu_sommerfeld_params(int fd_order, int NUM_GFS, const double *speed, const double *f_inf,
                             const double *radial_falloff_power);
-int apply_bcs_sommerfeld(const paramstruct *params, double *xx[3], const bc_struct *bcstruct, int NUM_GFS,
+int apply_bcs_sommerfeld(const NRGPU_PARAMSTRUCT *params, double *xx[3], const bc_struct *bcstruct, int NUM_GFS,
                          const int8_t *gfs_parity, const double *gfs, double *rhs_gfs);
 
 /* -------------------------------------------------------- RHS kernels */
 /* ScalarWave Cartesian: rhs_eval(params, in_gfs, rhs_gfs)
  * (Tutorial-Start_to_Finish-ScalarWave.ipynb, rhs_eval; ScalarWave_RHSs.py:46-71) */
-int ScalarWave_rhs_eval(const paramstruct *params, const double *in_gfs, double *rhs_gfs);
-int ScalarWave_rhs_eval_f32(const paramstruct *params, const float *in_gfs, float *rhs_gfs);
+int ScalarWave_rhs_eval(const NRGPU_PARAMSTRUCT *params, const double *in_gfs, double *rhs_gfs);
+int ScalarWave_rhs_eval_f32(const NRGPU_PARAMSTRUCT *params, const float *in_gfs, float *rhs_gfs);
 /* ScalarWave curvilinear: rhs_eval(rfmstruct, params, in_gfs, rhs_gfs)
  * (ScalarWaveCurvilinear_RHSs.py:43-98) */
-int ScalarWaveCurvilinear_rhs_eval(const rfm_struct *rfm, const paramstruct *params,
+int ScalarWaveCurvilinear_rhs_eval(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                    const double *in_gfs, double *rhs_gfs);
-int ScalarWaveCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+int ScalarWaveCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                        const float *in_gfs, float *rhs_gfs);
 /* Vacuum Maxwell System I, Cartesian (VacuumMaxwell_Flat_Evol_Cartesian.py:54-74) */
-int Maxwell_rhs_eval(const paramstruct *params, const double *in_gfs, double *rhs_gfs);
-int Maxwell_rhs_eval_f32(const paramstruct *params, const float *in_gfs, float *rhs_gfs);
+int Maxwell_rhs_eval(const NRGPU_PARAMSTRUCT *params, const double *in_gfs, double *rhs_gfs);
+int Maxwell_rhs_eval_f32(const NRGPU_PARAMSTRUCT *params, const float *in_gfs, float *rhs_gfs);
 /* Maxwell divergence constraint C = d_i E^i at interior points
  * (VacuumMaxwell_Flat_Evol_Cartesian.py:49-52) into aux_gfs[0]. */
-int Maxwell_Constraints(const paramstruct *params, const double *in_gfs, double *aux_gfs);
+int Maxwell_Constraints(const NRGPU_PARAMSTRUCT *params, const double *in_gfs, double *aux_gfs);
 /* Vacuum Maxwell System II in rescaled curvilinear form
  * (Maxwell/VacuumMaxwell_Flat_Evol_Curvilinear_rescaled.py:22-190; the
  * rhs_eval of Tutorial-Start_to_Finish-Solving_Maxwells_Equations_in_Vacuum-
@@ -314,49 +324,49 @@ int Maxwell_Constraints(const paramstruct *params, const double *in_gfs, double 
  * NULL on a Cartesian grid.  Constraints C (divergence of E) and G
  * (Gamma - div A) into aux_gfs[0], aux_gfs[1].  Toroidal-dipole data in the
  * grid's basis (Maxwell/InitialData.py:26-117, System II) at every point. */
-int MaxwellCurvilinear_rhs_eval(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+int MaxwellCurvilinear_rhs_eval(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, const double *in_gfs,
                                 double *rhs_gfs);
-int MaxwellCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params, const float *in_gfs,
+int MaxwellCurvilinear_rhs_eval_f32(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, const float *in_gfs,
                                     float *rhs_gfs);
-int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+int MaxwellCurvilinear_constraints(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, const double *in_gfs,
                                    double *aux_gfs);
-int MaxwellCurvilinear_initial_data_toroidal_dipole(const paramstruct *params, double amp, double lam,
+int MaxwellCurvilinear_initial_data_toroidal_dipole(const NRGPU_PARAMSTRUCT *params, double amp, double lam,
                                                     double time, double *in_gfs);
 /* BSSN conformal Ricci tensor into auxevol_gfs (RbarDD00..22, 6 gfs):
  * Ricci_eval(rfmstruct, params, in_gfs, auxevol_gfs)
  * (BSSN_quantities.py:260-425; Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:501-502) */
-int BSSN_Ricci_eval(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_Ricci_eval(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                     const double *in_gfs, double *auxevol_gfs);
-int BSSN_Ricci_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_Ricci_eval_f32(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                         const float *in_gfs, float *auxevol_gfs);
 /* BSSN + gauge RHSs: rhs_eval(rfmstruct, params, auxevol_gfs, in_gfs, rhs_gfs)
  * (BSSN_RHSs.py:28-328, BSSN_gauge_RHSs.py:33-293; ...Two_BHs_Collide.ipynb:477-478) */
-int BSSN_rhs_eval(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_rhs_eval(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                   const double *auxevol_gfs, const double *in_gfs, double *rhs_gfs);
-int BSSN_rhs_eval_f32(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_rhs_eval_f32(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                       const float *auxevol_gfs, const float *in_gfs, float *rhs_gfs);
 /* The same two functions in the reference's no-precompute form
  * rhs_eval(params, xx, auxevol_gfs, in_gfs, rhs_gfs)
  * (...Two_BHs_Collide-no_rfm_precompute.ipynb:477): the reference metric is
  * evaluated at each point from the caller's coordinate arrays xx[0][i0],
  * xx[1][i1] (device pointers; xx[2] is not read).  FP64. */
-int BSSN_Ricci_eval_xx(const paramstruct *params, double *xx[3], const double *in_gfs, double *auxevol_gfs);
-int BSSN_rhs_eval_xx(const paramstruct *params, double *xx[3], const double *auxevol_gfs,
+int BSSN_Ricci_eval_xx(const NRGPU_PARAMSTRUCT *params, double *xx[3], const double *in_gfs, double *auxevol_gfs);
+int BSSN_rhs_eval_xx(const NRGPU_PARAMSTRUCT *params, double *xx[3], const double *auxevol_gfs,
                      const double *in_gfs, double *rhs_gfs);
 /* enforce_detgammabar_constraint(rfmstruct, params, in_gfs) at ALL points
  * (Enforce_Detgammabar_Constraint.py:16-75).  FP64 arithmetic on FP64 data;
  * float-float arithmetic (~48 significant bits, FP32 pipe) on FP32 data. */
-int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_enforce_detgammabar_constraint(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                         double *in_gfs);
-int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_enforce_detgammabar_constraint_f32(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                             float *in_gfs);
 /* Hamiltonian constraint H at interior points into aux_gfs[0]
  * (BSSN_constraints.py:19-74; Ricci evaluated inline). */
-int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_Hamiltonian_constraint(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                 const double *in_gfs, double *aux_gfs);
 /* Momentum constraint M^i (rescaled by ReU) at interior points into
  * aux_gfs[0..2] (BSSN_constraints.py:76-126). */
-int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
+int BSSN_momentum_constraint(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                              const double *in_gfs, double *aux_gfs);
 
 /* Matter terms of the constraints (BSSN_stress_energy_source_terms.py:134-161;
@@ -364,7 +374,7 @@ int BSSN_momentum_constraint(const rfm_struct *rfm, const paramstruct *params,
  * MU[i] += -8 pi S^i / ReU^i at interior points, from the ten T4UU
  * gridfunctions T4UU00, 01, 02, 03, 11, 12, 13, 22, 23, 33 (FP64).  H or MU
  * may be NULL.  Call after BSSN_Hamiltonian_constraint / BSSN_momentum_constraint. */
-int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs,
+int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, const double *in_gfs,
                                       const double *T4UU_gfs, double *H_gf, double *MU_gfs);
 /* psi_4 in the quasi-Kinnersley tetrad (BSSN/Psi4.py:14-193 with
  * BSSN/Psi4_tetrads.py:25-193; the reference's psi4() of
@@ -373,7 +383,7 @@ int BSSN_constraints_add_source_terms(const rfm_struct *rfm, const paramstruct *
  * psi4_gfs[0], Im psi_4 into psi4_gfs[1] (two gridfunctions of the grid), at
  * interior points with i0_min <= i0 < i0_max (a radial shell or slab; pass
  * -1, -1 for the whole interior).  FP64. */
-int BSSN_psi4(const rfm_struct *rfm, const paramstruct *params, const double *in_gfs, double *psi4_gfs,
+int BSSN_psi4(const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, const double *in_gfs, double *psi4_gfs,
               int i0_min, int i0_max);
 /* Spin-weight -2 spherical-harmonic modes of psi_4 on the shell i0 of a
  * Spherical/SinhSpherical grid (driver_psi4_spinweightm2_decomposition and
@@ -382,7 +392,7 @@ int BSSN_psi4(const rfm_struct *rfm, const paramstruct *params, const double *in
  * sum over interior (theta, phi) of psi4 conj(sY_lm) sin(theta) dxx1 dxx2,
  * q running over l = 2..l_max (<= 12), m = -l..l.  modes: device, 2 *
  * ((l_max+1)^2 - 4) doubles.  psi4_gfs as written by BSSN_psi4. */
-int BSSN_psi4_spinweightm2_decomposition(const paramstruct *params, const double *psi4_gfs, int i0, int l_max,
+int BSSN_psi4_spinweightm2_decomposition(const NRGPU_PARAMSTRUCT *params, const double *psi4_gfs, int i0, int l_max,
                                          double *modes);
 
 /* --------------------------------------------------------- initial data */
@@ -390,13 +400,13 @@ int BSSN_psi4_spinweightm2_decomposition(const paramstruct *params, const double
  * kind 0 PlaneWave (uu = sin(khat.x - c t) + 2, vv = d uu/dt, khat = kk/|kk|),
  * kind 1 SphericalGaussian (width sigma), at Cartesian positions of the grid's
  * CoordSystem, time `time`, c = params->wavespeed. */
-int ScalarWave_initial_data(const paramstruct *params, int kind, double time, const double kk[3],
+int ScalarWave_initial_data(const NRGPU_PARAMSTRUCT *params, int kind, double time, const double kk[3],
                             double sigma, double *in_gfs);
 /* Brill-Lindquist two-puncture data converted to rescaled BSSN variables in
  * the grid's coordinates at ALL points (BrillLindquist.py:48-82,
  * ADM_Exact_Spherical_or_Cartesian_to_BSSNCurvilinear.py:16-135,
  * BSSN_ID_function_string.py:9-45). */
-int BSSN_initial_data_BrillLindquist(const paramstruct *params,
+int BSSN_initial_data_BrillLindquist(const NRGPU_PARAMSTRUCT *params,
                                      double BH1_mass, const double BH1_posn[3],
                                      double BH2_mass, const double BH2_posn[3],
                                      double *in_gfs);
@@ -409,28 +419,28 @@ int BSSN_initial_data_BrillLindquist(const paramstruct *params,
  * the RHS kernel's epilogue at interior points; ghost points are set by the
  * boundary conditions, as in the reference where every ghost point is a
  * boundary point.  rfm may be NULL for Cartesian grids. */
-int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruct *params,
+int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                              const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* The same step, unfused, exactly in the reference's order: separate RHS
  * kernel, LOOP_ALL_GFS_GPS update over all points, BCs, rescale. */
-int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const paramstruct *params,
+int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                      const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* The RHS kernel(s) of one substep of MoL_step_forward_in_time alone, with
  * the substep's fused RK update and no boundary conditions; for timing and
  * profiling a step's dominant kernel.  which: 0 every RHS kernel of the
  * substep, 1 BSSN Ricci_eval only, 2 BSSN rhs_eval only.  The buffers must
  * hold a previous step's values (e.g. after one full step). */
-int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *params, MoL_gridfunctions *gfs,
+int MoL_substep_rhs(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, MoL_gridfunctions *gfs,
                     int stage, double dt, int which);
 /* The RK4 step of the reference's Sommerfeld drivers: RHS_string = rhs_eval +
  * apply_bcs_sommerfeld (on the stage's RHS), empty post_RHS_string, the
  * update over every point (C_Code_Generation.py:266-329).  FP64. */
-int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const paramstruct *params,
+int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                         const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* Host-buffer form for callers whose state lives in host memory: copies
  * y_n_gfs (host, FP64, pinned or pageable) to gfs->y_n_gfs, runs n_steps
  * steps, copies the state back, and synchronises the stream. */
-int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *params,
+int MoL_evolve_host(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                     const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt,
                     int n_steps, double *y_n_gfs_host);
 
@@ -495,15 +505,15 @@ int nrgpu_batch_get_tile(const nrgpu_batch *batch, int *tx, int *ty, int *grid);
  *   MoL_adjoint_step_backward:  lam_out = (dy_{n+1}/dy_n)^T lam_in for one
  *       MoL_step_forward_in_time step; lam_in is overwritten; scratch holds
  *       4 * NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot doubles.  Maxwell only. */
-int Maxwell_rhs_eval_adjoint(const paramstruct *params, const double *adj_rhs_gfs, double *adj_in_gfs);
-int apply_bcs_curvilinear_adjoint(const paramstruct *params, const bc_struct *bcstruct, int NUM_GFS,
+int Maxwell_rhs_eval_adjoint(const NRGPU_PARAMSTRUCT *params, const double *adj_rhs_gfs, double *adj_in_gfs);
+int apply_bcs_curvilinear_adjoint(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct, int NUM_GFS,
                                   const int8_t *gfs_parity, double *adj_gfs);
-int MoL_adjoint_step_backward(int system, const paramstruct *params, const bc_struct *bcstruct,
+int MoL_adjoint_step_backward(int system, const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
                               double *lam_in, double *lam_out, double *scratch, double dt);
 /* Toroidal-dipole initial data (Maxwell/InitialData.py:41-104) at all
  * points, and its derivatives with respect to amp and lam (any of the three
  * outputs may be NULL). */
-int Maxwell_initial_data_toroidal_dipole(const paramstruct *params, double amp, double lam, double time,
+int Maxwell_initial_data_toroidal_dipole(const NRGPU_PARAMSTRUCT *params, double amp, double lam, double time,
                                          double *in_gfs, double *d_in_d_amp, double *d_in_d_lam);
 /* Extraction sphere: tricubic Lagrange interpolation of gridfunctions
  * gf0..gf0+ngf-1 at npts Cartesian points (device array pts[3*npts]) into
@@ -513,12 +523,12 @@ int Maxwell_initial_data_toroidal_dipole(const paramstruct *params, double amp, 
  * nrgpu_sphere_sample_adjoint adds the gradient of J = sqrt(accum[0]) with
  * respect to the sampled gridfunctions for one sample set:
  * adj_gfs += (scale/J) sum_p wts[p] samples[p] (x) interpolation weights. */
-int nrgpu_sphere_sample(const paramstruct *params, const double *gfs, int gf0, int ngf, const double *pts,
+int nrgpu_sphere_sample(const NRGPU_PARAMSTRUCT *params, const double *gfs, int gf0, int ngf, const double *pts,
                         const double *wts, int npts, double scale, double *samples, double *accum);
-int nrgpu_sphere_sample_adjoint(const paramstruct *params, const double *samples, int gf0, int ngf,
+int nrgpu_sphere_sample_adjoint(const NRGPU_PARAMSTRUCT *params, const double *samples, int gf0, int ngf,
                                 const double *pts, const double *wts, int npts, double scale,
                                 const double *accum, double *adj_gfs);
-int nrgpu_sphere_check(const paramstruct *params, int *outside);
+int nrgpu_sphere_check(const NRGPU_PARAMSTRUCT *params, int *outside);
 /* result[0] = sum_i a[i] b[i] (device arrays, FP64, fixed summation order). */
 int nrgpu_dot(const double *a, const double *b, long long n, double *scratch, int scratch_len, double *result);
 
@@ -528,7 +538,7 @@ int nrgpu_dot(const double *a, const double *b, long long n, double *scratch, in
  * `result` is a DEVICE pointer to 2 doubles.  Used for the RMS L2 norms of
  * the constraint diagnostics (Tutorial-Start_to_Finish-Solving_Maxwells_
  * Equations_in_Vacuum-Cartesian.ipynb:1089-1106). */
-int nrgpu_l2_norm_sq(const paramstruct *params, const double *gfs, int gf,
+int nrgpu_l2_norm_sq(const NRGPU_PARAMSTRUCT *params, const double *gfs, int gf,
                      double *scratch, int scratch_len, double *result);
 /* The same reduction for callers that cannot allocate device memory: host
  * codes that pass this library only the arrays they own and allow no device
@@ -543,7 +553,7 @@ int nrgpu_l2_norm_sq(const paramstruct *params, const double *gfs, int gf,
  * device's primary context) it is stale, so do not call this entry point
  * again in that process.  All calls share the array, so calls that overlap
  * on the GPU race; no cudaMalloc/cudaFree. */
-int nrgpu_l2_norm_sq_static(const paramstruct *params, const double *gfs, int gf, double *result);
+int nrgpu_l2_norm_sq_static(const NRGPU_PARAMSTRUCT *params, const double *gfs, int gf, double *result);
 
 #ifdef __cplusplus
 }

@@ -33,6 +33,9 @@ Writes:
       generated rhs_eval: central-midplane errors against the exact solution
       at t = 2.5, 5, 15.625 and 4096 sampled points of the final 64^3 state
       (`config1`).
+  declare_Cparameters_struct_<config>.h  the reference's generated
+      paramstruct declarations of bssn_ship_sinhsph_fd4 and bssn_cart_fd6
+      (NRPy_param_funcs.py:216-304), for the params-shim test (`params`).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -263,6 +266,18 @@ def c1_central(e, N, g):
     n = N + 2 * g
     lo, hi = int(n * 0.25) + 1, int(np.ceil(n * 0.75))
     return e[n // 2, lo:hi, lo:hi]
+
+
+PARAM_CFGS = ("bssn_ship_sinhsph_fd4", "bssn_cart_fd6")
+
+
+def params():
+    """declare_Cparameters_struct_<cfg>.h: copies of the reference's generated
+    paramstruct declarations (written by oracle/gen_ref*.py into oracle/_ref/src)."""
+    import shutil
+    for cfg in PARAM_CFGS:
+        src = os.path.join(ROOT, "oracle", "_ref", "src", cfg, "declare_Cparameters_struct.h")
+        shutil.copy(src, os.path.join(HERE, "declare_Cparameters_struct_%s.h" % cfg))
 
 
 def config1():
@@ -526,6 +541,8 @@ if __name__ == "__main__":
         evolution_scalarwave()
     if "config1" in what:
         config1()
+    if "params" in what:
+        params()
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)
