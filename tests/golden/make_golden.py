@@ -36,6 +36,10 @@ Writes:
   declare_Cparameters_struct_<config>.h  the reference's generated
       paramstruct declarations of bssn_ship_sinhsph_fd4 and bssn_cart_fd6
       (NRPy_param_funcs.py:216-304), for the params-shim test (`params`).
+  ref_sommerfeld.npz  the reference's generated apply_bcs_sommerfeld
+      (oracle/gen_ref_somm.py: ScalarWave on Spherical and SinhSpherical
+      10x8x6 grids, d_r orders 2 and 4) applied to seeded gridfunctions and
+      RHSs: the RHS after the boundary condition (`sommerfeld`).
   swsh_m2.json  the reference's generated spin-weight -2 spherical
       harmonics (C, l <= 8) at five (theta, phi) points.
   fd_coefficients.json  exact FD coefficients of
@@ -278,6 +282,36 @@ def params():
     for cfg in PARAM_CFGS:
         src = os.path.join(ROOT, "oracle", "_ref", "src", cfg, "declare_Cparameters_struct.h")
         shutil.copy(src, os.path.join(HERE, "declare_Cparameters_struct_%s.h" % cfg))
+
+
+SOMM = {"somm_sph_dr2": ("Spherical", 2), "somm_sph_dr4": ("Spherical", 4),
+        "somm_sinhsph_dr2": ("SinhSpherical", 2), "somm_sinhsph_dr4": ("SinhSpherical", 4)}
+SOMM_GRID = dict(Nxx=(10, 8, 6), AMPL=5.0, SINHW=0.3, RMAX=5.0)
+
+
+def somm_inputs(cfg, shape):
+    from tests.helpers import sommerfeld_inputs
+    return sommerfeld_inputs(SOMM[cfg], shape)
+
+
+def sommerfeld():
+    """ref_sommerfeld.npz: for each SOMM configuration, the RHS after the
+    reference's generated apply_bcs_sommerfeld (strict build)."""
+    import ctypes as C
+    import oracle.grid as og
+    from oracle.ref_build import LIB
+    out = {}
+    g = SOMM_GRID
+    for cfg, (coord, dr) in SOMM.items():
+        gp = og.GridParams(coord, g["Nxx"], 2, 4, AMPL=g["AMPL"], SINHW=g["SINHW"], RMAX=g["RMAX"])
+        lib = C.CDLL(os.path.join(LIB, "%s.strict.so" % cfg))
+        lib.somm_setup.argtypes = [C.c_int] * 3 + [C.c_double] * 3
+        lib.somm_setup(*g["Nxx"], g["AMPL"], g["SINHW"], g["RMAX"])
+        f, rhs = somm_inputs(cfg, gp.shape)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        lib.somm_apply(dp(f), dp(rhs))
+        out[cfg] = rhs
+    np.savez_compressed(os.path.join(HERE, "ref_sommerfeld.npz"), **out)
 
 
 def config1():
@@ -543,6 +577,8 @@ if __name__ == "__main__":
         config1()
     if "params" in what:
         params()
+    if "sommerfeld" in what:
+        sommerfeld()
     names = [w[len("trusted:"):] for w in what if w.startswith("trusted:")]
     if names:
         trusted(names)

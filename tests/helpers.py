@@ -64,3 +64,17 @@ def smooth_state(ngf, gp, seed=SEED, amp=0.1, offsets=None):
         for g, o in offsets.items():
             out[g] += o
     return out
+
+
+# Sommerfeld fixture configurations (tests/golden/ref_sommerfeld.npz): name ->
+# (CoordSystem, d_r FD order); ScalarWave, FD4, 2 ghosts, on this grid.
+SOMMERFELD_CFGS = {"somm_sph_dr2": ("Spherical", 2), "somm_sph_dr4": ("Spherical", 4),
+                   "somm_sinhsph_dr2": ("SinhSpherical", 2), "somm_sinhsph_dr4": ("SinhSpherical", 4)}
+SOMMERFELD_GRID = dict(Nxx=(10, 8, 6), AMPL=5.0, SINHW=0.3, RMAX=5.0)
+
+
+def sommerfeld_inputs(coord_dr, shape):
+    """Seeded (gfs, rhs) of a Sommerfeld fixture configuration."""
+    coord, dr = coord_dr
+    rng = np.random.default_rng(dr + 100 * (coord == "SinhSpherical"))
+    return rng.standard_normal((2,) + shape), rng.standard_normal((2,) + shape)

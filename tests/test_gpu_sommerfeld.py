@@ -1,13 +1,16 @@
-"""Sommerfeld radiation boundary condition on the GPU vs the oracle
-(CurviBoundaryConditions.py:259-658): the RHS at ghost points for Cartesian,
-Spherical and SinhSpherical grids at FD orders 2 and 4, and RK4 steps of the
-reference's Sommerfeld driver form."""
+"""Sommerfeld radiation boundary condition on the GPU vs the reference's own
+generated apply_bcs_sommerfeld (CurviBoundaryConditions.py:259-658, fixture
+tests/golden/ref_sommerfeld.npz: Spherical and SinhSpherical at d_r orders 2
+and 4) and vs the oracle (the RHS at ghost points for every coordinate
+family at FD orders 2 and 4, and RK4 steps of the reference's Sommerfeld
+driver form)."""
+import os
 import numpy as np
 import pytest
 
 import oracle.bcs as ob
 import oracle.wave_maxwell as ow
-from tests.helpers import grids, per_gf_rel
+from tests.helpers import SOMMERFELD_CFGS, SOMMERFELD_GRID, grids, per_gf_rel, sommerfeld_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -17,6 +20,22 @@ KW = dict(AMPL=5.0, SINHW=0.3, RMAX=5.0, domain=(-3.0, 3.0))
 def _set(fd, ngf, falloff=3.0):
     from nrpytutorial_gb300 import sommerfeld_params
     sommerfeld_params(fd, speed=[1.0] * ngf, f_inf=[0.0] * ngf, radial_falloff_power=[falloff] * ngf)
+
+
+@pytest.mark.parametrize("cfg", sorted(SOMMERFELD_CFGS))
+def test_sommerfeld_rhs_matches_reference_generated_c(cuda, cfg):
+    import torch
+    from nrpytutorial_gb300 import Evolution
+    coord, dr = SOMMERFELD_CFGS[cfg]
+    g = SOMMERFELD_GRID
+    G, gp = grids("ScalarWave", coord, g["Nxx"], 4, AMPL=g["AMPL"], SINHW=g["SINHW"], RMAX=g["RMAX"])
+    ev = Evolution("ScalarWave", G, device=cuda, boundary="sommerfeld")
+    _set(dr, 2)
+    f, rhs = sommerfeld_inputs(SOMMERFELD_CFGS[cfg], gp.shape)
+    want = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_sommerfeld.npz"))[cfg]
+    got = torch.tensor(rhs, device=cuda)
+    ev.apply_sommerfeld(torch.tensor(f, device=cuda), got)
+    assert per_gf_rel(got.cpu().numpy(), want) < 1e-12
 
 
 @pytest.mark.parametrize("system,coord,Nxx,order,fd", [
