@@ -17,7 +17,7 @@ Tutorial-Start_to_Finish-BSSNCurvilinear-Two_BHs_Collide.ipynb:1165-1166).
 stage pairs, FP64 RK state) with its error against the FP64 run stated in
 the line; the FP64 run, the plain FP32-stage run and the other
 configurations (Cartesian 256^3 FD6, 512 batched ScalarWave evolutions, the
-Maxwell adjoint gradient) are reported beside it.
+Maxwell and ScalarWave adjoint gradients) are reported beside it.
 
 Prints one JSON line (rank 0).  For N > 1 (torchrun) every rank evolves an
 independent replica ("replicas only": one evolution does not shard here).
@@ -426,6 +426,8 @@ def run_gpu(args):
         a5 = run_config5(dev, args.config5_steps, N=PROFILE_N5 or 128)
         out["adjoint_maxwell_128"] = a5
         out["adjoint_over_forward"] = a5["adjoint_over_forward"]
+    if args.sw_adjoint_steps > 0:
+        out["adjoint_scalarwave_sinhsph"] = run_scalarwave_adjoint(dev, args.sw_adjoint_steps)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -704,6 +706,54 @@ def run_config5(dev, K, N=128):
             "forward_gp_updates_per_s": K * nint / t_fwd, "checkpoints": len(m.checkpoints)}
 
 
+
+def run_scalarwave_adjoint(dev, K, Nxx=(128, 32, 64)):
+    """ScalarWave on a SinhSpherical grid (AMPL 10, SINHW 0.2, FD4, FP64),
+    K RK4 steps (CFL 0.5) from a Gaussian pulse u = A exp(-(r-r0)^2/w^2)
+    with seeded (A, r0, w); observable = L2 norm of u over the radial shell
+    at two thirds of the radial extent and the evolution; gradient with
+    respect to (A, r0, w) by the discrete adjoint (checkpoints every 20
+    steps), checked against central differences with h = 1e-6."""
+    import torch
+    from nrpytutorial_gb300 import Grid
+    from nrpytutorial_gb300.adjoint import ScalarWaveExtraction
+    rng = np.random.default_rng(7)
+    A, r0, w = rng.uniform(0.5, 1.5), rng.uniform(1.0, 2.0), rng.uniform(0.6, 1.0)
+    G = Grid("SinhSpherical", Nxx, FD_order=4, NGHOSTS=3, AMPL=10.0, SINHW=0.2)
+    i0 = 3 + (2 * Nxx[0]) // 3
+    m = ScalarWaveExtraction(G, i0, n_steps=K, checkpoint_every=20, device=dev)
+    m.forward(A, r0, w)  # warm-up
+    m.gradient()
+
+    def timed(f):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        r = f()
+        b.record()
+        torch.cuda.synchronize()
+        return r, a.elapsed_time(b) / 1e3
+
+    J, t_fwd = timed(lambda: m.forward(A, r0, w))
+    g, t_bwd = timed(m.gradient)
+    h = 1e-6
+    fd = []
+    for k in range(3):
+        p, q = [A, r0, w], [A, r0, w]
+        p[k] += h
+        q[k] -= h
+        fd.append((m.forward(*p) - m.forward(*q)) / (2 * h))
+    rel = [abs(g[i] - fd[i]) / abs(fd[i]) for i in range(3)]
+    nint = Nxx[0] * Nxx[1] * Nxx[2]
+    return {"workload": "ScalarWave SinhSpherical AMPL=10 SINHW=0.2 %dx%dx%d FD4 FP64, %d RK4 steps, Gaussian "
+                        "A=%.6f r0=%.6f w=%.6f (seed 7), u on the shell i0=%d, checkpoints every 20"
+                        % (Nxx + (K, A, r0, w, i0)),
+            "J": J, "grad": [float(v) for v in g], "grad_central_fd_h1e-6": [float(v) for v in fd],
+            "grad_rel_err_vs_fd": rel, "forward_s": t_fwd, "adjoint_s": t_bwd,
+            "adjoint_over_forward": t_bwd / t_fwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
+            "forward_gp_updates_per_s": K * nint / t_fwd, "checkpoints": len(m.checkpoints)}
+
+
 # ------------------------------------------------------------ CPU reference
 class RefStepper:
     """The reference's generated Ricci_eval/rhs_eval/enforce (OpenMP -Ofast
@@ -914,6 +964,8 @@ def main():
                     help="small configurations 3-5 (96^3, 64 instances, 48^3) for profiler captures")
     ap.add_argument("--config5-steps", type=int, default=300,
                     help="RK4 steps of the Maxwell 128^3 adjoint-gradient run (0 skips it)")
+    ap.add_argument("--sw-adjoint-steps", type=int, default=200,
+                    help="RK4 steps of the SinhSpherical ScalarWave adjoint-gradient run (0 skips it)")
     ap.add_argument("--config4-steps", type=int, default=400,
                     help="RK4 steps of the 512-instance batched ScalarWave run (0 skips it)")
     args = ap.parse_args()

@@ -254,6 +254,11 @@ int         nrgpu_fd_coeffs(int order, int kind, double *out);
  * family), as the reference does before building BC maps. */
 int    set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3],
                                          NRGPU_PARAMSTRUCT *params, double *xx[3]);
+/* reference_metric.py:1397-1410 (xx_to_Cart_h): Cartesian position of
+ * grid point (i0, i1, i2), from the host arrays xx[d] (or, where xx or xx[d]
+ * is NULL, the cell-centred coordinate of the uniform grid).  Host; returns
+ * a status (the reference's function is void). */
+int    xx_to_Cart(const NRGPU_PARAMSTRUCT *params, double *xx[3], int i0, int i1, int i2, double xCart[3]);
 /* reference_metric.py:1412-1439 (find_timestep): CFL * min over interior
  * points of the proper spacing dxx_i * scalefactor_i, / wavespeed.  Host. */
 double find_timestep(const NRGPU_PARAMSTRUCT *params, double CFL_FACTOR);
@@ -492,29 +497,54 @@ int nrgpu_batch_set_tile(nrgpu_batch *batch, int tx, int ty, int grid);
 int nrgpu_batch_get_tile(const nrgpu_batch *batch, int *tx, int *ty, int *grid);
 
 /* ------------------------------------------------------------ adjoint */
-/* Discrete adjoint of the Maxwell System I evolution (FP64, Cartesian).  The
- * reference has no adjoint; these are the transposes of the linear maps
- * above, so that gradients of observables of an evolution with respect to
- * its initial data are exact for the discretised problem.
- *   Maxwell_rhs_eval_adjoint:  adj_in = L^T adj_rhs at every point, where L
- *       is Maxwell_rhs_eval (interior rows only); adj_rhs is read at
- *       interior points only.
+/* Discrete adjoints of the linear evolutions: Maxwell System I (FP64,
+ * Cartesian) and ScalarWave (FP64, Cartesian and the curvilinear families
+ * Spherical/SinhSpherical(v2)/Cylindrical/SinhCylindrical(v2)/SymTP/
+ * SinhSymTP).  The reference has no adjoint; these are the transposes of
+ * the linear maps above, so that gradients of observables of an evolution
+ * with respect to its initial data are exact for the discretised problem.
+ *   Maxwell_rhs_eval_adjoint, ScalarWave_rhs_eval_adjoint:  adj_in = L^T
+ *       adj_rhs at every point, where L is Maxwell_rhs_eval /
+ *       ScalarWave(Curvilinear)_rhs_eval (interior rows only); adj_rhs is
+ *       read at interior points only.  rfmstruct: as for
+ *       ScalarWaveCurvilinear_rhs_eval (NULL on Cartesian grids).
  *   apply_bcs_curvilinear_adjoint:  in place, the transpose of
  *       apply_bcs_curvilinear: ghost adjoints are added onto the points they
  *       were computed from (phases in reverse order) and zeroed.
  *   MoL_adjoint_step_backward:  lam_out = (dy_{n+1}/dy_n)^T lam_in for one
- *       MoL_step_forward_in_time step; lam_in is overwritten; scratch holds
- *       4 * NUM_EVOL_GFS * Nxx_plus_2NGHOSTS_tot doubles.  Maxwell only. */
+ *       MoL_step_forward_in_time step of `system` (NRGPU_SYS_MAXWELL or
+ *       NRGPU_SYS_SCALARWAVE) with extrapolation/parity boundary conditions;
+ *       lam_in is overwritten; scratch holds 4 * NUM_EVOL_GFS *
+ *       Nxx_plus_2NGHOSTS_tot doubles. */
 int Maxwell_rhs_eval_adjoint(const NRGPU_PARAMSTRUCT *params, const double *adj_rhs_gfs, double *adj_in_gfs);
+int ScalarWave_rhs_eval_adjoint(const rfm_struct *rfmstruct, const NRGPU_PARAMSTRUCT *params,
+                                const double *adj_rhs_gfs, double *adj_in_gfs);
 int apply_bcs_curvilinear_adjoint(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct, int NUM_GFS,
                                   const int8_t *gfs_parity, double *adj_gfs);
-int MoL_adjoint_step_backward(int system, const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
-                              double *lam_in, double *lam_out, double *scratch, double dt);
+int MoL_adjoint_step_backward(int system, const rfm_struct *rfmstruct, const NRGPU_PARAMSTRUCT *params,
+                              const bc_struct *bcstruct, double *lam_in, double *lam_out, double *scratch,
+                              double dt);
 /* Toroidal-dipole initial data (Maxwell/InitialData.py:41-104) at all
  * points, and its derivatives with respect to amp and lam (any of the three
  * outputs may be NULL). */
 int Maxwell_initial_data_toroidal_dipole(const NRGPU_PARAMSTRUCT *params, double amp, double lam, double time,
                                          double *in_gfs, double *d_in_d_amp, double *d_in_d_lam);
+/* Gaussian pulse for ScalarWave at all points of any CoordSystem:
+ * uu = A exp(-(r - r0)^2 / w^2), vv = 0, r the Cartesian radius of the point;
+ * and its derivatives with respect to A, r0 and w (each output may be NULL;
+ * all are 2-gridfunction FP64 arrays). */
+int ScalarWave_initial_data_gaussian(const NRGPU_PARAMSTRUCT *params, double A, double r0, double w,
+                                     double *in_gfs, double *d_in_d_A, double *d_in_d_r0, double *d_in_d_w);
+/* Radial shell of a curvilinear grid: the Nxx1*Nxx2 interior (i1, i2)
+ * points of gridfunction gf on the i0 = const shell (i0 an interior index):
+ * samples[q] = f(i0, NGHOSTS + q % Nxx1, NGHOSTS + q / Nxx1), and
+ * accum[0] += scale * sum_q wts[q] samples[q]^2 (device arrays).
+ * nrgpu_shell_sample_adjoint adds the gradient of J = sqrt(accum[0]) for one
+ * sample set: adj_gfs[gf] += (scale/J) wts[q] samples[q] at the shell points. */
+int nrgpu_shell_sample(const NRGPU_PARAMSTRUCT *params, const double *gfs, int gf, int i0, const double *wts,
+                       double scale, double *samples, double *accum);
+int nrgpu_shell_sample_adjoint(const NRGPU_PARAMSTRUCT *params, const double *samples, int gf, int i0,
+                               const double *wts, double scale, const double *accum, double *adj_gfs);
 /* Extraction sphere: tricubic Lagrange interpolation of gridfunctions
  * gf0..gf0+ngf-1 at npts Cartesian points (device array pts[3*npts]) into
  * samples[npts*ngf], and accum[0] += scale * sum_p wts[p] |f(x_p)|^2 (device

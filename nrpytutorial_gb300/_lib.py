@@ -138,7 +138,14 @@ _PROTOS = {
     "nrgpu_l2_norm_sq_static": (C.c_int, [P(paramstruct), vp, C.c_int, vp]),
     "Maxwell_rhs_eval_adjoint": (C.c_int, [P(paramstruct), vp, vp]),
     "apply_bcs_curvilinear_adjoint": (C.c_int, [P(paramstruct), P(bc_struct), C.c_int, P(C.c_int8), vp]),
-    "MoL_adjoint_step_backward": (C.c_int, [C.c_int, P(paramstruct), P(bc_struct), vp, vp, vp, C.c_double]),
+    "xx_to_Cart": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, C.c_int, P(C.c_double)]),
+    "ScalarWave_rhs_eval_adjoint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
+    "MoL_adjoint_step_backward": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct), vp, vp, vp,
+                                            C.c_double]),
+    "ScalarWave_initial_data_gaussian": (C.c_int, [P(paramstruct), C.c_double, C.c_double, C.c_double,
+                                                   vp, vp, vp, vp]),
+    "nrgpu_shell_sample": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp, C.c_double, vp, vp]),
+    "nrgpu_shell_sample_adjoint": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp, C.c_double, vp, vp]),
     "Maxwell_initial_data_toroidal_dipole": (C.c_int, [P(paramstruct), C.c_double, C.c_double, C.c_double,
                                                        vp, vp, vp]),
     "nrgpu_sphere_sample": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_double,

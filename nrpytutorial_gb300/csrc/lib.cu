@@ -165,6 +165,19 @@ int set_Nxx_dxx_invdx_params__and__xx(int EigenCoord, const int Nxx[3], paramstr
   return NRGPU_OK;
 }
 
+int xx_to_Cart(const paramstruct *p, double *xx[3], int i0, int i1, int i2, double xCart[3]) {
+  NRGPU_REQUIRE(p && xCart, "NULL argument");
+  NRGPU_REQUIRE(i0 >= 0 && i0 < p->Nxx_plus_2NGHOSTS0 && i1 >= 0 && i1 < p->Nxx_plus_2NGHOSTS1 && i2 >= 0 &&
+                    i2 < p->Nxx_plus_2NGHOSTS2,
+                "point (%d, %d, %d) outside the grid", i0, i1, i2);
+  const double x0 = (xx && xx[0]) ? xx[0][i0] : xx_of(p->xxmin0, p->dxx0, i0, p->NGHOSTS);
+  const double x1 = (xx && xx[1]) ? xx[1][i1] : xx_of(p->xxmin1, p->dxx1, i1, p->NGHOSTS);
+  const double x2 = (xx && xx[2]) ? xx[2][i2] : xx_of(p->xxmin2, p->dxx2, i2, p->NGHOSTS);
+  double J[3][3];
+  cart_jacobian(coord_params(*p), x0, x1, x2, xCart, J);
+  return NRGPU_OK;
+}
+
 double find_timestep(const paramstruct *p, double CFL_FACTOR) {
   if (check_params(p) != NRGPU_OK) return -1.0;
   // min over interior points of dxx_i s_i; the scale factors depend on

@@ -83,7 +83,7 @@ def test_rk4_step_adjoint_is_the_transpose(cuda):
     Phix = ev.y_n.clone()
     lam_in, lam_out = y.clone(), torch.zeros_like(y)
     scratch = torch.zeros((4,) + tuple(y.shape), dtype=torch.float64, device=cuda)
-    _lib.check(ev.lib.MoL_adjoint_step_backward(1, C.byref(G.params), C.byref(ev.bc), _lib.ptr(lam_in),
+    _lib.check(ev.lib.MoL_adjoint_step_backward(1, None, C.byref(G.params), C.byref(ev.bc), _lib.ptr(lam_in),
                                                 _lib.ptr(lam_out), _lib.ptr(scratch), dt), "adjoint step")
     a, b = _dot(Phix, y), _dot(x, lam_out)
     assert abs(a - b) <= 1e-12 * abs(a), (a, b)
