@@ -289,6 +289,24 @@ int apply_bcs_curvilinear(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcst
                           int NUM_GFS, const int8_t *gfs_parity, double *gfs);
 int apply_bcs_curvilinear_f32(const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
                               int NUM_GFS, const int8_t *gfs_parity, float *gfs);
+/* The same boundary conditions on one slab of a grid split along i2 over
+ * several ranks (no counterpart in the reference, whose drivers run one
+ * grid in one process).  params describe the slab (its own Nxx2 and
+ * xxmin2); indices are the slab's idx3; FP64; device arrays.  A rank applies,
+ * per ghost layer, the outer rule to the outer points it owns, one face
+ * direction per call in the order i0, i1, i2 (nrgpu_bc_outer_points), then
+ * the parity copies of its inner points from source values gathered on the
+ * ranks that own them: nrgpu_bc_gather_points packs buf[j*NUM_GFS + gf] =
+ * gfs[gf][src[j]], the buffers travel rank to rank, and
+ * nrgpu_bc_scatter_parity writes gfs[gf][dest[j]] = +-buf[j*NUM_GFS + gf]
+ * (minus where bit gfs_parity[gf] of parity_bits[j] is set; gfs_parity a
+ * HOST array).  Arithmetic identical to apply_bcs_curvilinear. */
+int nrgpu_bc_outer_points(const NRGPU_PARAMSTRUCT *params, int NUM_GFS, const int *dest, const int *step, int n,
+                          double *gfs);
+int nrgpu_bc_gather_points(const NRGPU_PARAMSTRUCT *params, int NUM_GFS, const int *src, int n,
+                           const double *gfs, double *buf);
+int nrgpu_bc_scatter_parity(const NRGPU_PARAMSTRUCT *params, int NUM_GFS, const int8_t *gfs_parity,
+                            const int *dest, const int *parity_bits, int n, const double *buf, double *gfs);
 
 /* Sommerfeld radiation boundary condition (CurviBoundaryConditions.py:259-658,
  * apply_bcs_sommerfeld): sets rhs_gfs at every ghost point from the state

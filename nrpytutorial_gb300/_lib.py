@@ -138,6 +138,9 @@ _PROTOS = {
     "nrgpu_l2_norm_sq_static": (C.c_int, [P(paramstruct), vp, C.c_int, vp]),
     "Maxwell_rhs_eval_adjoint": (C.c_int, [P(paramstruct), vp, vp]),
     "apply_bcs_curvilinear_adjoint": (C.c_int, [P(paramstruct), P(bc_struct), C.c_int, P(C.c_int8), vp]),
+    "nrgpu_bc_outer_points": (C.c_int, [P(paramstruct), C.c_int, vp, vp, C.c_int, vp]),
+    "nrgpu_bc_gather_points": (C.c_int, [P(paramstruct), C.c_int, vp, C.c_int, vp, vp]),
+    "nrgpu_bc_scatter_parity": (C.c_int, [P(paramstruct), C.c_int, P(C.c_int8), vp, vp, C.c_int, vp, vp]),
     "xx_to_Cart": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, C.c_int, P(C.c_double)]),
     "ScalarWave_rhs_eval_adjoint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "MoL_adjoint_step_backward": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct), vp, vp, vp,

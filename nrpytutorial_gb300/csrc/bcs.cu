@@ -231,6 +231,26 @@ __global__ void bc_inner_kernel(const int *__restrict__ dest, const int *__restr
   f[dest[p]] = neg ? -v : v;
 }
 
+// Point-major exchange buffers of the slab path: buf[j * ngfs + gf].
+__global__ void bc_gather_kernel(const int *__restrict__ src, int npts, int ngfs, long long ntot,
+                                 const double *__restrict__ gfs, double *__restrict__ buf) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  buf[(long long)p * ngfs + gf] = gfs[(long long)gf * ntot + src[p]];
+}
+
+__global__ void bc_scatter_parity_kernel(const int *__restrict__ dest, const int *__restrict__ parity, int npts,
+                                         int ngfs, long long ntot, ParityTypes types,
+                                         const double *__restrict__ buf, double *__restrict__ gfs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gf = blockIdx.y;
+  if (p >= npts || gf >= ngfs) return;
+  const bool neg = (parity[p] >> types.t[gf]) & 1;
+  const double v = buf[(long long)p * ngfs + gf];
+  gfs[(long long)gf * ntot + dest[p]] = neg ? -v : v;
+}
+
 // FP32 pair gridfunctions (value = hi + lo): the outer rule evaluated in
 // FP64 on the values and re-split; the parity copy moves (or negates) both
 // parts, which is exact.
@@ -879,6 +899,58 @@ int apply_bcs_curvilinear(const paramstruct *p, const bc_struct *bc, int NUM_GFS
 int apply_bcs_curvilinear_f32(const paramstruct *p, const bc_struct *bc, int NUM_GFS,
                               const int8_t *gfs_parity, float *gfs) {
   return apply_bcs_impl<float>(p, bc, NUM_GFS, gfs_parity, gfs);
+}
+
+// ------------------------------------------------ slab (one rank's share)
+// The boundary conditions of a grid split into slabs along i2, applied by
+// each rank to the ghost points it owns; indices are the slab's own idx3.
+int nrgpu_bc_outer_points(const paramstruct *p, int NUM_GFS, const int *dest, const int *step, int n,
+                          double *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64 && n >= 0, "bad arguments");
+  if (n == 0) return NRGPU_OK;
+  NRGPU_REQUIRE(dest && step && gfs, "NULL argument");
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  dim3 grid((n + 127) / 128, NUM_GFS);
+  bc_outer_kernel<double><<<grid, 128, 0, stream()>>>(dest, step, n, NUM_GFS, ntot, gfs);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+int nrgpu_bc_gather_points(const paramstruct *p, int NUM_GFS, const int *src, int n, const double *gfs,
+                           double *buf) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64 && n >= 0, "bad arguments");
+  if (n == 0) return NRGPU_OK;
+  NRGPU_REQUIRE(src && gfs && buf, "NULL argument");
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  dim3 grid((n + 127) / 128, NUM_GFS);
+  bc_gather_kernel<<<grid, 128, 0, stream()>>>(src, n, NUM_GFS, ntot, gfs, buf);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+int nrgpu_bc_scatter_parity(const paramstruct *p, int NUM_GFS, const int8_t *gfs_parity, const int *dest,
+                            const int *parity_bits, int n, const double *buf, double *gfs) {
+  int st = check_params(p);
+  if (st) return st;
+  NRGPU_REQUIRE(NUM_GFS >= 1 && NUM_GFS <= 64 && n >= 0, "bad arguments");
+  if (n == 0) return NRGPU_OK;
+  NRGPU_REQUIRE(dest && parity_bits && buf && gfs, "NULL argument");
+  ParityTypes types;
+  memset(&types, 0, sizeof(types));
+  for (int g = 0; g < NUM_GFS; g++) {
+    const int t = gfs_parity ? gfs_parity[g] : 0;
+    NRGPU_REQUIRE(t >= 0 && t <= 9, "parity type %d of gf %d not in 0..9", t, g);
+    types.t[g] = (int8_t)t;
+  }
+  const long long ntot = (long long)p->Nxx_plus_2NGHOSTS0 * p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  dim3 grid((n + 127) / 128, NUM_GFS);
+  bc_scatter_parity_kernel<<<grid, 128, 0, stream()>>>(dest, parity_bits, n, NUM_GFS, ntot, types, buf, gfs);
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
 }
 
 }  // extern "C"

@@ -75,6 +75,29 @@ class Grid:
         self.shape = (np_[2], np_[1], np_[0])  # (i2, i1, i0) numpy order
         self.ntot = np_[0] * np_[1] * np_[2]
 
+    def slab(self, w0, w1):
+        """The planes w0 <= i2 < w1 of this grid as a grid of their own (its
+        interior the planes w0 + NGHOSTS .. w1 - NGHOSTS - 1): the same
+        paramstruct with Nxx2 = w1 - w0 - 2 NGHOSTS and xxmin2 moved to the
+        slab, for the library's interior kernels on one rank's slab."""
+        g = self.NGHOSTS
+        if not (0 <= w0 and w1 <= self.shape[0] and w1 - w0 > 2 * g):
+            raise ValueError("slab planes [%d, %d) invalid" % (w0, w1))
+        s = Grid.__new__(Grid)
+        p = _lib.paramstruct()
+        C.memmove(C.byref(p), C.byref(self.params), C.sizeof(p))
+        p.Nxx2 = w1 - w0 - 2 * g
+        p.Nxx_plus_2NGHOSTS2 = w1 - w0
+        p.xxmin2 = self.params.xxmin2 + w0 * self.params.dxx2
+        p.xxmax2 = p.xxmin2 + p.Nxx2 * self.params.dxx2
+        s.params = p
+        s.xx = [self.xx[0], self.xx[1], np.ascontiguousarray(self.xx[2][w0:w1])]
+        s.CoordSystem, s.NGHOSTS, s.FD_order = self.CoordSystem, g, self.FD_order
+        s.Nxx = (self.Nxx[0], self.Nxx[1], p.Nxx2)
+        s.shape = (w1 - w0, self.shape[1], self.shape[2])
+        s.ntot = s.shape[0] * s.shape[1] * s.shape[2]
+        return s
+
     @property
     def interior(self):
         g = self.NGHOSTS

@@ -18,8 +18,8 @@ from .grid import AUXEVOL_GFS, SYSTEM_GFS, T4UU_GFS, Grid
 class Evolution:
     def __init__(self, system, grid: Grid, precision="fp64", device="cuda", boundary="extrapolation"):
         self.lib = _lib.load()
-        if boundary not in ("extrapolation", "sommerfeld"):
-            raise ValueError("boundary must be 'extrapolation' or 'sommerfeld'")
+        if boundary not in ("extrapolation", "sommerfeld", "none"):
+            raise ValueError("boundary must be 'extrapolation', 'sommerfeld' or 'none'")
         if boundary == "sommerfeld" and precision != "fp64":
             raise ValueError("the Sommerfeld step is FP64")
         self.boundary = boundary
@@ -62,13 +62,21 @@ class Evolution:
             _lib.check(self.lib.rfm_struct__malloc(C.byref(grid.params), C.byref(self.rfm)), "rfm_struct__malloc")
             _lib.check(self.lib.rfm_struct__define(C.byref(grid.params), C.byref(self.rfm)), "rfm_struct__define")
             self._rfm_ok = True
+        # boundary="none": no boundary map (a slab of a grid split over ranks,
+        # whose boundary conditions the slab driver applies); step() is refused
         self.bc = _lib.bc_struct()
-        _lib.check(self.lib.driver_bcstruct(C.byref(grid.params), C.byref(self.bc)), "driver_bcstruct")
+        if boundary != "none":
+            _lib.check(self.lib.driver_bcstruct(C.byref(grid.params), C.byref(self.bc)), "driver_bcstruct")
+            self._bc_ok = True
         self.time = 0.0
 
     # -- plumbing
     def _sync_stream(self):
         _lib.set_stream(torch.cuda.current_stream(self.device))
+
+    def _need_bc(self):
+        if self.boundary == "none":
+            raise RuntimeError("this Evolution has no boundary map (boundary='none')")
 
     def _rfm(self):
         return C.byref(self.rfm) if self._rfm_ok else None
@@ -77,8 +85,9 @@ class Evolution:
         if getattr(self, "_rfm_ok", False):
             self.lib.rfm_struct__freemem(C.byref(self.rfm))
             self._rfm_ok = False
-        if hasattr(self, "bc"):
+        if getattr(self, "_bc_ok", False):
             self.lib.bcstruct_freemem(C.byref(self.bc))
+            self._bc_ok = False
 
     def __del__(self):
         try:
@@ -91,6 +100,7 @@ class Evolution:
         """One RK4 step (MoLtimestepping/RK_MoL.h).  With boundary="sommerfeld"
         the radiation condition acts on each stage's RHS instead
         (MoL_step_forward_in_time_sommerfeld; FP64)."""
+        self._need_bc()
         self._sync_stream()
         if self.boundary == "sommerfeld":
             f = self.lib.MoL_step_forward_in_time_sommerfeld
@@ -185,6 +195,7 @@ class Evolution:
                    "BSSN_Ricci_eval")
 
     def apply_bcs(self, gfs):
+        self._need_bc()
         self._sync_stream()
         f = self.lib.apply_bcs_curvilinear_f32 if gfs.dtype == torch.float32 else self.lib.apply_bcs_curvilinear
         _lib.check(f(C.byref(self.grid.params), C.byref(self.bc), gfs.shape[0],

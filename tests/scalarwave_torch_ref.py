@@ -49,7 +49,8 @@ class TorchScalarWave:
         if gp.CoordSystem == og.CART:
             r = np.sqrt(x * x + y * y + z * z)
         else:
-            r = np.broadcast_to(og.radial(gp.CoordSystem, gp.xx[0], gp.AMPL, gp.SINHW)[0], x.shape)
+            # the Cartesian radius |r(xx0)| (r(xx0) < 0 at the inner ghost points)
+            r = np.broadcast_to(np.abs(og.radial(gp.CoordSystem, gp.xx[0], gp.AMPL, gp.SINHW)[0]), x.shape)
         self.r = torch.tensor(np.ascontiguousarray(r))
 
     def initial_data(self, A, r0, w):

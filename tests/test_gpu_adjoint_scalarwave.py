@@ -131,7 +131,8 @@ def test_gaussian_pulse_and_its_derivatives(cuda):
     y = torch.zeros_like(m.ev.y_n)
     d = [torch.zeros_like(y) for _ in range(3)]
     m.initial_data(A, r0, w, out=y, derivs=d)
-    r = og.radial(gp.CoordSystem, gp.xx[0], gp.AMPL, gp.SINHW)[0][None, None, :]
+    # the Cartesian radius: |r(xx0)| (r(xx0) < 0 at the inner ghost points)
+    r = np.abs(og.radial(gp.CoordSystem, gp.xx[0], gp.AMPL, gp.SINHW)[0])[None, None, :]
 
     def u(A, r0, w):
         return A * np.exp(-((r - r0) / w) ** 2) * np.ones(gp.shape)

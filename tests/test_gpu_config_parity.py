@@ -10,17 +10,19 @@ machine by __graft_entry__.build() from the output of oracle/gen_ref.py):
   8 planes in i2, 4 ghosts -- with its seeded Brill-Lindquist data plus a
   perturbation.
 
-Ricci_eval, the Hamiltonian constraint and the det(gammabar) rescale must
-match at 1e-12 normwise relative per gridfunction (1e-14 for the rescale),
-rhs_eval (given the reference's RbarDD) at 1e-11, with every BSSN kernel
-family.  The identical FP64 input state goes to both sides.  The rhs bound
-is the FP64 conditioning of the RHS at Brill-Lindquist data, not a kernel
-property: on the same kind of input (a 64 x 64 x 8 slab at this grid
-spacing) the numpy oracle, an independent FP64 evaluation, differs from the
-reference's C by up to 3e-12 per gridfunction in aDD_ii and trK (1.4e-12
-over the whole RHS), and the GPU's point, staged and fused kernels show the
-same figures as each other (5e-12 on this slab, 1.5e-12 on the headline
-grid).
+Ricci_eval must match at 1e-12 normwise relative per gridfunction and the
+det(gammabar) rescale at 1e-14; rhs_eval (given the reference's RbarDD) and
+the Hamiltonian constraint at 1e-11; with every BSSN kernel family.  The
+identical FP64 input state goes to both sides.  The 1e-11 bounds are the
+FP64 conditioning of these sums of large cancelling terms at
+Brill-Lindquist data, not a kernel property: on the same kind of input the
+numpy oracle, an independent FP64 evaluation, differs from the reference's
+C by up to 3e-12 per gridfunction in the RHS (aDD_ii and trK; a 64 x 64 x 8
+Cartesian FD6 slab at this grid spacing) and by 5.4e-12 (64 x 64 x 8
+Cartesian FD6) and 1.3e-12 (64 x 32 x 16 SinhSpherical FD4) in H; the GPU's
+point, staged and fused kernels show the same figures as each other (RHS
+5e-12 on the 256^2 x 8 slab and 1.5e-12 on the headline grid; H 3.9e-12
+and 1.2e-12).
 """
 import numpy as np
 import pytest
@@ -67,7 +69,7 @@ def _compare(cuda, G, gp, cfg, m1, z1, m2, z2, seed):
 
     H = ev.hamiltonian(t).cpu().numpy()[0]
     r_H = rk.hamiltonian(f)
-    assert per_gf_rel(H[None, g:-g, g:-g, g:-g], r_H[None, g:-g, g:-g, g:-g]) < TOL
+    assert per_gf_rel(H[None, g:-g, g:-g, g:-g], r_H[None, g:-g, g:-g, g:-g]) < RHS_TOL
 
     t2 = t.clone()
     ev.enforce_detgammabar(t2)
