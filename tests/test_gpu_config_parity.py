@@ -10,8 +10,8 @@ machine by __graft_entry__.build() from the output of oracle/gen_ref.py):
   8 planes in i2, 4 ghosts -- with its seeded Brill-Lindquist data plus a
   perturbation.
 
-Ricci_eval must match at 1e-12 normwise relative per gridfunction and the
-det(gammabar) rescale at 1e-14; rhs_eval (given the reference's RbarDD) and
+Ricci_eval and the det(gammabar) rescale must match at 1e-12 normwise
+relative per gridfunction; rhs_eval (given the reference's RbarDD) and
 the Hamiltonian constraint at 1e-11; with every BSSN kernel family.  The
 identical FP64 input state goes to both sides.  The 1e-11 bounds are the
 FP64 conditioning of these sums of large cancelling terms at
@@ -22,7 +22,10 @@ Cartesian FD6 slab at this grid spacing) and by 5.4e-12 (64 x 64 x 8
 Cartesian FD6) and 1.3e-12 (64 x 32 x 16 SinhSpherical FD4) in H; the GPU's
 point, staged and fused kernels show the same figures as each other (RHS
 5e-12 on the 256^2 x 8 slab and 1.5e-12 on the headline grid; H 3.9e-12
-and 1.2e-12).
+and 1.2e-12).  The rescale acts on gammabar ~ 1 while hDD is ~1e-3 here,
+so FP64 rounding of gammabar is ~1e-13 relative to hDD: oracle vs the
+reference's C 4.0e-13 (Cartesian FD6 slab) and 5.0e-13 (SinhSpherical),
+GPU 5.0e-13 and 4.8e-13.
 """
 import numpy as np
 import pytest
@@ -74,7 +77,7 @@ def _compare(cuda, G, gp, cfg, m1, z1, m2, z2, seed):
     t2 = t.clone()
     ev.enforce_detgammabar(t2)
     r_enf = rk.enforce(f)
-    assert per_gf_rel(t2.cpu().numpy()[11:17], r_enf[11:17]) < 1e-14
+    assert per_gf_rel(t2.cpu().numpy()[11:17], r_enf[11:17]) < TOL
 
 
 def test_headline_grid_matches_reference_generated_c(cuda, bssn_kernels):
