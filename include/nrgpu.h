@@ -514,6 +514,39 @@ int nrgpu_batch_autotune(nrgpu_batch *batch, const void *in_gfs, void *rhs_scrat
 int nrgpu_batch_set_tile(nrgpu_batch *batch, int tx, int ty, int grid);
 int nrgpu_batch_get_tile(const nrgpu_batch *batch, int *tx, int *ty, int *grid);
 
+/* ------------------------------------------- tangent-linear BSSN (forward mode) */
+/* Derivatives of a BSSN evolution with respect to initial-data parameters
+ * by forward mode (no counterpart in the reference): a tangent state Y is
+ * (ntan + 1) consecutive FP64 state arrays of NUM_EVOL_GFS *
+ * Nxx_plus_2NGHOSTS_tot values -- the state, then its derivative along each
+ * of ntan parameters (ntan in {0, 1, 2, 4}; 0 is the plain FP64 evolution
+ * through the same code).  FD_order 4 on Cartesian and SinhSpherical(v2)
+ * grids, FP64, no source terms or dissipation.
+ *   BSSN_tangent_rhs_eval: Ricci_eval then rhs_eval of Y and their
+ *       derivatives at interior points; aux holds (ntan+1) x 6 RbarDD arrays,
+ *       rhs (ntan+1) state arrays.
+ *   BSSN_tangent_step: one RK4 step (the reference's unfused order; BCs on
+ *       the state and on every tangent, the det(gammabar) rescale and its
+ *       linearisation); scratch holds (ntan+1) x 78 x Nxx_plus_2NGHOSTS_tot
+ *       doubles.
+ *   BSSN_tangent_initial_data_BrillLindquist: the data of
+ *       BSSN_initial_data_BrillLindquist in Y[0] and, in Y[k], its
+ *       derivative with respect to parameter param_index[k-1]: 0 m1, 1 m2,
+ *       2..4 x1[0..2], 5..7 x2[0..2].
+ *   BSSN_tangent_shell_accumulate: on the shell i0 (its Nxx1*Nxx2 interior
+ *       (i1, i2) points, q = j1 + Nxx1 * j2) of gridfunction gf:
+ *       accum[0] += scale sum_q wts[q] (f_q - offset)^2 and
+ *       accum[k] += 2 scale sum_q wts[q] (f_q - offset) df_q/dp_k (device). */
+int BSSN_tangent_rhs_eval(const rfm_struct *rfmstruct, const NRGPU_PARAMSTRUCT *params, int ntan,
+                          const double *in_Y, double *aux, double *rhs_Y);
+int BSSN_tangent_step(const rfm_struct *rfmstruct, const NRGPU_PARAMSTRUCT *params, const bc_struct *bcstruct,
+                      int ntan, double *Y, double *scratch, double dt);
+int BSSN_tangent_initial_data_BrillLindquist(const NRGPU_PARAMSTRUCT *params, double m1, const double x1[3],
+                                             double m2, const double x2[3], int ntan, const int *param_index,
+                                             double *Y);
+int BSSN_tangent_shell_accumulate(const NRGPU_PARAMSTRUCT *params, int ntan, const double *Y, int gf, int i0,
+                                  const double *wts, double scale, double offset, double *accum);
+
 /* ------------------------------------------------------------ adjoint */
 /* Discrete adjoints of the linear evolutions: Maxwell System I (FP64,
  * Cartesian) and ScalarWave (FP64, Cartesian and the curvilinear families

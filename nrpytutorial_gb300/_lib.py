@@ -142,6 +142,12 @@ _PROTOS = {
     "nrgpu_bc_gather_points": (C.c_int, [P(paramstruct), C.c_int, vp, C.c_int, vp, vp]),
     "nrgpu_bc_scatter_parity": (C.c_int, [P(paramstruct), C.c_int, P(C.c_int8), vp, vp, C.c_int, vp, vp]),
     "xx_to_Cart": (C.c_int, [P(paramstruct), vp, C.c_int, C.c_int, C.c_int, P(C.c_double)]),
+    "BSSN_tangent_rhs_eval": (C.c_int, [P(rfm_struct), P(paramstruct), C.c_int, vp, vp, vp]),
+    "BSSN_tangent_step": (C.c_int, [P(rfm_struct), P(paramstruct), P(bc_struct), C.c_int, vp, vp, C.c_double]),
+    "BSSN_tangent_initial_data_BrillLindquist": (C.c_int, [P(paramstruct), C.c_double, P(C.c_double), C.c_double,
+                                                           P(C.c_double), C.c_int, P(C.c_int), vp]),
+    "BSSN_tangent_shell_accumulate": (C.c_int, [P(paramstruct), C.c_int, vp, C.c_int, C.c_int, vp, C.c_double,
+                                                C.c_double, vp]),
     "ScalarWave_rhs_eval_adjoint": (C.c_int, [P(rfm_struct), P(paramstruct), vp, vp]),
     "MoL_adjoint_step_backward": (C.c_int, [C.c_int, P(rfm_struct), P(paramstruct), P(bc_struct), vp, vp, vp,
                                             C.c_double]),

@@ -101,7 +101,7 @@ template <int CS, typename R> struct Metric {
   R Gbar[3][3][3];   // Gammabar^i_kl
 };
 
-template <int ORDER, int CS, typename R, typename PT, bool LOC>
+template <int ORDER, int CS, typename R, typename PT, int LOC>
 __device__ __forceinline__ void metric_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                              Metric<CS, R> &m) {
   using M = RfmMask<CS>;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void metric_point(const PT &P, const Rfm<CS, R, LOC> 
 }
 
 // Delta^i_jk = Gammabar - Gammahat, and Delta^i = gammabar^jk Delta^i_jk.
-template <int CS, typename R, bool LOC>
+template <int CS, typename R, int LOC>
 __device__ __forceinline__ void delta_gamma(const Metric<CS, R> &m, const Rfm<CS, R, LOC> &rf, R DG[3][3][3],
                                             R DGU[3]) {
   using M = RfmMask<CS>;
@@ -172,7 +172,7 @@ __device__ __forceinline__ void delta_gamma(const Metric<CS, R> &m, const Rfm<CS
 // ------------------------------------------------------------------ Ricci
 // Rbar_ij (BSSN_quantities.py:260-425), needs second derivatives of hDD and
 // first derivatives of lambdaU.
-template <int ORDER, int CS, typename R, typename PT, bool LOC>
+template <int ORDER, int CS, typename R, typename PT, int LOC>
 __device__ __forceinline__ void ricci_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                             const Metric<CS, R> &m, R Rbar[6]) {
   using M = RfmMask<CS>;
@@ -301,7 +301,7 @@ __device__ __forceinline__ void ricci_point(const PT &P, const Rfm<CS, R, LOC> &
 // M^i = e^{-4 phi}/ReU^i [gammabar^ik gammabar^jl Dbar_j Abar_kl
 //       + 6 Abar^ij d_j phi - 2/3 gammabar^ij d_j K]  (BSSN_constraints.py:76-126;
 // AbarDD_dD from BSSN_quantities.py:247-255; W = e^{-2 phi}).
-template <int ORDER, int CS, typename R, typename Tin, bool LOC>
+template <int ORDER, int CS, typename R, typename Tin, int LOC>
 __device__ __forceinline__ void momentum_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf, const R *inv, R MU[3]) {
   using M = RfmMask<CS>;
   Metric<CS, R> m;
@@ -373,7 +373,7 @@ __device__ __forceinline__ void momentum_point(const Point<Tin> &P, const Rfm<CS
 
 // -------------------------------------------------------------------- RHS
 // All 24 right-hand sides at one interior point, in gridfunction order.
-template <int ORDER, int CS, typename R, typename PT, bool LOC>
+template <int ORDER, int CS, typename R, typename PT, int LOC>
 __device__ __forceinline__ void rhs_point(const PT &P, const Rfm<CS, R, LOC> &rf, const R *inv,
                                           const R Rbar[6], R eta, R out[NUM_EVOL_GFS]) {
   using M = RfmMask<CS>;

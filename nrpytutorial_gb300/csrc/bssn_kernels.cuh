@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
 
 // Kreiss-Oliger dissipation of gridfunction gf at the point:
 // sum_k f_dKOD[k] ReU[k] (BaikalETK/BaikalETK_C_kernels_codegen.py:147-171).
-template <int ORDER, int CS, typename R, typename Tin, bool LOC>
+template <int ORDER, int CS, typename R, typename Tin, int LOC>
 __device__ __forceinline__ R ko_point(const Point<Tin> &P, int gf, const Rfm<CS, R, LOC> &rf, const R *inv) {
   R acc = (R)0;
 #pragma unroll
@@ -75,7 +75,7 @@ __device__ __forceinline__ R ko_point(const Point<Tin> &P, int gf, const Rfm<CS,
 //   Lambdabar source L^i = -16 pi alpha gammabar^ij S_j: lambda^i += L^i / ReU^i and,
 //   through the Gamma-driver's 3/4 d_t Lambdabar^i, B^i += (3/4) L^i / ReU^i.
 // T4: the ten T4UU gridfunctions at this point (stride ntot).
-template <int CS, typename R, typename Tin, bool LOC>
+template <int CS, typename R, typename Tin, int LOC>
 __device__ __forceinline__ void source_point(const Point<Tin> &P, const Rfm<CS, R, LOC> &rf,
                                              const R *__restrict__ T4, long long ntot, R *out) {
   using M = RfmMask<CS>;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RICCI_MIN_BLOCKS)
   if (!interior_point(g, i0, i1, i2, idx)) return;
   double q[rq::NQ];
   hatted_at_point<CS>(xa, i0, i1, i2, q);
-  const Rfm<CS, double, true> rf{q, 1};
+  const Rfm<CS, double, RFM_LOCAL> rf{q, 1};
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
   Metric<CS, double> m;
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kBlockX *kBlockY, NRGPU_BSSN_RHS_MIN_BLOCKS)
   if (!interior_point(g, i0, i1, i2, idx)) return;
   double q[rq::NQ];
   hatted_at_point<CS>(xa, i0, i1, i2, q);
-  const Rfm<CS, double, true> rf{q, 1};
+  const Rfm<CS, double, RFM_LOCAL> rf{q, 1};
   Point<double> P{in + idx, g.ntot, {1, (long long)g.n0, (long long)g.n0 * g.n1}};
   const double inv[3] = {g.invdx0, g.invdx1, g.invdx2};
   double Rbar[6];
