@@ -41,11 +41,6 @@
 #ifndef NRGPU_STAGED_EPILOGUE_UNROLL
 #define NRGPU_STAGED_EPILOGUE_UNROLL 4
 #endif
-// Phase B's reference metric from a shared-memory tile (1) or from the
-// table in global memory (0), for the RHS and fused variants.
-#ifndef NRGPU_STAGED_RFM_TILE
-#define NRGPU_STAGED_RFM_TILE 1
-#endif
 
 namespace nrgpu {
 namespace bssn {
@@ -104,24 +99,8 @@ template <typename R, typename E, int ORDER, int V> struct Tile {
   // room for two at two blocks per SM)
   static constexpr int NBUF = V == FUSED ? 2 : NRGPU_STAGED_NBUF;
   static constexpr int SLOT_OFFSET = 128 + NBUF * BOX_STRIDE;
-  static constexpr int RING_BYTES = NBUF * BOX_STRIDE;
   static_assert(TX % QX == 0, "box start must stay 16-byte aligned");
 };
-// Phase B's reference-metric tile (FP32 arithmetic on curvilinear grids):
-// the table entries of the brick's columns -- (i0, i1) for the Spherical and
-// SymTP families, (i0, i2) for the Cylindrical family -- copied into the
-// ring of boxes once phase A no longer needs it, one row per slot the family
-// can read plus a zero row.  Without it each thread reads ~100 table entries
-// from L1/L2 inside the algebra.
-template <typename R, typename E, int ORDER, int V, int CS> struct RfmTile {
-  using T = Tile<R, E, ORDER, V>;
-  static constexpr bool cyl = cylindrical_family(CS);
-  static constexpr int NCOL = T::TX * (cyl ? T::TZ : T::TY);
-  static constexpr int ROWS = rfm_used_count<CS>() + 1;
-  static constexpr bool use = NRGPU_STAGED_RFM_TILE && V != stage::RICCI && sizeof(R) == 4 &&
-                              !RfmMask<CS>::trivial && ROWS * NCOL * 4 <= T::RING_BYTES;
-};
-
 template <typename R, typename E, int ORDER, int V> constexpr int smem_bytes() {
   using T = Tile<R, E, ORDER, V>;
   return T::SLOT_OFFSET + total_slots(V) * T::NT * (int)sizeof(R);
@@ -297,8 +276,8 @@ __device__ __forceinline__ R ADV(const StagedPoint<RS, V, NT> &P, int g, const R
   return (R)P.at(stage::slot_adv(V, g));
 }
 
-// Phase B: the algebra on the staged values and the reference metric `rf`
-// (table, or the block's tile), then the variant's stores.
+// Phase B: the algebra on the staged values and the reference metric `rf`,
+// then the variant's stores.
 template <typename R, int CS, int ORDER, typename TStage, int V, int NT, typename RF>
 __device__ __forceinline__ void staged_phase_b(const StagedPoint<R, V, NT> &P, const RF &rf, const R inv[3],
                                                const R *__restrict__ aux_in, R eta, const RKEpilogue<TStage> &epi,
@@ -338,7 +317,7 @@ __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::
                                                                            Tin>::type, ORDER, V>::NT, 2)
     staged_kernel(Grid g, const __grid_constant__ CUtensorMap tmap, typename InRef<Tin>::type in,
                   const R *__restrict__ aux_in, const R *__restrict__ tab, R eta, RKEpilogue<TStage> epi,
-                  R *__restrict__ aux_out, int *status, const __grid_constant__ RfmTileMap rmap) {
+                  R *__restrict__ aux_out, int *status) {
   using E = typename std::conditional<std::is_same<Tin, Pair32>::value, float2, Tin>::type;
   using T = stage::Tile<R, E, ORDER, V>;
   constexpr int NT = T::NT, H = T::H, NSTG = stage::num_staged(V);
@@ -447,31 +426,9 @@ __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::
   }
 
   // ---- phase B
-  using RT = stage::RfmTile<R, E, ORDER, V, CS>;
-  if constexpr (RT::use) {
-    // The ring is free: every box issued was waited for.  All threads load
-    // the tile (threads past the interior's edge load the clamped columns).
-    float *tile = (float *)bufs;
-    const long long plane = (long long)g.n0 * (RT::cyl ? g.n2 : g.n1);
-    const int bB = RT::cyl ? z0 : y0, nB = RT::cyl ? nz : ny;
-#pragma unroll 4
-    for (int e = t; e < RT::ROWS * RT::NCOL; e += NT) {
-      const int u = e / RT::NCOL, c = e % RT::NCOL;
-      const int ci0 = g.ng + min(x0 + c % T::TX, nx - 1), ciB = g.ng + min(bB + c / T::TX, nB - 1);
-      const int slot = rmap.slot_of_row[u];
-      tile[e] = slot < 0 ? 0.f : (float)__ldg(tab + (long long)slot * plane + (long long)ciB * g.n0 + ci0);
-    }
-    __syncthreads();
-    if (!valid) return;
-    const int col = tx + T::TX * (RT::cyl ? tz : ty);
-    const Rfm<CS, R, RFM_TILE> rft{(const R *)(tile + col), RT::NCOL, rmap.row_of_slot};
-    staged_phase_b<R, CS, ORDER, TStage, V, NT>(StagedPoint<R, V, NT>{slots + t}, rft, inv, aux_in, eta, epi,
-                                                aux_out, g, idx);
-  } else {
-    if (!valid) return;
-    staged_phase_b<R, CS, ORDER, TStage, V, NT>(StagedPoint<R, V, NT>{slots + t}, rf, inv, aux_in, eta, epi,
-                                                aux_out, g, idx);
-  }
+  if (!valid) return;
+  staged_phase_b<R, CS, ORDER, TStage, V, NT>(StagedPoint<R, V, NT>{slots + t}, rf, inv, aux_in, eta, epi, aux_out,
+                                              g, idx);
 }
 
 // ---------------------------------------------------------------- launchers
@@ -503,9 +460,8 @@ int staged_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, c
   }
   const int nx = g.n0 - 2 * g.ng, ny = g.n1 - 2 * g.ng, nz = g.n2 - 2 * g.ng;
   const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY, (nz + T::TZ - 1) / T::TZ);
-  static const RfmTileMap rmap = rfm_tile_map<CS>();
   kern<<<grid, T::NT, smem, stream()>>>(g, map, (typename InRef<Tin>::type)in, aux_in, table_of<R>(rfm), eta, epi,
-                                        aux_out, status, rmap);
+                                        aux_out, status);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }

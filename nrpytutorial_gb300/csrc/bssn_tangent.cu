@@ -117,7 +117,12 @@ __global__ void enforce_tangent_kernel(Grid g, const double *__restrict__ tab, i
   const double det = gb[0][0] * C[0][0] + gb[0][1] * C[0][1] + gb[0][2] * C[0][2];
   const double adg = fabs(rf.detg());
   const double s = det / adg;
-  const double f = pow(s, -1.0 / 3.0);
+  // f = s^{-1/3} as the value's rescale computes it (enforce_kernel: Newton
+  // on w^{-3} = s from the FP32 reciprocal cube root), so that the tangent is
+  // the derivative of that map at every point, ghost points included.
+  double f = (double)rcbrtf((float)s);
+#pragma unroll
+  for (int it = 0; it < 2; it++) f = f * (4.0 - s * f * f * f) * (1.0 / 3.0);
   for (int k = 1; k <= ntan; k++) {
     double *t = Y + k * ts;
     double dh[3][3], ddet = 0.0;

@@ -96,21 +96,15 @@ template <int CS> struct RfmMask {
 // MODE RFM_TABLE: base = table + iB*N0 + i0, plane = N0*NB.
 // MODE RFM_LOCAL: base points at this thread's own NQ values (plane 1),
 //   computed from the caller's coordinates instead of read from the table.
-// MODE RFM_TILE: base = a block's shared-memory copy of the table entries its
-//   columns use + this thread's column, plane = the tile's row length, and
-//   map[slot] = the tile row of each slot (rows of slots a coordinate family
-//   never reads hold zeros).
-enum RfmMode { RFM_TABLE = 0, RFM_LOCAL = 1, RFM_TILE = 2 };
+enum RfmMode { RFM_TABLE = 0, RFM_LOCAL = 1 };
 
 template <int CS, typename R, int MODE = RFM_TABLE> struct Rfm {
   using M = RfmMask<CS>;
   const R *__restrict__ base;
   long long plane;
-  const short *map = nullptr;
 
   __device__ __forceinline__ R q(int slot) const {
     if constexpr (MODE == RFM_LOCAL) return base[slot];
-    else if constexpr (MODE == RFM_TILE) return base[map[slot] * plane];
     else return __ldg(base + slot * plane);
   }
 
@@ -151,76 +145,6 @@ template <int CS, typename R, int MODE = RFM_TABLE> struct Rfm {
   __device__ __forceinline__ R detgdD(int k) const { return q(rq::detgammahatdD + k); }
   __device__ __forceinline__ R detgdDD(int k, int l) const { return q(rq::detgammahatdDD + 3 * k + l); }
 };
-
-// Can table slot s be non-zero for coordinate family CS (the masks above,
-// slot by slot in the rq layout)?  Kernels read only such slots.
-template <int CS> __host__ __device__ constexpr bool rfm_slot_used(int s) {
-  using M = RfmMask<CS>;
-  if (M::trivial) return false;
-  if (s < rq::ReUdD) return true;
-  if (s < rq::ReUdDD) return M::ReUdD((s - rq::ReUdD) / 3, (s - rq::ReUdD) % 3);
-  if (s < rq::ReDD) {
-    const int r = s - rq::ReUdDD;
-    return M::ReUdDD(r / 9, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::ReDDdD) return true;
-  if (s < rq::ReDDdDD) {
-    const int r = s - rq::ReDDdD;
-    return M::ReDDdD(r / 9, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::ghatDD) {
-    const int r = s - rq::ReDDdDD;
-    return M::ReDDdDD(r / 27, (r / 9) % 3, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::ghatUU) return (s - rq::ghatDD) % 4 == 0;
-  if (s < rq::ghatDDdD) return (s - rq::ghatUU) % 4 == 0;
-  if (s < rq::ghatDDdDD) {
-    const int r = s - rq::ghatDDdD;
-    return M::ghatDDdD(r / 9, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::GammahatUDD) {
-    const int r = s - rq::ghatDDdDD;
-    return M::ghatDDdDD(r / 27, (r / 9) % 3, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::GammahatUDDdD) {
-    const int r = s - rq::GammahatUDD;
-    return M::Gammahat(r / 9, (r / 3) % 3, r % 3);
-  }
-  if (s < rq::detgammahat) {
-    const int r = s - rq::GammahatUDDdD;
-    return M::GammahatdD(r / 27, (r / 9) % 3, (r / 3) % 3, r % 3);
-  }
-  if (s == rq::detgammahat) return true;
-  if (s < rq::detgammahatdDD) return M::detgdD(s - rq::detgammahatdD);
-  if (s < rq::NQ) return M::detgdDD((s - rq::detgammahatdDD) / 3, (s - rq::detgammahatdDD) % 3);
-  return false;
-}
-template <int CS> __host__ __device__ constexpr int rfm_used_count() {
-  int n = 0;
-  for (int s = 0; s < rq::NQ; s++) n += rfm_slot_used<CS>(s) ? 1 : 0;
-  return n;
-}
-
-// A block's tile of table entries (RFM_TILE): the host-side map from slot to
-// tile row (unused slots -> the last row, all zeros) and from row to slot
-// (-1 for the zero row).  Passed to kernels as a __grid_constant__
-// parameter, so map[slot] with a constant slot is a constant-bank operand.
-struct RfmTileMap {
-  short row_of_slot[rq::NQ];
-  short slot_of_row[rq::NQ + 1];
-  int rows;
-};
-template <int CS> inline RfmTileMap rfm_tile_map() {
-  RfmTileMap m{};
-  int n = 0;
-  for (int s = 0; s < rq::NQ; s++)
-    if (rfm_slot_used<CS>(s)) m.slot_of_row[n++] = (short)s;
-  m.slot_of_row[n] = -1;
-  for (int s = 0; s < rq::NQ; s++) m.row_of_slot[s] = (short)n;
-  for (int r = 0; r < n; r++) m.row_of_slot[m.slot_of_row[r]] = (short)r;
-  m.rows = n + 1;
-  return m;
-}
 
 // Extent of the table's second coordinate, and whether tables fit a grid.
 inline int rfm_second_extent(const paramstruct *p) {
