@@ -41,19 +41,19 @@ W = dict(name="BSSN SinhSpherical 128x64x16 FD4 RK4 Brill-Lindquist", coord="Sin
 METRIC = "BSSN gridpoint-RHS/s (RK4 step), mixed precision at stated error vs FP64"
 KO_STRENGTH = 0.1  # Kreiss-Oliger strength of the dissipated runs (BaikalETK's default_KO_strength)
 UNIT = "gridpoint-RHS/s"
-# Algorithmic bytes per interior point of the BSSN rhs kernel in a fused RK4
-# substep 1 (stage input read, RbarDD read, y_n read, running total read and
-# written, stage output written; 24 gfs):
-#   compensated: 24 x 8 (pairs) + 6 x 4 + 24 x 8 + 24 x 16 + 24 x 8 = 984 B
-#   FP64:        24 x 8 + 6 x 8 + 24 x 8 + 24 x 16 + 24 x 8 = 1008 B
-RHS_BYTES_COMP = 24 * 8 + 6 * 4 + 24 * 8 + 24 * 16 + 24 * 8
-# DRAM bytes (read + write) of that launch, L2 flushed before it as in the
-# timing: one ncu capture of the launches inside the "roofline_rhs" range
-# (profiles/bssn_rhs_staged_compensated_roofline_traffic.md), mean of two
-# launches of the staged RHS kernel: 101.2 MB read + 21.4 MB written, 0.95x
-# the 129.0 MB algorithmic (the running-total and stage stores that are still
-# in L2 when the launch ends are written back later).
-RHS_TRAFFIC_COMP = 122.6e6
+# Algorithmic bytes per interior point of the step's dominant kernel, the
+# fused staged BSSN kernel (Ricci computed in the block, then the RHSs and
+# the RK4 update of substep 1): stage input read, y_n read, running total
+# read and written, stage output written; 24 gfs, compensated pairs:
+#   24 x 8 + 24 x 8 + 24 x 16 + 24 x 8 = 960 B
+# and of the separate RHS kernel (which also reads RbarDD, 6 x 4 B): 984 B.
+STEP_BYTES_COMP = 24 * 8 + 24 * 8 + 24 * 16 + 24 * 8
+RHS_BYTES_COMP = STEP_BYTES_COMP + 6 * 4
+# DRAM bytes (read + write) of the roofline launch, L2 flushed before it as
+# in the timing: one ncu capture of the launches inside the "roofline_rhs"
+# range, mean of two launches of the fused staged kernel (None until
+# captured for this kernel).
+STEP_TRAFFIC_COMP = None
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 
@@ -316,8 +316,9 @@ def run_gpu(args):
     evc.y_n.copy_(y0)
     evc.step(dt)
     t_ric_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 1))
-    torch.cuda.nvtx.range_push("roofline_rhs")  # the launches the roofline's traffic capture selects
     t_rhs_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 2))
+    torch.cuda.nvtx.range_push("roofline_rhs")  # the launches the roofline's traffic capture selects
+    t_step_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 0))  # the step's own kernel: fused Ricci + RHS
     torch.cuda.nvtx.range_pop()
     ev.y_n.copy_(y0)
     ev.step(dt)
@@ -354,7 +355,7 @@ def run_gpu(args):
     clocks = sampler.stop()
 
     hbm, src = peaks()
-    achieved = nint * RHS_BYTES_COMP / t_rhs_c / 1e9
+    achieved = nint * STEP_BYTES_COMP / t_step_c / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
         "ms_per_step": tc / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -384,16 +385,16 @@ def run_gpu(args):
         "e2e": {"value": world * K * nint * 4 / te2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
                 "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call"},
-        "roofline": {"bound": "hbm", "kernel": "bssn staged_kernel (RHS variant), compensated (FP32 pairs "
-                                               "in/out, fused RK4 substep 1)",
+        "roofline": {"bound": "hbm", "kernel": "bssn staged_kernel (FUSED variant: Ricci in the block, then the "
+                                               "RHSs and the RK4 update of substep 1), compensated FP32 pairs",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": RHS_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
-                     "bytes_per_point": RHS_BYTES_COMP,
-                     "launch_ms": t_rhs_c * 1e3,
-                     "note": "the staged kernel (TMA-staged shared-memory finite differences, 236 registers, no "
-                             "spills, 8 warps per SM) is issue/latency bound by the BSSN algebra, not by HBM; "
-                             "HBM fraction reported as asked"},
-        "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3},
+                     "peak_source": src, "traffic": STEP_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
+                     "bytes_per_point": STEP_BYTES_COMP,
+                     "launch_ms": t_step_c * 1e3,
+                     "note": "the step's dominant kernel (TMA-staged shared-memory finite differences, 8 warps "
+                             "per SM) is issue/latency bound by the BSSN algebra, not by HBM; HBM fraction "
+                             "reported as asked"},
+        "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3, "fused_ricci_rhs": t_step_c * 1e3},
                        "fp64": {"ricci": t_ric_64 * 1e3, "rhs": t_rhs_64 * 1e3}},
         "fp64": {"value": world * K * nint * 4 / t64, "unit": UNIT, "ms_per_step": t64 / K * 1e3,
                  "launches_per_step": lps64, "H_l2": H64,

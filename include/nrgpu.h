@@ -224,10 +224,13 @@ int         nrgpu_device_status(int clear);
  *           differences evaluated there, then the algebra;
  *   FUSED:  STAGED with Ricci computed inside the RHS kernel of a MoL step
  *           (auxevol is neither written nor read by the step);
- *   AUTO:   STAGED for FP32 arithmetic (mixed and compensated precision)
- *           where the grid allows it (NGHOSTS = FD_order/2 + 1, 16-byte-
- *           aligned stage arrays and rows), POINT otherwise and for FP64 --
- *           the faster of the two on GB300 in each case.
+ *   AUTO:   per grid and precision, the family measured fastest for a
+ *           whole step on GB300: FP64 and Cartesian grids POINT; curvilinear
+ *           grids with FP32 pair stages (the compensated modes) FUSED, SymTP
+ *           family STAGED; curvilinear grids with plain FP32 stages STAGED.
+ *           A grid the staged kernels cannot take (NGHOSTS other than
+ *           FD_order/2 + 1, stage arrays or rows not 16-byte aligned) runs
+ *           POINT.
  * Kreiss-Oliger dissipation, T^{mu nu} sources, the no-precompute _xx
  * functions and FP32 arithmetic on FP64 input always run on POINT.
  * Process-wide setting. */

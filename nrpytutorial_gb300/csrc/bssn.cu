@@ -27,14 +27,24 @@ NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 
 // Which BSSN Ricci/RHS kernels run (nrgpu_set_bssn_kernels).
 static int g_kernels = NRGPU_BSSN_KERNELS_AUTO;
-// AUTO takes the staged kernels for FP32 arithmetic and the point kernels
-// for FP64, whichever measured faster on GB300 at the headline grid (the
-// FP64 kernels are FP64-pipe bound; the staged FP64 form's slot arrays halve
-// its occupancy).
-static bool staged_for(int prec) {
-  return g_kernels == NRGPU_BSSN_KERNELS_STAGED || g_kernels == NRGPU_BSSN_KERNELS_FUSED ||
-         (g_kernels == NRGPU_BSSN_KERNELS_AUTO && prec != NRGPU_PREC_FP64);
+// The family a grid and precision run on.  AUTO: the fastest whole step
+// measured on GB300 (128^3 Cartesian FD2/4/6 and 128x64x16-class curvilinear
+// grids, every family): FP64 is FP64-pipe bound and the point kernels keep
+// their occupancy; on Cartesian grids the point kernels' stencil loads hit
+// L1 and the staged bricks' halos cost more than they save (FD6: 13.5 vs
+// 16.9 ms per 128^3 compensated step); on curvilinear grids with FP32 pair
+// stages the fused staged kernel saves the RbarDD round trip and the Ricci
+// launch (headline grid 1.02 vs 1.05 ms), except the SymTP family, whose
+// larger Christoffel tables favour the separate staged kernels; plain FP32
+// stages measure the same in every family (staged).
+static int family(const paramstruct *p, int prec) {
+  if (g_kernels != NRGPU_BSSN_KERNELS_AUTO) return g_kernels;
+  const int cs = dispatch_cs(p->CoordSystem);
+  if (prec == NRGPU_PREC_FP64 || cs == NRGPU_COORD_CARTESIAN) return NRGPU_BSSN_KERNELS_POINT;
+  if (pair_precision(prec)) return cs == NRGPU_COORD_SINHSYMTP ? NRGPU_BSSN_KERNELS_STAGED : NRGPU_BSSN_KERNELS_FUSED;
+  return NRGPU_BSSN_KERNELS_STAGED;
 }
+static bool staged_for(const paramstruct *p, int prec) { return family(p, prec) != NRGPU_BSSN_KERNELS_POINT; }
 
 #define NRGPU_BSSN_SWITCH(CALL)                                                               \
   switch (dispatch_cs(p->CoordSystem) * 16 + p->FD_order) {                                   \
@@ -463,7 +473,7 @@ int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *i
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(in && auxevol, "NULL gridfunctions");
-  if (staged_for(prec)) {
+  if (staged_for(p, prec)) {
     st = staged_ricci(rfm, p, in, in_is_f64, prec, auxevol);
     if (st != NRGPU_ERR_UNSUPPORTED) return st;
   }
@@ -483,7 +493,7 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
   if (st) return st;
   NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
   // Kreiss-Oliger dissipation and T^{mu nu} sources run on the point kernels.
-  if (staged_for(a.prec) && !extras_on(p)) {
+  if (staged_for(p, a.prec) && !extras_on(p)) {
     st = staged_rhs(rfm, p, a, false);
     if (st != NRGPU_ERR_UNSUPPORTED) return st;
   }
@@ -495,7 +505,7 @@ int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
-  if (g_kernels == NRGPU_BSSN_KERNELS_FUSED && !extras_on(p)) {
+  if (family(p, a.prec) == NRGPU_BSSN_KERNELS_FUSED && !extras_on(p)) {
     st = staged_rhs(rfm, p, a, true);
     if (st != NRGPU_ERR_UNSUPPORTED) return st;
   }
