@@ -51,9 +51,10 @@ STEP_BYTES_COMP = 24 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_COMP = STEP_BYTES_COMP + 6 * 4
 # DRAM bytes (read + write) of the roofline launch, L2 flushed before it as
 # in the timing: one ncu capture of the launches inside the "roofline_rhs"
-# range, mean of two launches of the fused staged kernel (None until
-# captured for this kernel).
-STEP_TRAFFIC_COMP = None
+# range (profiles/bssn_staged_fused_compensated_roofline_traffic.md), mean of
+# two launches of the fused staged kernel: 100.58 MB read + 27.88 MB
+# written, 1.02x the 125.8 MB algorithmic.
+STEP_TRAFFIC_COMP = 128.46e6
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 
