@@ -432,6 +432,8 @@ def run_gpu(args):
         out["adjoint_scalarwave_sinhsph"] = run_scalarwave_adjoint(dev, args.sw_adjoint_steps)
     if args.bl_gradient_steps > 0:
         out["gradient_bssn_brill_lindquist"] = run_bl_gradient(dev, args.bl_gradient_steps)
+    if not args.profile_sizes and world == 1:
+        out["slab_two_ranks_one_gpu"] = run_slab_local(dev)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -814,6 +816,49 @@ def run_bl_gradient(dev, K, Nxx=(64, 32, 8)):
             "J": J, "J_plain": J0, "grad": [float(v) for v in g], "grad_central_fd_h1e-6": [float(v) for v in fd],
             "grad_rel_err_vs_fd": rel, "forward_s": t_fwd, "tangent_pass_s": t_tan,
             "gradient_over_forward": t_tan / t_fwd}
+
+
+
+def run_slab_local(dev, K=5):
+    """The slab decomposition's own cost on one GPU: the headline grid's FP64
+    BSSN step split into two i2 slabs driven in this process (LocalComm:
+    per substep both ranks' kernels, the cross-rank parity gathers and the
+    halo exchange, all on this GPU), against the one-grid step; bit-for-bit
+    agreement checked.  On two GPUs the ranks' kernels would run
+    concurrently; here they run one after the other, so the difference of the
+    two times is the exchange overhead."""
+    import torch
+    from nrpytutorial_gb300 import Evolution, Grid
+    from nrpytutorial_gb300.slab import LocalComm, SlabEvolution
+    G = Grid(W["coord"], W["Nxx"], FD_order=W["fd"], NGHOSTS=W["ng"], AMPL=W["AMPL"], SINHW=W["SINHW"],
+             eta=W["eta"])
+    ev = Evolution("BSSN", G, precision="fp64", device=dev)
+    ev.initial_data_brill_lindquist(W["m1"], W["pos1"], W["m2"], W["pos2"])
+    ev.apply_bcs(ev.y_n)
+    ev.enforce_detgammabar(ev.y_n)
+    sl = SlabEvolution("BSSN", G, LocalComm(2), device=dev)
+    sl.set_state(ev.y_n)
+    dt = G.find_timestep(0.5)
+    ev.step(dt)
+    sl.step(dt)  # warm-up
+
+    def timed(f):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(K):
+            f()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / K
+
+    t1 = timed(lambda: ev.step(dt))
+    t2 = timed(lambda: sl.step(dt))
+    parts = sorted(sl.owned_state(r) for r in range(2))
+    same = bool(torch.equal(torch.cat([p for _, p in parts], dim=1), ev.y_n))
+    return {"workload": "BSSN headline grid FP64, split into 2 slabs of 8 i2 planes on one GPU (LocalComm)",
+            "one_grid_ms_per_step": t1, "two_slabs_ms_per_step": t2, "exchange_overhead_ms": t2 - t1,
+            "bit_identical_to_one_grid": same}
 
 
 # ------------------------------------------------------------ CPU reference
