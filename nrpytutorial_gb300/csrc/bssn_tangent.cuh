@@ -141,9 +141,13 @@ template <> struct Types<0> {
   static __device__ __forceinline__ void store(double *p, long long, double v) { p[0] = v; }
 };
 
+// Both kernels declare a minimum of one block per SM: without it ptxas keeps
+// the dual-number kernels at 32 registers and spills their whole state
+// (38 KB of stack per thread for 4 tangents, against 12 KB at 255 registers).
+
 // RbarDD (value and tangents) at interior points: aux at stride ats.
 template <int CS, int ORDER, int N>
-__global__ void __launch_bounds__(128) ricci_kernel(Grid g, const double *__restrict__ in, long long ts,
+__global__ void __launch_bounds__(128, 1) ricci_kernel(Grid g, const double *__restrict__ in, long long ts,
                                                     const double *__restrict__ tab, double *__restrict__ aux,
                                                     long long ats) {
   using TY = Types<N>;
@@ -164,7 +168,7 @@ __global__ void __launch_bounds__(128) ricci_kernel(Grid g, const double *__rest
 
 // The 24 RHSs (value and tangents) at interior points into out (stride ts).
 template <int CS, int ORDER, int N>
-__global__ void __launch_bounds__(128) rhs_kernel(Grid g, const double *__restrict__ in, long long ts,
+__global__ void __launch_bounds__(128, 1) rhs_kernel(Grid g, const double *__restrict__ in, long long ts,
                                                   const double *__restrict__ aux, long long ats,
                                                   const double *__restrict__ tab, double eta,
                                                   double *__restrict__ out) {

@@ -245,6 +245,14 @@ class SlabStepper:
         self.plans = plans  # {rank: SlabPlan}
         self.comm = comm
         self.ops = ops
+        self._bufs = {}  # exchange buffers, allocated once per (rank, layer, peer)
+
+    def _buffer(self, key, r, n):
+        b = self._bufs.get(key)
+        if b is None or b.numel() != n:
+            b = self.ops.new_buffer(r, n)
+            self._bufs[key] = b
+        return b
 
     def step(self, dt):
         for s in range(4):
@@ -266,14 +274,14 @@ class SlabStepper:
             for r in comm.ranks:
                 pl = self.plans[r]
                 counts = pl.inner_counts[k]
-                recv[r] = ops.new_buffer(r, sum(counts) * ngf)
+                recv[r] = self._buffer(("recv", r, k), r, sum(counts) * ngf)
                 offs = np.concatenate([[0], np.cumsum(counts)]) * ngf
                 sends[r] = {}
                 for q, idx in pl.inner_send[k].items():
                     if q == r:  # local sources straight into this rank's receive buffer
                         ops.gather(r, s, k, q, recv[r][offs[r]:offs[r + 1]])
                     else:
-                        buf = ops.new_buffer(r, len(idx) * ngf)
+                        buf = self._buffer(("send", r, k, q), r, len(idx) * ngf)
                         ops.gather(r, s, k, q, buf)
                         sends[r][q] = buf
                 specs[r] = {q: (counts[q] * ngf, recv[r].dtype, recv[r].device) for q in range(comm.world)
