@@ -179,3 +179,18 @@ def test_gloo_slab_evolution_matches_the_one_grid_oracle(case, world):
         s, n = res[r][2]
         assert n == interior.size
         assert abs(s - float((interior ** 2).sum())) <= 1e-13 * s
+
+
+def test_grid_slab_is_the_window_of_the_grid():
+    from nrpytutorial_gb300 import Grid
+    G = Grid("SinhSpherical", (10, 6, 12), FD_order=4, NGHOSTS=3, AMPL=5.0, SINHW=0.3)
+    s = G.slab(4, 13)  # planes 4..12: 3 interior planes' worth of halo on each side + 3 owned
+    p, q = G.params, s.params
+    assert q.Nxx2 == 3 and q.Nxx_plus_2NGHOSTS2 == 9 and s.shape == (9, G.shape[1], G.shape[2])
+    assert q.dxx2 == p.dxx2 and q.Nxx0 == p.Nxx0 and q.Nxx1 == p.Nxx1
+    # the slab's cell-centred xx2 are the grid's planes 4..12
+    xx2 = q.xxmin2 + (np.arange(9) - 3 + 0.5) * q.dxx2
+    assert np.allclose(xx2, np.asarray(G.xx[2])[4:13], rtol=0, atol=1e-14)
+    assert np.array_equal(s.xx[2], np.asarray(G.xx[2])[4:13])
+    with pytest.raises(ValueError):
+        G.slab(0, 6)  # no interior plane
