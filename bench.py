@@ -856,9 +856,15 @@ def run_slab_local(dev, K=5):
     t2 = timed(lambda: sl.step(dt))
     parts = sorted(sl.owned_state(r) for r in range(2))
     same = bool(torch.equal(torch.cat([p for _, p in parts], dim=1), ev.y_n))
+    # the same steps replayed from CUDA graphs: launch and host costs out
+    g1 = ev.capture(dt, 1)
+    g2 = sl.capture(dt, 1)
+    t1g = timed(g1)
+    t2g = timed(g2)
     return {"workload": "BSSN headline grid FP64, split into 2 slabs of 8 i2 planes on one GPU (LocalComm)",
             "one_grid_ms_per_step": t1, "two_slabs_ms_per_step": t2, "exchange_overhead_ms": t2 - t1,
-            "bit_identical_to_one_grid": same}
+            "graph_one_grid_ms_per_step": t1g, "graph_two_slabs_ms_per_step": t2g,
+            "graph_exchange_overhead_ms": t2g - t1g, "bit_identical_to_one_grid": same}
 
 
 # ------------------------------------------------------------ CPU reference

@@ -444,6 +444,34 @@ class SlabEvolution:
     def step(self, dt):
         self.stepper.step(dt)
 
+    def capture(self, dt, n_steps=1):
+        """Captures n_steps slab steps of every local rank into one CUDA graph
+        and returns a callable that replays them (LocalComm only: its
+        exchanges are device copies on the capturing stream; NCCL exchanges
+        between processes are not captured here).  The first step runs once
+        outside the graph and is undone."""
+        if not isinstance(self.comm, LocalComm):
+            raise ValueError("capture needs the in-process communicator (LocalComm)")
+        g = torch.cuda.CUDAGraph()
+        snap = {r: ev.y_n.clone() for r, ev in self.ops.ev.items()}
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.step(dt)  # warm-up: module load, exchange buffers
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        with torch.cuda.graph(g):
+            for _ in range(n_steps):
+                self.step(dt)
+        for r, ev in self.ops.ev.items():
+            ev.y_n.copy_(snap[r])
+        for ev in self.ops.ev.values():
+            ev._sync_stream()
+
+        def replay():
+            g.replay()
+        replay.graph = g
+        return replay
+
     def l2_norm(self, gf=0):
         """RMS over the whole grid's interior points of gridfunction gf of
         y_n: the ranks' sums of squares and point counts, all-reduced."""

@@ -76,3 +76,22 @@ def test_slab_rank_has_no_full_grid_step(cuda):
     sl = SlabEvolution("ScalarWave", G, LocalComm(2), device=cuda)
     with pytest.raises(RuntimeError):
         sl.local(0).step(0.01)
+
+
+def test_slab_step_graph_replay_equals_the_eager_step(cuda):
+    import torch
+    from nrpytutorial_gb300.slab import LocalComm, SlabEvolution
+    G, gp = grids("ScalarWave", "SinhSpherical", (12, 8, 12), 4, ng=3, AMPL=5.0, SINHW=0.3)
+    y = torch.tensor(smooth_state(2, gp, seed=3, amp=0.1), device=cuda)
+    a = SlabEvolution("ScalarWave", G, LocalComm(3), device=cuda)
+    b = SlabEvolution("ScalarWave", G, LocalComm(3), device=cuda)
+    a.set_state(y)
+    b.set_state(y)
+    dt = G.find_timestep(0.5)
+    replay = b.capture(dt, 2)
+    for _ in range(2):
+        a.step(dt)
+    replay()
+    torch.cuda.synchronize()
+    for r in range(3):
+        assert torch.equal(a.owned_state(r)[1], b.owned_state(r)[1])
