@@ -42,19 +42,20 @@ METRIC = "BSSN gridpoint-RHS/s (RK4 step), mixed precision at stated error vs FP
 KO_STRENGTH = 0.1  # Kreiss-Oliger strength of the dissipated runs (BaikalETK's default_KO_strength)
 UNIT = "gridpoint-RHS/s"
 # Algorithmic bytes per interior point of the step's dominant kernel, the
-# fused staged BSSN kernel (Ricci computed in the block, then the RHSs and
-# the RK4 update of substep 1): stage input read, y_n read, running total
-# read and written, stage output written; 24 gfs, compensated pairs:
-#   24 x 8 + 24 x 8 + 24 x 16 + 24 x 8 = 960 B
-# and of the separate RHS kernel (which also reads RbarDD, 6 x 4 B): 984 B.
-STEP_BYTES_COMP = 24 * 8 + 24 * 8 + 24 * 16 + 24 * 8
-RHS_BYTES_COMP = STEP_BYTES_COMP + 6 * 4
-# DRAM bytes (read + write) of the roofline launch, L2 flushed before it as
-# in the timing: one ncu capture of the launches inside the "roofline_rhs"
-# range (profiles/bssn_staged_fused_compensated_roofline_traffic.md), mean of
-# two launches of the fused staged kernel: 100.58 MB read + 27.88 MB
-# written, 1.02x the 125.8 MB algorithmic.
-STEP_TRAFFIC_COMP = 128.46e6
+# fused staged BSSN kernel of substep 1 (Ricci computed in the block, then
+# the RHSs, k stored for the separate RK update kernel): stage input read
+# and k written, 24 gfs as compensated FP32 pairs: 24 x 8 + 24 x 8 = 384 B.
+DOM_BYTES_COMP = 24 * 8 + 24 * 8
+# and of the step's RK update kernel (substep 1): k, y_n and running total
+# read, running total and stage value written: 24 x 5 x 8 = 960 B.
+UPDATE_BYTES_COMP = 24 * 5 * 8
+# DRAM bytes (read + write) per launch of the two, L2 flushed before each
+# launch as in the timing: one ncu capture of the launches inside the
+# "roofline_rhs" and "roofline_update" ranges
+# (profiles/bssn_split_step_compensated_roofline_traffic.md), means over the
+# captured launches.
+DOM_TRAFFIC_COMP = 45.13e6  # 42.90 MB read + 2.23 MB written
+UPDATE_TRAFFIC_COMP = None
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 
@@ -318,8 +319,13 @@ def run_gpu(args):
     evc.step(dt)
     t_ric_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 1))
     t_rhs_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 2))
-    torch.cuda.nvtx.range_push("roofline_rhs")  # the launches the roofline's traffic capture selects
-    t_step_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 0))  # the step's own kernel: fused Ricci + RHS
+    # the launches the roofline's traffic capture selects: the step's fused
+    # Ricci + RHS kernel storing k, and its RK update kernel
+    torch.cuda.nvtx.range_push("roofline_rhs")
+    t_step_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 3))
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_push("roofline_update")
+    t_upd_c = kernel_time(lambda: evc.substep_rhs(dt, 1, 4))
     torch.cuda.nvtx.range_pop()
     ev.y_n.copy_(y0)
     ev.step(dt)
@@ -356,7 +362,8 @@ def run_gpu(args):
     clocks = sampler.stop()
 
     hbm, src = peaks()
-    achieved = nint * STEP_BYTES_COMP / t_step_c / 1e9
+    achieved = nint * DOM_BYTES_COMP / t_step_c / 1e9
+    achieved_upd = nint * UPDATE_BYTES_COMP / t_upd_c / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
         "ms_per_step": tc / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -387,15 +394,21 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
                 "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call"},
         "roofline": {"bound": "hbm", "kernel": "bssn staged_kernel (FUSED variant: Ricci in the block, then the "
-                                               "RHSs and the RK4 update of substep 1), compensated FP32 pairs",
+                                               "RHSs, k stored) of substep 1, compensated FP32 pairs",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": STEP_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
-                     "bytes_per_point": STEP_BYTES_COMP,
+                     "peak_source": src, "traffic": DOM_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
+                     "bytes_per_point": DOM_BYTES_COMP,
                      "launch_ms": t_step_c * 1e3,
                      "note": "the step's dominant kernel (TMA-staged shared-memory finite differences, 8 warps "
                              "per SM) is issue/latency bound by the BSSN algebra, not by HBM; HBM fraction "
-                             "reported as asked"},
-        "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3, "fused_ricci_rhs": t_step_c * 1e3},
+                             "reported as asked. The RK update runs in the separate kernel of roofline_update"},
+        "roofline_update": {"bound": "hbm", "kernel": "rk4_update_interior_kernel<float2, 1> (float-float RK4 "
+                                                      "update of substep 1 at the interior points)",
+                            "achieved": achieved_upd, "peak": hbm, "unit": "GB/s", "frac": achieved_upd / hbm,
+                            "peak_source": src, "traffic": UPDATE_TRAFFIC_COMP, "traffic_unit": "bytes per launch",
+                            "bytes_per_point": UPDATE_BYTES_COMP, "launch_ms": t_upd_c * 1e3},
+        "kernels_ms": {"compensated": {"ricci": t_ric_c * 1e3, "rhs": t_rhs_c * 1e3, "fused_ricci_rhs": t_step_c * 1e3,
+                                       "rk_update": t_upd_c * 1e3},
                        "fp64": {"ricci": t_ric_64 * 1e3, "rhs": t_rhs_64 * 1e3}},
         "fp64": {"value": world * K * nint * 4 / t64, "unit": UNIT, "ms_per_step": t64 / K * 1e3,
                  "launches_per_step": lps64, "H_l2": H64,

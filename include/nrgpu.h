@@ -441,21 +441,27 @@ int BSSN_initial_data_BrillLindquist(const NRGPU_PARAMSTRUCT *params,
 /* One RK4 step of MoLtimestepping/RK_MoL.h for RK_method "RK4"
  * (C_Code_Generation.py:266-329, Butcher table RK_Butcher_Table_Dictionary.py:86-91):
  * four substeps of RHS -> RK update -> apply_bcs_curvilinear ->
- * (BSSN only) enforce_detgammabar_constraint.  The RK update is fused into
- * the RHS kernel's epilogue at interior points; ghost points are set by the
- * boundary conditions, as in the reference where every ghost point is a
- * boundary point.  rfm may be NULL for Cartesian grids. */
+ * (BSSN only) enforce_detgammabar_constraint.  The RK update runs at the
+ * interior points, fused into the RHS kernel's epilogue or, for BSSN's
+ * staged kernels with FP32 stages and the float-float update
+ * (NRGPU_PREC_COMPENSATED, NRGPU_PREC_MIXED), as a separate interior kernel
+ * after the RHS kernel stored k (same arithmetic, same bits); ghost points
+ * are set by the boundary conditions, as in the reference where every ghost
+ * point is a boundary point.  rfm may be NULL for Cartesian grids. */
 int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                              const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* The same step, unfused, exactly in the reference's order: separate RHS
  * kernel, LOOP_ALL_GFS_GPS update over all points, BCs, rescale. */
 int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                                      const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
-/* The RHS kernel(s) of one substep of MoL_step_forward_in_time alone, with
- * the substep's fused RK update and no boundary conditions; for timing and
- * profiling a step's dominant kernel.  which: 0 every RHS kernel of the
- * substep, 1 BSSN Ricci_eval only, 2 BSSN rhs_eval only.  The buffers must
- * hold a previous step's values (e.g. after one full step). */
+/* The kernels of one substep of MoL_step_forward_in_time before its
+ * boundary conditions, for timing and profiling a step's dominant kernel.
+ * which: 0 every kernel of the substep (the RHS kernel(s) with the RK
+ * update), 1 BSSN Ricci_eval only, 2 BSSN rhs_eval only, 3 the RHS
+ * kernel(s) without a split step's separate update kernel (the same as 0
+ * when the update is fused), 4 that update kernel alone (an error when the
+ * step fuses its update).  The buffers must hold a previous step's values
+ * (e.g. after one full step). */
 int MoL_substep_rhs(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params, MoL_gridfunctions *gfs,
                     int stage, double dt, int which);
 /* The RK4 step of the reference's Sommerfeld drivers: RHS_string = rhs_eval +

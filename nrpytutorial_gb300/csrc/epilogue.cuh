@@ -45,29 +45,38 @@ inline StageConsts stage_consts(double dt) {
                      pair_const(dt)};
 }
 
-// Float-float RK4 substep update of value i (FP32 stage modes): y2, r2 are
-// the y_n and running-total buffers holding (hi, lo) pairs; returns the
-// stage value (substeps 0..2) or writes y_n[i] as FP64 (substep 3).  Shared
-// by the fused epilogue and the unfused update kernel, so both round alike.
+// Float-float RK4 substep on loaded values (FP32 stage modes): y the y_n
+// pair, r the running-total pair (not read by substep 0; updated in place by
+// substeps 0..2); returns the stage value (substeps 0..2) or the new y_n
+// pair (substep 3).  Every FP32-stage update goes through this function, so
+// all of them round alike.
+__device__ __forceinline__ float2 ff_rk4_pairs(int stage, float k, const StageConsts &kc, float2 y, float2 &r) {
+  switch (stage) {
+    case 0:
+      r = ff_mul(k, kc.c6);
+      return ff_add(y, ff_mul(k, kc.c2));
+    case 1:
+      r = ff_add(r, ff_mul(k, kc.c3));
+      return ff_add(y, ff_mul(k, kc.c2));
+    case 2:
+      r = ff_add(r, ff_mul(k, kc.c3));
+      return ff_add(y, ff_mul(k, kc.c1));
+    default:
+      return ff_add(ff_add(y, r), ff_mul(k, kc.c6));
+  }
+}
+
+// The same update of value i in memory: y_n and rt hold (hi, lo) pairs;
+// returns the stage value (substeps 0..2) or writes y_n[i] as FP64
+// (substep 3).  Used by the fused epilogue and the unfused update kernel.
 __device__ __forceinline__ float2 ff_rk4_update(int stage, float k, const StageConsts &kc, double *y_n, double *rt,
                                                 long long i) {
   float2 *y2 = (float2 *)y_n, *r2 = (float2 *)rt;
-  switch (stage) {
-    case 0:
-      r2[i] = ff_mul(k, kc.c6);
-      return ff_add(y2[i], ff_mul(k, kc.c2));
-    case 1:
-      r2[i] = ff_add(r2[i], ff_mul(k, kc.c3));
-      return ff_add(y2[i], ff_mul(k, kc.c2));
-    case 2:
-      r2[i] = ff_add(r2[i], ff_mul(k, kc.c3));
-      return ff_add(y2[i], ff_mul(k, kc.c1));
-    default: {
-      const float2 s = ff_add(ff_add(y2[i], r2[i]), ff_mul(k, kc.c6));
-      y_n[i] = f2d_bits(s.x) + f2d_bits(s.y);
-      return s;
-    }
-  }
+  float2 r = (stage > 0) ? r2[i] : make_float2(0.f, 0.f);
+  const float2 s = ff_rk4_pairs(stage, k, kc, y2[i], r);
+  if (stage < 3) r2[i] = r;
+  else y_n[i] = f2d_bits(s.x) + f2d_bits(s.y);
+  return s;
 }
 
 // RK4 substep update of one value; stage < 0 stores k itself into `out`.

@@ -105,6 +105,68 @@ __global__ void rk4_update_kernel(int stage, double dt, StageConsts kc, long lon
   }
 }
 
+// RK update of a split step (FP32 stages, float-float update) at the
+// interior points, where the RHS kernel stored k (as (k, 0) pairs, or FP32
+// values): ff_rk4_pairs, exactly as the fused epilogue applies it, with the
+// stage value written over k (substeps 0..2) or y_n written as FP64
+// (substep 3).  Ghost points are left to the boundary conditions, as in the
+// fused step.  One thread per point of a 128-point row along i0; each thread
+// walks the gfs in groups of 8 whose loads are issued together.
+template <typename TStage, int STAGE>
+__global__ void __launch_bounds__(128) rk4_update_interior_kernel(Grid g, int ngf, StageConsts kc, double *y_n,
+                                                                  double *rt, TStage *k) {
+  const int i0 = g.ng + blockIdx.x * 128 + threadIdx.x;
+  if (i0 >= g.n0 - g.ng) return;
+  const long long idx =
+      (long long)i0 + (long long)g.n0 * ((long long)(g.ng + blockIdx.y) + (long long)g.n1 * (g.ng + blockIdx.z));
+  float2 *y2 = (float2 *)y_n, *r2 = (float2 *)rt;
+  constexpr int GRP = 8;
+  for (int g0 = 0; g0 < ngf; g0 += GRP) {
+    float kv[GRP];
+    float2 yv[GRP], rv[GRP];
+#pragma unroll
+    for (int j = 0; j < GRP; j++) {
+      if (g0 + j < ngf) {
+        const long long i = (long long)(g0 + j) * g.ntot + idx;
+        if constexpr (std::is_same<TStage, float2>::value) kv[j] = k[i].x;
+        else kv[j] = k[i];
+        yv[j] = y2[i];
+        rv[j] = (STAGE > 0) ? r2[i] : make_float2(0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < GRP; j++) {
+      if (g0 + j < ngf) {
+        const long long i = (long long)(g0 + j) * g.ntot + idx;
+        const float2 v = ff_rk4_pairs(STAGE, kv[j], kc, yv[j], rv[j]);
+        if (STAGE < 3) {
+          r2[i] = rv[j];
+          if constexpr (std::is_same<TStage, float2>::value) k[i] = v;
+          else k[i] = v.x;
+        } else {
+          y_n[i] = f2d_bits(v.x) + f2d_bits(v.y);
+        }
+      }
+    }
+  }
+}
+
+template <typename TStage>
+static int update_interior_t(const paramstruct *p, int ngf, int stage, StageConsts kc, double *y_n, double *rt,
+                             TStage *k) {
+  const Grid g = make_grid(p);
+  NRGPU_REQUIRE(p->Nxx1 <= 65535 && p->Nxx2 <= 65535, "Nxx1, Nxx2 above the launch's grid limit");
+  const dim3 grid((unsigned)((p->Nxx0 + 127) / 128), (unsigned)p->Nxx1, (unsigned)p->Nxx2);
+  switch (stage) {
+    case 0: rk4_update_interior_kernel<TStage, 0><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
+    case 1: rk4_update_interior_kernel<TStage, 1><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
+    case 2: rk4_update_interior_kernel<TStage, 2><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
+    default: rk4_update_interior_kernel<TStage, 3><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
+  }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
 // SM count of the current device, cached per device ordinal (grid sizes of
 // the reductions and update loops depend on the device they run on).
 static int sm_count() {
@@ -184,6 +246,20 @@ static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) 
   return NRGPU_OK;
 }
 
+// A split step (bssn_split_update): the RHS kernel stores k and the RK
+// update runs as rk4_update_interior_kernel; the arithmetic is the fused
+// epilogue's, so both forms give the same bits.
+static bool split_step(int system, const paramstruct *p, int prec) {
+  return system == NRGPU_SYS_BSSN && bssn_split_update(p, prec);
+}
+static int update_interior(int system, const paramstruct *p, MoL_gridfunctions *gfs, int stage, StageConsts kc,
+                           void *k) {
+  const int ngf = system_num_gfs(system);
+  if (pair_precision(gfs->precision))
+    return update_interior_t<float2>(p, ngf, stage, kc, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, (float2 *)k);
+  return update_interior_t<float>(p, ngf, stage, kc, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, (float *)k);
+}
+
 static int check_step_args(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
                            const MoL_gridfunctions *gfs) {
   int st = check_params(p);
@@ -214,11 +290,13 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
   const bool pair = pair_precision(gfs->precision);
   const bool acc64 = gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK;
+  const bool split = split_step(system, p, gfs->precision);
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
   if (!f64 && (st = prep_state(system, p, gfs))) return st;
+  const StageConsts kc = stage_consts(dt);
   for (int s = 0; s < 4; s++) {
     StageArgs a{};
-    a.stage = s;
+    a.stage = split ? -1 : s;
     a.dt = dt;
     a.prec = gfs->precision;
     // substep 0 reads y_n: itself in FP64, its pairs in place when compensated,
@@ -228,9 +306,11 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
     a.in_is_f64 = f64;
     a.y_n = gfs->y_n_gfs;
     a.rt = gfs->y_nplus1_running_total_gfs;
-    a.out = (s == 3) ? nullptr : kbuf[s % 2];
+    // fused: the stage value (substeps 0..2; substep 3 writes y_n); split: k
+    a.out = (s == 3 && !split) ? nullptr : kbuf[s % 2];
     a.auxevol = gfs->auxevol_gfs;
     if ((st = rhs_stage(system, rfm, p, a))) return st;
+    if (split && (st = update_interior(system, p, gfs, s, kc, kbuf[s % 2]))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
     if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64 && !acc64, acc64))) return st;
@@ -244,13 +324,16 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   if (st) return st;
   NRGPU_REQUIRE(system_num_gfs(system) > 0 && gfs, "bad arguments");
   NRGPU_REQUIRE(stage >= 0 && stage <= 3, "stage %d not in 0..3", stage);
-  NRGPU_REQUIRE(which >= 0 && which <= 2, "which %d not in 0..2", which);
-  NRGPU_REQUIRE(which == 0 || system == NRGPU_SYS_BSSN, "which = 1, 2 select BSSN's two kernels");
+  NRGPU_REQUIRE(which >= 0 && which <= 4, "which %d not in 0..4", which);
+  NRGPU_REQUIRE(which == 0 || which == 3 || system == NRGPU_SYS_BSSN, "which = 1, 2 select BSSN's two kernels");
   const bool f64 = gfs->precision == NRGPU_PREC_FP64;
   const bool pair = pair_precision(gfs->precision);
+  const bool split = split_step(system, p, gfs->precision);
+  NRGPU_REQUIRE(which != 4 || split, "which = 4: this step updates in the RHS kernel's epilogue");
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
+  if (which == 4) return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2]);
   StageArgs a{};
-  a.stage = stage;
+  a.stage = split ? -1 : stage;
   a.dt = dt;
   a.prec = gfs->precision;
   a.in = (stage == 0) ? (pair ? (const void *)gfs->k_even_gfs : (const void *)gfs->y_n_gfs)
@@ -258,11 +341,12 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   a.in_is_f64 = !pair && ((stage == 0) || f64);
   a.y_n = gfs->y_n_gfs;
   a.rt = gfs->y_nplus1_running_total_gfs;
-  a.out = (stage == 3) ? nullptr : kbuf[stage % 2];
+  a.out = (stage == 3 && !split) ? nullptr : kbuf[stage % 2];
   a.auxevol = gfs->auxevol_gfs;
   if (which == 1) return bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
   if (which == 2) return bssn_rhs_launch(rfm, p, a);
-  return rhs_stage(system, rfm, p, a);
+  if ((st = rhs_stage(system, rfm, p, a)) || which == 3 || !split) return st;
+  return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2]);
 }
 
 int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const paramstruct *p,

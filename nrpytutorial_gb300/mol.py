@@ -137,8 +137,10 @@ class Evolution:
         return replay
 
     def substep_rhs(self, dt, stage=1, which=0):
-        """One substep's RHS kernel(s) with the fused RK update, no BCs
-        (timing and profiling; run a full step first)."""
+        """One substep's kernels before its BCs (timing and profiling; run a
+        full step first).  which: 0 all of them, 1 BSSN Ricci, 2 BSSN RHS,
+        3 the RHS kernel(s) without a split step's update kernel, 4 that
+        update kernel alone."""
         self._sync_stream()
         _lib.check(self.lib.MoL_substep_rhs(self.sys_id, self._rfm(), C.byref(self.grid.params),
                                             C.byref(self.gfs), int(stage), float(dt), int(which)),

@@ -105,6 +105,33 @@ def test_compensated_fused_equals_unfused(cuda, system, coord, Nxx, order, prec)
     assert rel_l2(a, b) < 1e-13
 
 
+@pytest.mark.parametrize("prec", ["compensated", "mixed"])
+@pytest.mark.parametrize("coord", ["SinhSpherical", "SinhSymTP"])
+def test_split_update_step_equals_the_unfused_step_bitwise(cuda, coord, prec):
+    """Curvilinear BSSN with the float-float update: the step's staged (or
+    fused) kernel stores k and a separate kernel updates the interior
+    points, the arithmetic the unfused step applies at every point, so the
+    two states agree bit for bit; FP64 accumulation keeps the fused
+    epilogue and has no separate update kernel."""
+    import torch
+    system, Nxx, order = "BSSN", (12, 10, 8), 4
+    G, gp = grids(system, coord, Nxx, order, **KW)
+    y = _state(system, gp)
+    dt = G.find_timestep(0.5)
+    a = _run(cuda, system, coord, Nxx, order, prec, y, dt, 3, fused=True)
+    b = _run(cuda, system, coord, Nxx, order, prec, y, dt, 3, fused=False)
+    assert np.array_equal(a, b)
+    ev, _ = _evo(cuda, system, coord, Nxx, order, prec)
+    ev.y_n.copy_(torch.tensor(y, device=cuda))
+    ev.step(dt)
+    ev.substep_rhs(dt, 1, 4)  # the update kernel exists for this step
+    e64, _ = _evo(cuda, system, coord, Nxx, order, "compensated_fp64rk")
+    e64.y_n.copy_(torch.tensor(y, device=cuda))
+    e64.step(dt)
+    with pytest.raises(RuntimeError):
+        e64.substep_rhs(dt, 1, 4)
+
+
 @pytest.mark.parametrize("prec", ["compensated", "compensated_fp64rk"])
 def test_compensated_graph_replay_matches_eager(cuda, prec):
     import torch
