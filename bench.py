@@ -55,7 +55,7 @@ UPDATE_BYTES_COMP = 24 * 5 * 8
 # (profiles/bssn_split_step_compensated_roofline_traffic.md), means over the
 # captured launches.
 DOM_TRAFFIC_COMP = 45.13e6  # 42.90 MB read + 2.23 MB written
-UPDATE_TRAFFIC_COMP = None
+UPDATE_TRAFFIC_COMP = 81.75e6  # 79.13 MB read + 2.62 MB written
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 

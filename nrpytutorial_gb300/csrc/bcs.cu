@@ -282,25 +282,29 @@ __global__ void bc_inner_pair_kernel(const int *__restrict__ dest, const int *__
 // One entry of the schedule: an outer point (3 f1 - 3 f2 + f3 along its step,
 // the same arithmetic as bc_outer_kernel / bc_outer_pair_kernel) or an inner
 // point (parity copy).
-template <typename T>
-__device__ __forceinline__ void bc_entry(T *f, long long d, long long a, int bits, bool inner, int type) {
-  if (inner) {
-    const T v = f[a];
-    const bool neg = (bits >> type) & 1;
-    if constexpr (std::is_same<T, float2>::value) f[d] = neg ? make_float2(-v.x, -v.y) : v;
-    else f[d] = neg ? -v : v;
-  } else if constexpr (std::is_same<T, double>::value) {
-    f[d] = __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[d + a]), __dmul_rn(3.0, f[d + 2 * a])), f[d + 3 * a]);
+template <typename T> __device__ __forceinline__ T bc_outer_value(T f1, T f2, T f3) {
+  if constexpr (std::is_same<T, double>::value) {
+    return __dadd_rn(__dsub_rn(__dmul_rn(3.0, f1), __dmul_rn(3.0, f2)), f3);
   } else if constexpr (std::is_same<T, float>::value) {
-    f[d] = __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[d + a]), __fmul_rn(3.0f, f[d + 2 * a])), f[d + 3 * a]);
+    return __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f1), __fmul_rn(3.0f, f2)), f3);
   } else {
-    const float2 x = ff_mul(3.0f, f[d + a]), y = ff_mul(3.0f, f[d + 2 * a]);
-    f[d] = ff_add(ff_add(x, ff_neg(y)), f[d + 3 * a]);
+    const float2 x = ff_mul(3.0f, f1), y = ff_mul(3.0f, f2);
+    return ff_add(ff_add(x, ff_neg(y)), f3);
   }
 }
+template <typename T> __device__ __forceinline__ T bc_parity_value(T v, bool neg) {
+  if constexpr (std::is_same<T, float2>::value) return neg ? make_float2(-v.x, -v.y) : v;
+  else return neg ? -v : v;
+}
+template <typename T>
+__device__ __forceinline__ void bc_entry(T *f, long long d, long long a, int bits, bool inner, int type) {
+  if (inner) f[d] = bc_parity_value(f[a], (bits >> type) & 1);
+  else f[d] = bc_outer_value(f[d + a], f[d + 2 * a], f[d + 3 * a]);
+}
 
-// One level: one thread per entry, looping over the gridfunctions (the
-// entry's indices are read once; its per-gridfunction copies are independent).
+// One level: one thread per entry over a chunk of gridfunctions (the entry's
+// indices are read once).  Within a level no entry reads another's
+// destination, so the chunk's loads are all issued before its stores.
 constexpr int kBcGfChunk = 6;  // gridfunctions per thread (blockIdx.y picks the chunk)
 template <typename T>
 __global__ void bc_level_kernel(const int *__restrict__ dest, const int *__restrict__ arg,
@@ -310,12 +314,30 @@ __global__ void bc_level_kernel(const int *__restrict__ dest, const int *__restr
   if (p >= end) return;
   const long long d = dest[p], a = arg[p];
   const int bits = par[p];
-  const bool inner = p >= inner_start;
-  const int g0 = blockIdx.y * kBcGfChunk, g1 = min(ngfs, g0 + kBcGfChunk);
+  const int g0 = blockIdx.y * kBcGfChunk, n = min(ngfs - g0, kBcGfChunk);
+  T *f0 = gfs + (long long)g0 * ntot;
+  if (p >= inner_start) {
+    T v[kBcGfChunk];
 #pragma unroll
-  for (int k = 0; k < kBcGfChunk; k++) {
-    const int gf = g0 + k;
-    if (gf < g1) bc_entry(gfs + (long long)gf * ntot, d, a, bits, inner, types.t[gf]);
+    for (int k = 0; k < kBcGfChunk; k++)
+      if (k < n) v[k] = f0[(long long)k * ntot + a];
+#pragma unroll
+    for (int k = 0; k < kBcGfChunk; k++)
+      if (k < n) f0[(long long)k * ntot + d] = bc_parity_value(v[k], (bits >> types.t[g0 + k]) & 1);
+  } else {
+    T v1[kBcGfChunk], v2[kBcGfChunk], v3[kBcGfChunk];
+#pragma unroll
+    for (int k = 0; k < kBcGfChunk; k++) {
+      if (k < n) {
+        const T *f = f0 + (long long)k * ntot + d;
+        v1[k] = f[a];
+        v2[k] = f[2 * a];
+        v3[k] = f[3 * a];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kBcGfChunk; k++)
+      if (k < n) f0[(long long)k * ntot + d] = bc_outer_value(v1[k], v2[k], v3[k]);
   }
 }
 

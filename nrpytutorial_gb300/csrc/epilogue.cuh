@@ -154,13 +154,24 @@ __device__ __forceinline__ bool interior_point(const Grid &g, int &i0, int &i1, 
 // split in place into (hi, lo) pairs (the float-float accumulation state of
 // the epilogue, and the compensated substep-0 input); for plain FP32 stages
 // also y_n rounded to FP32 into f (substep 0's input).
+// In place, so each thread loads 4 values before it stores their pairs.
 template <bool ROUND>
 __global__ void split_state_kernel(long long n, double *__restrict__ y, float *__restrict__ f) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const float2 p = split_pair_fast(y[i]);
-    if (ROUND) f[i] = p.x;
-    ((float2 *)y)[i] = p;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (i0 + j * stride < n) v[j] = y[i0 + j * stride];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const long long i = i0 + j * stride;
+      if (i < n) {
+        const float2 p = split_pair_fast(v[j]);
+        if (ROUND) f[i] = p.x;
+        ((float2 *)y)[i] = p;
+      }
+    }
   }
 }
 

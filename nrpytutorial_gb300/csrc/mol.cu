@@ -227,9 +227,16 @@ static long long state_len(int system, const paramstruct *p) {
 // Start of an NRGPU_PREC_COMPENSATED_FP64RK step: the FP64 y_n stays as it is
 // and its (hi, lo) pairs go to `out`, substep 0's stencil input.
 __global__ void pair_copy_kernel(long long n, const double *__restrict__ y, float2 *__restrict__ out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    out[i] = split_pair(y[i]);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (i0 + j * stride < n) v[j] = y[i0 + j * stride];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (i0 + j * stride < n) out[i0 + j * stride] = split_pair(v[j]);
+  }
 }
 
 static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
