@@ -111,16 +111,18 @@ __global__ void rk4_update_kernel(int stage, double dt, StageConsts kc, long lon
 // stage value written over k (substeps 0..2) or y_n written as FP64
 // (substep 3).  Ghost points are left to the boundary conditions, as in the
 // fused step.  One thread per point of a 128-point row along i0; each thread
-// walks the gfs in groups of 8 whose loads are issued together.
+// walks the gfs in groups of 6 whose loads are issued together.  At most 64
+// registers, so 8 blocks fit an SM: the 1024 rows of a 128x64x16 grid run in
+// one wave (at 77 registers, 6 blocks per SM, they took two).
 template <typename TStage, int STAGE>
-__global__ void __launch_bounds__(128) rk4_update_interior_kernel(Grid g, int ngf, StageConsts kc, double *y_n,
+__global__ void __launch_bounds__(128, 8) rk4_update_interior_kernel(Grid g, int ngf, StageConsts kc, double *y_n,
                                                                   double *rt, TStage *k) {
   const int i0 = g.ng + blockIdx.x * 128 + threadIdx.x;
   if (i0 >= g.n0 - g.ng) return;
   const long long idx =
       (long long)i0 + (long long)g.n0 * ((long long)(g.ng + blockIdx.y) + (long long)g.n1 * (g.ng + blockIdx.z));
   float2 *y2 = (float2 *)y_n, *r2 = (float2 *)rt;
-  constexpr int GRP = 8;
+  constexpr int GRP = 6;
   for (int g0 = 0; g0 < ngf; g0 += GRP) {
     float kv[GRP];
     float2 yv[GRP], rv[GRP];
