@@ -241,16 +241,32 @@ __global__ void pair_copy_kernel(long long n, const double *__restrict__ y, floa
   }
 }
 
+// Blocks of a grid-stride loop over n items: as many as the SMs hold at once
+// (one wave; a fixed multiple of the SM count can leave a partial second
+// wave), fewer when n is small.
+template <typename K> static int one_wave_blocks(K kernel, int threads, long long n) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return (int)std::max<long long>(1, std::min<long long>((n + threads - 1) / threads,
+                                                         (long long)sm_count() * per_sm));
+}
+
 static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) {
   const long long n = state_len(system, p);
   const int threads = 256;
-  const int blocks = (int)std::min<long long>((n + threads - 1) / threads, (long long)sm_count() * 8);
-  if (gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK)
+  if (gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK) {
+    const int blocks = one_wave_blocks(pair_copy_kernel, threads, n);
     pair_copy_kernel<<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float2 *)gfs->k_even_gfs);
-  else if (gfs->precision == NRGPU_PREC_COMPENSATED)
+  } else if (gfs->precision == NRGPU_PREC_COMPENSATED) {
+    const int blocks = one_wave_blocks(split_state_kernel<false>, threads, n);
     split_state_kernel<false><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, nullptr);
-  else
+  } else {
+    const int blocks = one_wave_blocks(split_state_kernel<true>, threads, n);
     split_state_kernel<true><<<blocks, threads, 0, stream()>>>(n, gfs->y_n_gfs, (float *)gfs->k_even_gfs);
+  }
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
