@@ -66,8 +66,18 @@ __global__ void __launch_bounds__(TX *TY)
     const long long st[3] = {1, I.n0, (long long)I.n0 * I.n1};
     const R inv[3] = {(R)I.invdx0, (R)I.invdx1, (R)I.invdx2};
     const long long plane = (long long)I.n0 * I.n1;
+    // the epilogue indexes gf g at base + g*ntot + idx of this instance
+    RKEpilogue<TStage> e = epi;
+    e.ntot = I.ntot;
+    e.dt = I.dt;
+    e.kc = I.kc;
+    e.y_n = epi.y_n ? epi.y_n + I.base : nullptr;
+    e.rt = epi.rt ? epi.rt + I.base : nullptr;
+    e.out = epi.out ? epi.out + I.base : nullptr;
     for (int i0 = kBatchNG + threadIdx.x; i0 < I.n0 - kBatchNG; i0 += TX) {
       const long long idx = i0 + I.n0 * ((long long)i1 + (long long)I.n1 * i2);
+      // the update's y_n and running-total loads go out with the stencil loads
+      const typename RKEpilogue<TStage>::Operands o0 = e.fetch(0, idx), o1 = e.fetch(1, idx);
       const auto uu = in + I.base + idx;
       const R vv = val<R>(in + I.base + I.ntot + idx);
       const R *t = tab + I.tab + (long long)i1 * I.n0 + i0;
@@ -77,16 +87,8 @@ __global__ void __launch_bounds__(TX *TY)
         lap += __ldg(t + d * plane) * (fd_d2<4, R>(uu, st[d]) * (inv[d] * inv[d]));
         if (d < 2) lap -= __ldg(t + (3 + d) * plane) * (fd_d1<4, R>(uu, st[d]) * inv[d]);
       }
-      // the epilogue indexes gf g at base + g*ntot + idx of this instance
-      RKEpilogue<TStage> e = epi;
-      e.ntot = I.ntot;
-      e.dt = I.dt;
-      e.kc = I.kc;
-      e.y_n = epi.y_n ? epi.y_n + I.base : nullptr;
-      e.rt = epi.rt ? epi.rt + I.base : nullptr;
-      e.out = epi.out ? epi.out + I.base : nullptr;
-      e(0, idx, vv);
-      e(1, idx, c2 * lap);
+      e.apply(0, idx, vv, o0);
+      e.apply(1, idx, c2 * lap, o1);
     }
   }
 }

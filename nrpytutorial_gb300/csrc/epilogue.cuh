@@ -68,7 +68,7 @@ __device__ __forceinline__ float2 ff_rk4_pairs(int stage, float k, const StageCo
 
 // The same update of value i in memory: y_n and rt hold (hi, lo) pairs;
 // returns the stage value (substeps 0..2) or writes y_n[i] as FP64
-// (substep 3).  Used by the fused epilogue and the unfused update kernel.
+// (substep 3).  Used by the unfused update kernel.
 __device__ __forceinline__ float2 ff_rk4_update(int stage, float k, const StageConsts &kc, double *y_n, double *rt,
                                                 long long i) {
   float2 *y2 = (float2 *)y_n, *r2 = (float2 *)rt;
@@ -105,7 +105,28 @@ template <typename TStage> struct RKEpilogue {
     else out[i] = (TStage)v.x;
   }
 
-  template <typename R> __device__ __forceinline__ void operator()(int gf, long long idx, R value) const {
+  // The y_n and running-total words the update of value (gf, idx) reads
+  // (FP64 values, or (hi, lo) pairs as raw 8-byte words), so that a kernel
+  // can issue these loads early, with its stencil loads; apply() then does
+  // the update on them.
+  struct Operands {
+    double y, r;
+  };
+  __device__ __forceinline__ Operands fetch(int gf, long long idx) const {
+    Operands o{0.0, 0.0};
+    if (stage < 0) return o;
+    const long long i = (long long)gf * ntot + idx;
+    o.y = y_n[i];
+    if (stage > 0) o.r = rt[i];
+    return o;
+  }
+  __device__ __forceinline__ static float2 as_pair(double w) {
+    const long long b = __double_as_longlong(w);
+    return make_float2(__int_as_float((int)(b & 0xffffffffLL)), __int_as_float((int)(b >> 32)));
+  }
+
+  template <typename R>
+  __device__ __forceinline__ void apply(int gf, long long idx, R value, const Operands &o) const {
     const long long i = (long long)gf * ntot + idx;
     if (stage < 0) {
       if constexpr (std::is_same<TStage, float2>::value) out[i] = make_float2((float)value, 0.f);
@@ -114,8 +135,14 @@ template <typename TStage> struct RKEpilogue {
     }
     if constexpr (!std::is_same<TStage, double>::value) {
       if (!f64_update) {
-        const float2 v = ff_rk4_update(stage, (float)value, kc, y_n, rt, i);
-        if (stage < 3) put_pair(i, v);
+        float2 r = as_pair(o.r);
+        const float2 v = ff_rk4_pairs(stage, (float)value, kc, as_pair(o.y), r);
+        if (stage < 3) {
+          ((float2 *)rt)[i] = r;
+          put_pair(i, v);
+        } else {
+          y_n[i] = f2d_bits(v.x) + f2d_bits(v.y);
+        }
         return;
       }
     }
@@ -123,20 +150,24 @@ template <typename TStage> struct RKEpilogue {
     switch (stage) {
       case 0:
         rt[i] = dmul(kdt, 1.0 / 6.0);
-        put(i, dadd(y_n[i], dmul(kdt, 1.0 / 2.0)));
+        put(i, dadd(o.y, dmul(kdt, 1.0 / 2.0)));
         break;
       case 1:
-        rt[i] = dadd(rt[i], dmul(kdt, 1.0 / 3.0));
-        put(i, dadd(y_n[i], dmul(kdt, 1.0 / 2.0)));
+        rt[i] = dadd(o.r, dmul(kdt, 1.0 / 3.0));
+        put(i, dadd(o.y, dmul(kdt, 1.0 / 2.0)));
         break;
       case 2:
-        rt[i] = dadd(rt[i], dmul(kdt, 1.0 / 3.0));
-        put(i, dadd(y_n[i], kdt));
+        rt[i] = dadd(o.r, dmul(kdt, 1.0 / 3.0));
+        put(i, dadd(o.y, kdt));
         break;
       default:
-        y_n[i] = dadd(dadd(y_n[i], rt[i]), dmul(kdt, 1.0 / 6.0));
+        y_n[i] = dadd(dadd(o.y, o.r), dmul(kdt, 1.0 / 6.0));
         break;
     }
+  }
+
+  template <typename R> __device__ __forceinline__ void operator()(int gf, long long idx, R value) const {
+    apply(gf, idx, value, fetch(gf, idx));
   }
 };
 
