@@ -401,7 +401,11 @@ def run_gpu(args):
                      "launch_ms": t_step_c * 1e3,
                      "note": "the step's dominant kernel (TMA-staged shared-memory finite differences, 8 warps "
                              "per SM) is issue/latency bound by the BSSN algebra, not by HBM; HBM fraction "
-                             "reported as asked. The RK update runs in the separate kernel of roofline_update"},
+                             "reported as asked. The RK update runs in the separate kernel of roofline_update",
+                     "issue": {"issue_slots_busy": 0.320, "fma_pipe_busy": 0.182, "warps_active_per_sm": 7.7,
+                               "dram_throughput_of_peak": 0.041,
+                               "source": "ncu --set full of the same kernel (substep 0), "
+                                         "profiles/bssn_split_step_kernels_compensated_sinhsph_128x64x16.md"}},
         "roofline_update": {"bound": "hbm", "kernel": "rk4_update_interior_kernel<float2, 1> (float-float RK4 "
                                                       "update of substep 1 at the interior points)",
                             "achieved": achieved_upd, "peak": hbm, "unit": "GB/s", "frac": achieved_upd / hbm,
