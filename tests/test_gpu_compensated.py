@@ -132,6 +132,33 @@ def test_split_update_step_equals_the_unfused_step_bitwise(cuda, coord, prec):
         e64.substep_rhs(dt, 1, 4)
 
 
+@pytest.mark.parametrize("prec", ["compensated", "mixed"])
+def test_substep_rhs_kernel_then_update_kernel_equals_the_substep(cuda, prec):
+    """MoL_substep_rhs on a split step: the RHS kernel alone (which = 3) and
+    then the update kernel alone (which = 4) leave every buffer as the whole
+    substep (which = 0) does."""
+    import torch
+    system, coord, Nxx, order = "BSSN", "SinhSpherical", (12, 10, 8), 4
+    G, gp = grids(system, coord, Nxx, order, **KW)
+    y = _state(system, gp)
+    dt = G.find_timestep(0.5)
+
+    def run(whiches):
+        ev, _ = _evo(cuda, system, coord, Nxx, order, prec)
+        ev.y_n.copy_(torch.tensor(y, device=cuda))
+        ev.apply_bcs(ev.y_n)
+        ev.enforce_detgammabar(ev.y_n)
+        ev.step(dt)
+        for w in whiches:
+            ev.substep_rhs(dt, 1, w)
+        torch.cuda.synchronize()
+        return [t.cpu().numpy().copy() for t in (ev.y_n, ev.rt, ev.k_odd, ev.k_even)]
+
+    whole, parts = run([0]), run([3, 4])
+    for a, b in zip(whole, parts):
+        assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("prec", ["compensated", "compensated_fp64rk"])
 def test_compensated_graph_replay_matches_eager(cuda, prec):
     import torch
