@@ -136,7 +136,9 @@ def test_split_update_step_equals_the_unfused_step_bitwise(cuda, coord, prec):
 def test_substep_rhs_kernel_then_update_kernel_equals_the_substep(cuda, prec):
     """MoL_substep_rhs on a split step: the RHS kernel alone (which = 3) and
     then the update kernel alone (which = 4) leave every buffer as the whole
-    substep (which = 0) does."""
+    substep (which = 0) does, byte for byte.  (A lone substep after a full
+    step reads the FP64 y_n words as pairs, so some of its values are not
+    finite; both forms produce the same words.)"""
     import torch
     system, coord, Nxx, order = "BSSN", "SinhSpherical", (12, 10, 8), 4
     G, gp = grids(system, coord, Nxx, order, **KW)
@@ -156,7 +158,7 @@ def test_substep_rhs_kernel_then_update_kernel_equals_the_substep(cuda, prec):
 
     whole, parts = run([0]), run([3, 4])
     for a, b in zip(whole, parts):
-        assert np.array_equal(a, b)
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
 @pytest.mark.parametrize("prec", ["compensated", "compensated_fp64rk"])
