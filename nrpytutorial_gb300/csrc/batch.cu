@@ -53,8 +53,12 @@ struct BatchWork {
 };
 
 // vv_rhs = c^2 (ghat^ii d_i d_i uu - ghat^ij Gammahat^k_ij d_k uu), per point.
+// At most 64 registers (1024 threads' worth of blocks per SM): the kernel is
+// bound by load latency, and 32 warps per SM instead of the ~16 that 96
+// registers allow took the 512-instance step from 2.00 to 1.60 ms (plain
+// FP32 stages) and 2.18 to 1.91 ms (pairs), despite a few spilled bytes.
 template <typename R, typename Tin, typename TStage, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY)
+__global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY))
     sw_batch_rhs_kernel(const BatchInstance *__restrict__ insts, const BatchWork *__restrict__ work, int nwork,
                         typename InRef<Tin>::type in, const R *__restrict__ tab, R c2, RKEpilogue<TStage> epi) {
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -150,14 +154,17 @@ __global__ void sw_batch_gaussian_kernel(const BatchInstance *__restrict__ insts
 // phases (per layer: outer faces along i0, i1, i2, then inner points) in
 // order.  Offsets a (dest) and b (outer: signed step; inner: src) are
 // relative to the instance's first point; both gridfunctions per thread.
-template <typename T> __device__ __forceinline__ T bc_extrapolate(const T *f, long long s) {
+template <typename T> __device__ __forceinline__ T bc_extrapolate3(T f1, T f2, T f3) {
   if constexpr (std::is_same<T, double>::value)
-    return __dadd_rn(__dsub_rn(__dmul_rn(3.0, f[s]), __dmul_rn(3.0, f[2 * s])), f[3 * s]);
+    return __dadd_rn(__dsub_rn(__dmul_rn(3.0, f1), __dmul_rn(3.0, f2)), f3);
   else if constexpr (std::is_same<T, float>::value)
-    return __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f[s]), __fmul_rn(3.0f, f[2 * s])), f[3 * s]);
+    return __fadd_rn(__fsub_rn(__fmul_rn(3.0f, f1), __fmul_rn(3.0f, f2)), f3);
   else  // FP32 pairs: the rule on the FP64 values, re-split
-    return split_pair(__dadd_rn(__dsub_rn(__dmul_rn(3.0, pair_value(f[s])), __dmul_rn(3.0, pair_value(f[2 * s]))),
-                                pair_value(f[3 * s])));
+    return split_pair(__dadd_rn(__dsub_rn(__dmul_rn(3.0, pair_value(f1)), __dmul_rn(3.0, pair_value(f2))),
+                                pair_value(f3)));
+}
+template <typename T> __device__ __forceinline__ T bc_extrapolate(const T *f, long long s) {
+  return bc_extrapolate3(f[s], f[2 * s], f[3 * s]);
 }
 
 template <typename T>
@@ -193,12 +200,20 @@ __global__ void sw_batch_bc_kernel(const BatchInstance *__restrict__ insts, cons
 constexpr int kBcMaxLevels = 8;
 constexpr int kBcOffStride = 2 * (kBcMaxLevels + 2);
 
+// Both gridfunctions' source values are loaded before either store (within
+// a level no entry reads another entry's destination).
 template <typename T>
 __device__ __forceinline__ void bc_apply_entry(T *f, long long ntot, long long d, long long e, bool inner) {
-#pragma unroll
-  for (int g = 0; g < 2; g++) {
-    T *fg = f + g * ntot;
-    fg[d] = inner ? fg[e] : bc_extrapolate(fg + d, e);  // scalars: parity +1
+  T *f1 = f + ntot;
+  if (inner) {  // scalars: parity +1
+    const T a = f[e], b = f1[e];
+    f[d] = a;
+    f1[d] = b;
+  } else {
+    const T a1 = f[d + e], a2 = f[d + 2 * e], a3 = f[d + 3 * e];
+    const T b1 = f1[d + e], b2 = f1[d + 2 * e], b3 = f1[d + 3 * e];
+    f[d] = bc_extrapolate3(a1, a2, a3);
+    f1[d] = bc_extrapolate3(b1, b2, b3);
   }
 }
 
