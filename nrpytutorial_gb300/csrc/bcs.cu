@@ -296,6 +296,11 @@ template <typename T> __device__ __forceinline__ T bc_parity_value(T v, bool neg
   if constexpr (std::is_same<T, float2>::value) return neg ? make_float2(-v.x, -v.y) : v;
   else return neg ? -v : v;
 }
+template <typename T>
+__device__ __forceinline__ void bc_entry(T *f, long long d, long long a, int bits, bool inner, int type) {
+  if (inner) f[d] = bc_parity_value(f[a], (bits >> type) & 1);
+  else f[d] = bc_outer_value(f[d + a], f[d + 2 * a], f[d + 3 * a]);
+}
 
 // One level: one thread per entry over a chunk of gridfunctions (the entry's
 // indices are read once).  Within a level no entry reads another's
@@ -337,8 +342,7 @@ __global__ void bc_level_kernel(const int *__restrict__ dest, const int *__restr
 }
 
 // The small trailing levels: one block per gridfunction, a block barrier
-// between levels; within a level a thread loads two entries' sources before
-// storing either.
+// between levels.
 struct LevelTable {
   int start[NRGPU_MAX_BC_LEVELS + 1], inner[NRGPU_MAX_BC_LEVELS];
 };
@@ -346,29 +350,11 @@ template <typename T>
 __global__ void bc_tail_kernel(const int *__restrict__ dest, const int *__restrict__ arg,
                                const int *__restrict__ par, LevelTable lt, int l0, int nlev, long long ntot,
                                ParityTypes types, T *gfs) {
-  constexpr int K = 2;  // entries per thread whose loads are issued before their stores
   const int gf = blockIdx.x;
   T *f = gfs + (long long)gf * ntot;
-  const int type = types.t[gf];
   for (int l = l0; l < nlev; l++) {
-    const int e = lt.start[l + 1], si = lt.inner[l];
-    for (int p0 = lt.start[l] + threadIdx.x; p0 < e; p0 += K * blockDim.x) {
-      T v[K];
-      long long dd[K];
-#pragma unroll
-      for (int j = 0; j < K; j++) {
-        const int p = p0 + j * blockDim.x;
-        if (p < e) {
-          const long long d = dest[p], a = arg[p];
-          dd[j] = d;
-          v[j] = (p >= si) ? bc_parity_value(f[a], (par[p] >> type) & 1)
-                           : bc_outer_value(f[d + a], f[d + 2 * a], f[d + 3 * a]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < K; j++)
-        if (p0 + j * (int)blockDim.x < e) f[dd[j]] = v[j];
-    }
+    for (int p = lt.start[l] + threadIdx.x; p < lt.start[l + 1]; p += blockDim.x)
+      bc_entry(f, dest[p], arg[p], par[p], p >= lt.inner[l], types.t[gf]);
     __syncthreads();
   }
 }

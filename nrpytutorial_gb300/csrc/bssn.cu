@@ -509,7 +509,7 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 // with a separate all-points update) and lose with pairs (compensated:
 // 8.62 vs 8.79 ms).  With the update in FP64 arithmetic
 // (COMPENSATED_FP64RK) the FP64 pipe bounds a separate update kernel and
-// the fused epilogue measures faster (1.20 vs 1.30 ms).  Kreiss-Oliger and
+// the fused epilogue measures faster (1.12 vs 1.29 ms).  Kreiss-Oliger and
 // source-term runs keep the fused epilogue (not measured split).
 bool bssn_split_update(const paramstruct *p, int prec) {
   if (extras_on(p)) return false;
