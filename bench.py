@@ -56,6 +56,12 @@ UPDATE_BYTES_COMP = 24 * 5 * 8
 # captured launches.
 DOM_TRAFFIC_COMP = 45.13e6  # 42.90 MB read + 2.23 MB written
 UPDATE_TRAFFIC_COMP = 81.75e6  # 79.13 MB read + 2.62 MB written
+# Arithmetic of one BSSN Ricci + RHS evaluation at a SinhSpherical FD4 point,
+# counted from the reference-generated C (+ - * / outside load lines,
+# approximate): ~5.5k in rhs_eval and ~3.6k in Ricci_eval.  The FP32
+# non-tensor nominal rate: 152 SMs x 128 lanes x 2 flops x 2.07 GHz.
+BSSN_FLOPS_PER_POINT = 9100
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 RHS_BYTES_F64_FUSED = 24 * 8 + 6 * 8 + 24 * 8 + 24 * 16 + 24 * 8
 RHS_BYTES_F64 = (24 + 6 + 24) * 8
 
@@ -405,7 +411,12 @@ def run_gpu(args):
                      "issue": {"issue_slots_busy": 0.320, "fma_pipe_busy": 0.182, "warps_active_per_sm": 7.7,
                                "dram_throughput_of_peak": 0.041,
                                "source": "ncu --set full of the same kernel (substep 0), "
-                                         "profiles/bssn_split_step_kernels_compensated_sinhsph_128x64x16.md"}},
+                                         "profiles/bssn_split_step_kernels_compensated_sinhsph_128x64x16.md",
+                               "fp32_flops_per_point": BSSN_FLOPS_PER_POINT,
+                               "achieved_fp32_tflops": nint * BSSN_FLOPS_PER_POINT / t_step_c / 1e12,
+                               "fp32_nominal_tflops": FP32_NOMINAL_TFLOPS,
+                               "frac_of_fp32_nominal": nint * BSSN_FLOPS_PER_POINT / t_step_c / 1e12
+                                                       / FP32_NOMINAL_TFLOPS}},
         "roofline_update": {"bound": "hbm", "kernel": "rk4_update_interior_kernel<float2, 1> (float-float RK4 "
                                                       "update of substep 1 at the interior points)",
                             "achieved": achieved_upd, "peak": hbm, "unit": "GB/s", "frac": achieved_upd / hbm,
