@@ -471,7 +471,13 @@ int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const
                                         const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt);
 /* Host-buffer form for callers whose state lives in host memory: copies
  * y_n_gfs (host, FP64, pinned or pageable) to gfs->y_n_gfs, runs n_steps
- * steps, copies the state back, and synchronises the stream. */
+ * steps, copies the state back, and synchronises the stream.  A call that
+ * repeats the previous one exactly (same structures' contents, buffers, dt,
+ * n_steps <= 16, host array) with a pinned host array replays a CUDA graph
+ * of the copies and steps, captured on its second repetition (one graph is
+ * kept per process; results are the same bits as the eager call).  Like
+ * nrgpu_l2_norm_sq_static, the cached graph belongs to the device's current
+ * context: do not call this again after cudaDeviceReset. */
 int MoL_evolve_host(int system, const rfm_struct *rfm, const NRGPU_PARAMSTRUCT *params,
                     const bc_struct *bcstruct, MoL_gridfunctions *gfs, double dt,
                     int n_steps, double *y_n_gfs_host);

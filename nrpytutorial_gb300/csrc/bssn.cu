@@ -511,6 +511,8 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 // (COMPENSATED_FP64RK) the FP64 pipe bounds a separate update kernel and
 // the fused epilogue measures faster (1.12 vs 1.29 ms).  Kreiss-Oliger and
 // source-term runs keep the fused epilogue (not measured split).
+int bssn_kernels_mode() { return g_kernels; }
+
 bool bssn_split_update(const paramstruct *p, int prec) {
   if (extras_on(p)) return false;
   if (prec == NRGPU_PREC_MIXED) return true;

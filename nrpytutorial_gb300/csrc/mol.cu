@@ -454,17 +454,114 @@ int MoL_step_forward_in_time_unfused(int system, const rfm_struct *rfm, const pa
   return NRGPU_OK;
 }
 
+// The host-buffer evolution's work on the library stream: copy in, n_steps
+// steps, copy out (no synchronisation).
+static int evolve_host_enqueue(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
+                               MoL_gridfunctions *gfs, double dt, int n_steps, double *y_host) {
+  const size_t bytes = sizeof(double) * (size_t)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 *
+                       p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
+  int st;
+  NRGPU_CUDA_CHECK(cudaMemcpyAsync(gfs->y_n_gfs, y_host, bytes, cudaMemcpyHostToDevice, stream()));
+  for (int n = 0; n < n_steps; n++)
+    if ((st = MoL_step_forward_in_time(system, rfm, p, bc, gfs, dt))) return st;
+  NRGPU_CUDA_CHECK(cudaMemcpyAsync(y_host, gfs->y_n_gfs, bytes, cudaMemcpyDeviceToHost, stream()));
+  return NRGPU_OK;
+}
+
+// A call that repeats the previous one exactly (system, the bytes of the
+// parameter, reference-metric, boundary and gridfunction structures, dt,
+// step count, host array, device, BSSN kernel selection) with a pinned host
+// array replays a CUDA graph of its copies and steps, captured on the
+// second such call: one graph launch instead of ~21 kernel launches per
+// step removes their launch gaps.  Other calls return NRGPU_ERR_UNSUPPORTED
+// and run eagerly.  One graph is cached per process, for the last
+// configuration seen.
+constexpr int kEvolveGraphMaxSteps = 16;
+struct EvolveKey {
+  int system, n_steps, dev, kernels, has_rfm, pad;
+  double dt;
+  const double *y_host;
+  paramstruct p;
+  rfm_struct rfm;
+  bc_struct bc;
+  MoL_gridfunctions gfs;
+};
+static std::mutex g_evolve_mutex;
+static bool g_evolve_have_key = false;
+static EvolveKey g_evolve_key;
+static cudaGraphExec_t g_evolve_exec = nullptr;
+
+static int evolve_host_graph(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
+                             MoL_gridfunctions *gfs, double dt, int n_steps, double *y_host) {
+  if (n_steps < 1 || n_steps > kEvolveGraphMaxSteps) return NRGPU_ERR_UNSUPPORTED;
+  cudaPointerAttributes pa;
+  memset(&pa, 0, sizeof(pa));
+  if (cudaPointerGetAttributes(&pa, y_host) != cudaSuccess || pa.type != cudaMemoryTypeHost) {
+    cudaGetLastError();
+    return NRGPU_ERR_UNSUPPORTED;
+  }
+  EvolveKey k;
+  memset(&k, 0, sizeof(k));
+  k.system = system;
+  k.n_steps = n_steps;
+  if (cudaGetDevice(&k.dev) != cudaSuccess) {
+    cudaGetLastError();
+    return NRGPU_ERR_UNSUPPORTED;
+  }
+  k.kernels = bssn_kernels_mode();
+  k.dt = dt;
+  k.y_host = y_host;
+  k.p = *p;
+  if (rfm) {
+    k.has_rfm = 1;
+    k.rfm = *rfm;
+  }
+  k.bc = *bc;
+  k.gfs = *gfs;
+  std::lock_guard<std::mutex> lock(g_evolve_mutex);
+  if (!g_evolve_have_key || memcmp(&g_evolve_key, &k, sizeof(k)) != 0) {
+    if (g_evolve_exec) cudaGraphExecDestroy(g_evolve_exec);
+    g_evolve_exec = nullptr;
+    g_evolve_key = k;
+    g_evolve_have_key = true;
+    return NRGPU_ERR_UNSUPPORTED;  // first call of this configuration: eager
+  }
+  if (!g_evolve_exec) {
+    cudaStream_t cs = nullptr, saved = stream();
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      return NRGPU_ERR_UNSUPPORTED;
+    }
+    cudaGraph_t graph = nullptr;
+    int st = NRGPU_ERR_CUDA;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      nrgpu_set_stream(cs);
+      st = evolve_host_enqueue(system, rfm, p, bc, gfs, dt, n_steps, y_host);
+      nrgpu_set_stream(saved);
+      if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) st = NRGPU_ERR_CUDA;
+    }
+    if (st == NRGPU_OK && graph && cudaGraphInstantiate(&g_evolve_exec, graph, 0) != cudaSuccess)
+      g_evolve_exec = nullptr;
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    cudaGetLastError();
+    if (!g_evolve_exec) {
+      g_evolve_have_key = false;
+      return NRGPU_ERR_UNSUPPORTED;  // capture failed: this call runs eagerly
+    }
+  }
+  NRGPU_CUDA_CHECK(cudaGraphLaunch(g_evolve_exec, stream()));
+  NRGPU_CUDA_CHECK(cudaStreamSynchronize(stream()));
+  return NRGPU_OK;
+}
+
 int MoL_evolve_host(int system, const rfm_struct *rfm, const paramstruct *p, const bc_struct *bc,
                     MoL_gridfunctions *gfs, double dt, int n_steps, double *y_host) {
   int st = check_step_args(system, rfm, p, bc, gfs);
   if (st) return st;
   NRGPU_REQUIRE(y_host != nullptr && n_steps >= 0, "bad host buffer or step count");
-  const size_t bytes = sizeof(double) * (size_t)system_num_gfs(system) * p->Nxx_plus_2NGHOSTS0 *
-                       p->Nxx_plus_2NGHOSTS1 * p->Nxx_plus_2NGHOSTS2;
-  NRGPU_CUDA_CHECK(cudaMemcpyAsync(gfs->y_n_gfs, y_host, bytes, cudaMemcpyHostToDevice, stream()));
-  for (int n = 0; n < n_steps; n++)
-    if ((st = MoL_step_forward_in_time(system, rfm, p, bc, gfs, dt))) return st;
-  NRGPU_CUDA_CHECK(cudaMemcpyAsync(y_host, gfs->y_n_gfs, bytes, cudaMemcpyDeviceToHost, stream()));
+  if ((st = evolve_host_graph(system, rfm, p, bc, gfs, dt, n_steps, y_host)) != NRGPU_ERR_UNSUPPORTED) return st;
+  if ((st = evolve_host_enqueue(system, rfm, p, bc, gfs, dt, n_steps, y_host))) return st;
   NRGPU_CUDA_CHECK(cudaStreamSynchronize(stream()));
   return NRGPU_OK;
 }

@@ -39,6 +39,8 @@ int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
 // Whether a BSSN step stores the RHS and runs the RK update as a separate
 // interior kernel instead of the RHS kernel's epilogue.
 bool bssn_split_update(const paramstruct *p, int prec);
+// The BSSN kernel selection (nrgpu_set_bssn_kernels).
+int bssn_kernels_mode();
 // is_f64: double array; otherwise float, or float2 pairs when pair is set
 // ff_f64: FP64 data rescaled in float-float arithmetic (the FP32-stage steps' state)
 // f64_pair: pair data rescaled in FP64 arithmetic (COMPENSATED_FP64RK stages)
