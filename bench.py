@@ -398,7 +398,8 @@ def run_gpu(args):
         "state_finite": finite,
         "e2e": {"value": world * K * nint * 4 / te2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(y0.numel() * 8), "d2h_bytes_per_step": int(y0.numel() * 8),
-                "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call"},
+                "path": "MoL_evolve_host (C ABI), compensated precision, pinned host FP64 state, 1 step per call "
+                        "(repeated identical calls replay a CUDA graph of the two copies and the step)"},
         "roofline": {"bound": "hbm", "kernel": "bssn staged_kernel (FUSED variant: Ricci in the block, then the "
                                                "RHSs, k stored) of substep 1, compensated FP32 pairs",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
