@@ -504,19 +504,19 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 // 128x64x16 (compensated) the RK update costs ~60 us of the fused kernel's
 // ~210 us, while storing k (the kernel then takes 142 us) and updating in a
 // separate high-occupancy kernel (29 us) takes the step from 0.97 to
-// 0.82 ms (graph replay; mixed: 0.82 to 0.72 ms).  The point kernels gain
-// with plain FP32 stages (128^3 Cartesian FD4 mixed: 6.10 ms fused, 5.69
-// with a separate all-points update) and lose with pairs (compensated:
-// 8.62 vs 8.79 ms).  With the update in FP64 arithmetic
-// (COMPENSATED_FP64RK) the FP64 pipe bounds a separate update kernel and
-// the fused epilogue measures faster (1.12 vs 1.29 ms).  Kreiss-Oliger and
-// source-term runs keep the fused epilogue (not measured split).
+// 0.82 ms (graph replay; mixed: 0.82 to 0.72 ms).  With the update in FP64
+// arithmetic (COMPENSATED_FP64RK) the separate kernel is FP64-pipe bound
+// (70 us a substep) and the split gains less: 1.12 to 1.10 ms.  The point
+// kernels gain with plain FP32 stages (128^3 Cartesian FD4 mixed: 6.10 ms
+// fused, 5.69 with a separate all-points update) and lose with pairs
+// (compensated: 8.62 vs 8.79 ms).  Kreiss-Oliger and source-term runs keep
+// the fused epilogue (not measured split).
 int bssn_kernels_mode() { return g_kernels; }
 
 bool bssn_split_update(const paramstruct *p, int prec) {
   if (extras_on(p)) return false;
   if (prec == NRGPU_PREC_MIXED) return true;
-  return prec == NRGPU_PREC_COMPENSATED && staged_for(p, prec);
+  return (prec == NRGPU_PREC_COMPENSATED || prec == NRGPU_PREC_COMPENSATED_FP64RK) && staged_for(p, prec);
 }
 
 // One MoL substep's Ricci + RHS: the fused staged kernel when selected,

@@ -153,6 +153,57 @@ __global__ void __launch_bounds__(128, 8) rk4_update_interior_kernel(Grid g, int
   }
 }
 
+// The same for pair stages with the update in FP64 arithmetic on the FP64
+// y_n and running total (NRGPU_PREC_COMPENSATED_FP64RK): the FP64 branch of
+// RKEpilogue::apply on k = the stored FP32 RHS, so it gives the fused
+// epilogue's bits.
+template <int STAGE>
+__global__ void __launch_bounds__(128, 8) rk4_update_interior_f64_kernel(Grid g, int ngf, double dt, double *y_n,
+                                                                      double *rt, float2 *k) {
+  const int i0 = g.ng + blockIdx.x * 128 + threadIdx.x;
+  if (i0 >= g.n0 - g.ng) return;
+  const long long idx =
+      (long long)i0 + (long long)g.n0 * ((long long)(g.ng + blockIdx.y) + (long long)g.n1 * (g.ng + blockIdx.z));
+  constexpr int GRP = 6;
+  for (int g0 = 0; g0 < ngf; g0 += GRP) {
+    float kv[GRP];
+    double yv[GRP], rv[GRP];
+#pragma unroll
+    for (int j = 0; j < GRP; j++) {
+      if (g0 + j < ngf) {
+        const long long i = (long long)(g0 + j) * g.ntot + idx;
+        kv[j] = k[i].x;
+        yv[j] = y_n[i];
+        rv[j] = (STAGE > 0) ? rt[i] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < GRP; j++) {
+      if (g0 + j < ngf) {
+        const long long i = (long long)(g0 + j) * g.ntot + idx;
+        const double kdt = dmul((double)kv[j], dt);
+        switch (STAGE) {
+          case 0:
+            rt[i] = dmul(kdt, 1.0 / 6.0);
+            k[i] = split_pair(dadd(yv[j], dmul(kdt, 1.0 / 2.0)));
+            break;
+          case 1:
+            rt[i] = dadd(rv[j], dmul(kdt, 1.0 / 3.0));
+            k[i] = split_pair(dadd(yv[j], dmul(kdt, 1.0 / 2.0)));
+            break;
+          case 2:
+            rt[i] = dadd(rv[j], dmul(kdt, 1.0 / 3.0));
+            k[i] = split_pair(dadd(yv[j], kdt));
+            break;
+          default:
+            y_n[i] = dadd(dadd(yv[j], rv[j]), dmul(kdt, 1.0 / 6.0));
+            break;
+        }
+      }
+    }
+  }
+}
+
 template <typename TStage>
 static int update_interior_t(const paramstruct *p, int ngf, int stage, StageConsts kc, double *y_n, double *rt,
                              TStage *k) {
@@ -164,6 +215,21 @@ static int update_interior_t(const paramstruct *p, int ngf, int stage, StageCons
     case 1: rk4_update_interior_kernel<TStage, 1><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
     case 2: rk4_update_interior_kernel<TStage, 2><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
     default: rk4_update_interior_kernel<TStage, 3><<<grid, 128, 0, stream()>>>(g, ngf, kc, y_n, rt, k); break;
+  }
+  NRGPU_LAUNCH_CHECK();
+  return NRGPU_OK;
+}
+
+static int update_interior_f64(const paramstruct *p, int ngf, int stage, double dt, double *y_n, double *rt,
+                               float2 *k) {
+  const Grid g = make_grid(p);
+  NRGPU_REQUIRE(p->Nxx1 <= 65535 && p->Nxx2 <= 65535, "Nxx1, Nxx2 above the launch's grid limit");
+  const dim3 grid((unsigned)((p->Nxx0 + 127) / 128), (unsigned)p->Nxx1, (unsigned)p->Nxx2);
+  switch (stage) {
+    case 0: rk4_update_interior_f64_kernel<0><<<grid, 128, 0, stream()>>>(g, ngf, dt, y_n, rt, k); break;
+    case 1: rk4_update_interior_f64_kernel<1><<<grid, 128, 0, stream()>>>(g, ngf, dt, y_n, rt, k); break;
+    case 2: rk4_update_interior_f64_kernel<2><<<grid, 128, 0, stream()>>>(g, ngf, dt, y_n, rt, k); break;
+    default: rk4_update_interior_f64_kernel<3><<<grid, 128, 0, stream()>>>(g, ngf, dt, y_n, rt, k); break;
   }
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
@@ -278,8 +344,10 @@ static bool split_step(int system, const paramstruct *p, int prec) {
   return system == NRGPU_SYS_BSSN && bssn_split_update(p, prec);
 }
 static int update_interior(int system, const paramstruct *p, MoL_gridfunctions *gfs, int stage, StageConsts kc,
-                           void *k) {
+                           void *k, double dt) {
   const int ngf = system_num_gfs(system);
+  if (gfs->precision == NRGPU_PREC_COMPENSATED_FP64RK)
+    return update_interior_f64(p, ngf, stage, dt, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, (float2 *)k);
   if (pair_precision(gfs->precision))
     return update_interior_t<float2>(p, ngf, stage, kc, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, (float2 *)k);
   return update_interior_t<float>(p, ngf, stage, kc, gfs->y_n_gfs, gfs->y_nplus1_running_total_gfs, (float *)k);
@@ -335,7 +403,7 @@ int MoL_step_forward_in_time(int system, const rfm_struct *rfm, const paramstruc
     a.out = (s == 3 && !split) ? nullptr : kbuf[s % 2];
     a.auxevol = gfs->auxevol_gfs;
     if ((st = rhs_stage(system, rfm, p, a))) return st;
-    if (split && (st = update_interior(system, p, gfs, s, kc, kbuf[s % 2]))) return st;
+    if (split && (st = update_interior(system, p, gfs, s, kc, kbuf[s % 2], dt))) return st;
     void *post = (s == 3) ? (void *)gfs->y_n_gfs : kbuf[s % 2];
     const bool post_f64 = (s == 3) || f64;
     if ((st = post_rhs(system, rfm, p, bc, post, post_f64, pair && s < 3, !f64 && !acc64, acc64))) return st;
@@ -356,7 +424,7 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   const bool split = split_step(system, p, gfs->precision);
   NRGPU_REQUIRE(which != 4 || split, "which = 4: this step updates in the RHS kernel's epilogue");
   void *kbuf[2] = {gfs->k_odd_gfs, gfs->k_even_gfs};
-  if (which == 4) return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2]);
+  if (which == 4) return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2], dt);
   StageArgs a{};
   a.stage = split ? -1 : stage;
   a.dt = dt;
@@ -371,7 +439,7 @@ int MoL_substep_rhs(int system, const rfm_struct *rfm, const paramstruct *p, MoL
   if (which == 1) return bssn_ricci_launch(rfm, p, a.in, a.in_is_f64, a.prec, a.auxevol);
   if (which == 2) return bssn_rhs_launch(rfm, p, a);
   if ((st = rhs_stage(system, rfm, p, a)) || which == 3 || !split) return st;
-  return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2]);
+  return update_interior(system, p, gfs, stage, stage_consts(dt), kbuf[stage % 2], dt);
 }
 
 int MoL_step_forward_in_time_sommerfeld(int system, const rfm_struct *rfm, const paramstruct *p,
