@@ -28,19 +28,24 @@ NRGPU_BSSN_STAGED_DECLARE(NRGPU_COORD_SPHERICAL, 4)
 // Which BSSN Ricci/RHS kernels run (nrgpu_set_bssn_kernels).
 static int g_kernels = NRGPU_BSSN_KERNELS_AUTO;
 // The family a grid and precision run on.  AUTO: the fastest whole step
-// measured on GB300 (128^3 Cartesian FD2/4/6 and 128x64x16-class curvilinear
-// grids, every family): FP64 is FP64-pipe bound and the point kernels keep
-// their occupancy; on Cartesian grids the point kernels' stencil loads hit
-// L1 and the staged bricks' halos cost more than they save (FD6: 13.5 vs
-// 16.9 ms per 128^3 compensated step); on curvilinear grids with FP32 pair
-// stages the fused staged kernel saves the RbarDD round trip and the Ricci
-// launch (headline grid 1.02 vs 1.05 ms), except the SymTP family, whose
-// larger Christoffel tables favour the separate staged kernels; plain FP32
-// stages measure the same in every family (staged).
+// measured on GB300 with the split RK update (graph replay, one call; ms per
+// step, 128^3 Cartesian and 128x64x16 curvilinear grids):
+//   pairs, Cartesian FD2 / 4 / 6 / 8:  point 5.40 / 8.30 / 13.02 / 18.82,
+//     staged 6.17 / 7.80 / 11.85 / 16.80, fused 5.73 / 7.47 / 11.96 / 15.77;
+//   pairs, SinhSpherical / SinhCylindrical / SinhSymTP FD4:  point 0.938 /
+//     0.934 / 1.020, staged 0.831 / 0.851 / 0.849, fused 0.802 / 0.804 / 0.882;
+//   plain FP32, Cartesian FD2 / FD6:  point 4.13 / 8.26, staged 5.03 / 8.41,
+//     fused 5.16 / 7.69 (grids whose FP32 rows are not a multiple of 16 bytes,
+//     e.g. 134 points, run the point kernels whatever the selection).
+// FP64 is FP64-pipe bound and keeps the point kernels.
 static int family(const paramstruct *p, int prec) {
   if (g_kernels != NRGPU_BSSN_KERNELS_AUTO) return g_kernels;
   const int cs = dispatch_cs(p->CoordSystem);
-  if (prec == NRGPU_PREC_FP64 || cs == NRGPU_COORD_CARTESIAN) return NRGPU_BSSN_KERNELS_POINT;
+  if (prec == NRGPU_PREC_FP64) return NRGPU_BSSN_KERNELS_POINT;
+  if (cs == NRGPU_COORD_CARTESIAN) {
+    if (p->FD_order <= 2) return NRGPU_BSSN_KERNELS_POINT;
+    return (pair_precision(prec) || p->FD_order >= 6) ? NRGPU_BSSN_KERNELS_FUSED : NRGPU_BSSN_KERNELS_POINT;
+  }
   if (pair_precision(prec)) return cs == NRGPU_COORD_SINHSYMTP ? NRGPU_BSSN_KERNELS_STAGED : NRGPU_BSSN_KERNELS_FUSED;
   return NRGPU_BSSN_KERNELS_STAGED;
 }
@@ -509,8 +514,9 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 // (70 us a substep) and the split gains less: 1.12 to 1.10 ms.  The point
 // kernels gain with plain FP32 stages (128^3 Cartesian FD4 mixed: 6.10 ms
 // fused, 5.69 with a separate all-points update) and lose with pairs
-// (compensated: 8.62 vs 8.79 ms).  Kreiss-Oliger and source-term runs keep
-// the fused epilogue (not measured split).
+// (compensated: 8.62 vs 8.79 ms), so there they keep their epilogue.
+// Kreiss-Oliger and source-term runs keep the fused epilogue (not measured
+// split).
 int bssn_kernels_mode() { return g_kernels; }
 
 bool bssn_split_update(const paramstruct *p, int prec) {

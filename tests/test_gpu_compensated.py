@@ -112,10 +112,9 @@ def test_compensated_fused_equals_unfused(cuda, system, coord, Nxx, order, prec)
 def test_split_update_step_equals_the_unfused_step_bitwise(cuda, coord, prec):
     """BSSN with FP32 stages: the step's kernel stores k and a separate
     kernel updates the interior points (staged and fused kernels, in
-    float-float or FP64 arithmetic; the Cartesian point kernels with plain
-    FP32 stages), or the kernel's epilogue updates them (Cartesian pairs);
-    either way the arithmetic is the one the unfused step applies at every
-    point, so the states agree bit for bit."""
+    float-float or FP64 arithmetic; the point kernels with plain FP32
+    stages), the arithmetic the unfused step applies at every point, so the
+    states agree bit for bit."""
     import torch
     system, order = "BSSN", 4
     Nxx = (12, 12, 12) if coord == "Cartesian" else (12, 10, 8)
@@ -128,11 +127,7 @@ def test_split_update_step_equals_the_unfused_step_bitwise(cuda, coord, prec):
     ev, _ = _evo(cuda, system, coord, Nxx, order, prec)
     ev.y_n.copy_(torch.tensor(y, device=cuda))
     ev.step(dt)
-    if coord != "Cartesian" or prec == "mixed":
-        ev.substep_rhs(dt, 1, 4)  # the update kernel exists for this step
-    else:
-        with pytest.raises(RuntimeError):
-            ev.substep_rhs(dt, 1, 4)
+    ev.substep_rhs(dt, 1, 4)  # the update kernel exists for this step
 
 
 @pytest.mark.parametrize("prec", ["compensated", "mixed", "compensated_fp64rk"])
