@@ -487,10 +487,6 @@ int bssn_ricci_launch(const rfm_struct *rfm, const paramstruct *p, const void *i
 static bool extras_on(const paramstruct *p) {
   return p->diss_strength != 0.0 || p->enable_stress_energy_source_terms;
 }
-// T^{mu nu} source terms run on the point kernels only; Kreiss-Oliger
-// dissipation also on the staged kernels when they store the RHS (split step
-// or plain rhs_eval), and otherwise on the point kernels.
-static bool sources_on(const paramstruct *p) { return p->enable_stress_energy_source_terms != 0; }
 #define RHS_CALL(CS, ORD) \
   (extras_on(p) ? rhs_launch_t<CS, ORD, true>(rfm, p, a) : rhs_launch_t<CS, ORD, false>(rfm, p, a))
 #define STAGED_RHS_CALL(CS, ORD) staged_rhs_launch_t<CS, ORD>(rfm, p, a, fused)
@@ -501,7 +497,8 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
-  if (staged_for(p, a.prec) && !sources_on(p)) {
+  // Kreiss-Oliger dissipation and T^{mu nu} sources run on the point kernels.
+  if (staged_for(p, a.prec) && !extras_on(p)) {
     st = staged_rhs(rfm, p, a, false);
     if (st != NRGPU_ERR_UNSUPPORTED) return st;
   }
@@ -518,12 +515,12 @@ int bssn_rhs_launch(const rfm_struct *rfm, const paramstruct *p, const StageArgs
 // kernels gain with plain FP32 stages (128^3 Cartesian FD4 mixed: 6.10 ms
 // fused, 5.69 with a separate all-points update) and lose with pairs
 // (compensated: 8.62 vs 8.79 ms), so there they keep their epilogue.
-// Kreiss-Oliger runs split too (the staged kernels add the dissipation before
-// their store); source-term runs keep the point kernels' fused epilogue.
+// Kreiss-Oliger and source-term runs keep the fused epilogue (not measured
+// split).
 int bssn_kernels_mode() { return g_kernels; }
 
 bool bssn_split_update(const paramstruct *p, int prec) {
-  if (sources_on(p)) return false;
+  if (extras_on(p)) return false;
   if (prec == NRGPU_PREC_MIXED) return true;
   return (prec == NRGPU_PREC_COMPENSATED || prec == NRGPU_PREC_COMPENSATED_FP64RK) && staged_for(p, prec);
 }
@@ -534,7 +531,7 @@ int bssn_stage_launch(const rfm_struct *rfm, const paramstruct *p, const StageAr
   int st = check_bssn(rfm, p);
   if (st) return st;
   NRGPU_REQUIRE(a.in && a.auxevol, "NULL gridfunctions");
-  if (family(p, a.prec) == NRGPU_BSSN_KERNELS_FUSED && !sources_on(p)) {
+  if (family(p, a.prec) == NRGPU_BSSN_KERNELS_FUSED && !extras_on(p)) {
     st = staged_rhs(rfm, p, a, true);
     if (st != NRGPU_ERR_UNSUPPORTED) return st;
   }

@@ -220,28 +220,6 @@ template <int ORDER, typename R, typename E> __device__ __forceinline__ R s_dup(
   }
 }
 
-// Kreiss-Oliger stencil (fd_ko of fd.cuh) on the box: the symmetric
-// (ORDER+3)-point weights, pairs treated like the other stencils.
-template <int ORDER, typename R, typename E> __device__ __forceinline__ R s_ko(const E *p, int s) {
-  using C = FDCoef<ORDER>;
-  if constexpr (std::is_same<E, float2>::value) {
-    const float2 c = p[0];
-    R hi = (R)0, lo = (R)C::ko(0) * (R)c.y;
-#pragma unroll
-    for (int k = 1; k <= C::R + 1; k++) {
-      const float2 a = p[k * s], b = p[-k * s];
-      hi += (R)C::ko(k) * (((R)a.x - (R)c.x) + ((R)b.x - (R)c.x));
-      lo += (R)C::ko(k) * ((R)a.y + (R)b.y);
-    }
-    return hi + lo;
-  } else {
-    R acc = (R)C::ko(0) * (R)p[0];
-#pragma unroll
-    for (int k = 1; k <= C::R + 1; k++) acc += (R)C::ko(k) * ((R)p[k * s] + (R)p[-k * s]);
-    return acc;
-  }
-}
-
 // Phase A for one gridfunction: this thread's slots from the box centred
 // at p (strides 1, sy, sz).  out: this thread's slot `b` (stride NT).
 template <int ORDER, typename R, typename E, int NT>
@@ -300,14 +278,10 @@ __device__ __forceinline__ R ADV(const StagedPoint<RS, V, NT> &P, int g, const R
 
 // Phase B: the algebra on the staged values and the reference metric `rf`,
 // then the variant's stores.
-// diss != 0: phase A stored diss * (Kreiss-Oliger term) of each gridfunction
-// where its RHS goes (a plain store, stage -1); it is added here as the
-// point kernels add it, out + diss * KO.
 template <typename R, int CS, int ORDER, typename TStage, int V, int NT, typename RF>
 __device__ __forceinline__ void staged_phase_b(const StagedPoint<R, V, NT> &P, const RF &rf, const R inv[3],
-                                               const R *__restrict__ aux_in, R eta, R diss,
-                                               const RKEpilogue<TStage> &epi, R *__restrict__ aux_out, const Grid &g,
-                                               long long idx) {
+                                               const R *__restrict__ aux_in, R eta, const RKEpilogue<TStage> &epi,
+                                               R *__restrict__ aux_out, const Grid &g, long long idx) {
   if constexpr (V == stage::RICCI) {
     Metric<CS, R> m;
     metric_point<ORDER, CS, R>(P, rf, inv, m);
@@ -327,14 +301,6 @@ __device__ __forceinline__ void staged_phase_b(const StagedPoint<R, V, NT> &P, c
     }
     R out[NUM_EVOL_GFS];
     rhs_point<ORDER, CS, R>(P, rf, inv, Rbar, eta, out);
-    if (diss != (R)0) {
-#pragma unroll 1
-      for (int gf = 0; gf < NUM_EVOL_GFS; gf++) {
-        const long long i = (long long)gf * g.ntot + idx;
-        if constexpr (std::is_same<TStage, float2>::value) out[gf] += (R)epi.out[i].x;
-        else out[gf] += (R)epi.out[i];
-      }
-    }
 #pragma unroll stage::kEpilogueUnroll
     for (int gf = 0; gf < NUM_EVOL_GFS; gf++) epi(gf, idx, out[gf]);
   }
@@ -350,7 +316,7 @@ template <typename R, typename Tin, int CS, int ORDER, typename TStage, int V>
 __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::is_same<Tin, Pair32>::value, float2,
                                                                            Tin>::type, ORDER, V>::NT, 2)
     staged_kernel(Grid g, const __grid_constant__ CUtensorMap tmap, typename InRef<Tin>::type in,
-                  const R *__restrict__ aux_in, const R *__restrict__ tab, R eta, R diss, RKEpilogue<TStage> epi,
+                  const R *__restrict__ aux_in, const R *__restrict__ tab, R eta, RKEpilogue<TStage> epi,
                   R *__restrict__ aux_out, int *status) {
   using E = typename std::conditional<std::is_same<Tin, Pair32>::value, float2, Tin>::type;
   using T = stage::Tile<R, E, ORDER, V>;
@@ -432,19 +398,6 @@ __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::
     } else {
       stage::stage_one<ORDER, R, E, NT>(box + centre, T::BX, T::BX * T::BY, inv, betaU, pos, stage::has_d1(V, gf),
                                         stage::has_d2(V, gf), stage::has_adv(V, gf), myslots + (long long)sbase * NT);
-      if constexpr (V != stage::RICCI) {
-        if (diss != (R)0 && valid) {
-          // sum_k f_dKOD[k] ReU[k], as the point kernels' ko_point
-          const int kst[3] = {1, T::BX, T::BX * T::BY};
-          R acc = (R)0;
-#pragma unroll
-          for (int k = 0; k < 3; k++) {
-            const R d = stage::s_ko<ORDER, R, E>(box + centre, kst[k]) * inv[k];
-            acc += RfmMask<CS>::trivial ? d : d * rf.ReU(k);
-          }
-          epi.put_raw(gf, idx, diss * acc);
-        }
-      }
     }
     sbase += stage::nslots(V, gf);
     __syncthreads();  // every thread is done with this box
@@ -474,8 +427,8 @@ __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::
 
   // ---- phase B
   if (!valid) return;
-  staged_phase_b<R, CS, ORDER, TStage, V, NT>(StagedPoint<R, V, NT>{slots + t}, rf, inv, aux_in, eta, diss, epi,
-                                              aux_out, g, idx);
+  staged_phase_b<R, CS, ORDER, TStage, V, NT>(StagedPoint<R, V, NT>{slots + t}, rf, inv, aux_in, eta, epi, aux_out,
+                                              g, idx);
 }
 
 // ---------------------------------------------------------------- launchers
@@ -484,11 +437,9 @@ __global__ void __launch_bounds__(stage::Tile<R, typename std::conditional<std::
 // or base are not 16-byte aligned, or an FP32-arithmetic step on FP64 input.
 // The caller then runs the point kernels.
 
-// diss != 0 (Kreiss-Oliger) only with a plain store of the RHS (stage -1).
 template <typename R, typename Tin, int CS, int ORDER, typename TStage, int V>
 int staged_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, const R *aux_in, R *aux_out, R eta,
-                  R diss, const RKEpilogue<TStage> &epi) {
-  if (diss != (R)0 && (V == stage::RICCI || epi.stage >= 0)) return NRGPU_ERR_UNSUPPORTED;
+                  const RKEpilogue<TStage> &epi) {
   using E = typename std::conditional<std::is_same<Tin, Pair32>::value, float2, Tin>::type;
   using T = stage::Tile<R, E, ORDER, V>;
   Grid g = make_grid(p);
@@ -509,8 +460,8 @@ int staged_launch(const rfm_struct *rfm, const paramstruct *p, const void *in, c
   }
   const int nx = g.n0 - 2 * g.ng, ny = g.n1 - 2 * g.ng, nz = g.n2 - 2 * g.ng;
   const dim3 grid((nx + T::TX - 1) / T::TX, (ny + T::TY - 1) / T::TY, (nz + T::TZ - 1) / T::TZ);
-  kern<<<grid, T::NT, smem, stream()>>>(g, map, (typename InRef<Tin>::type)in, aux_in, table_of<R>(rfm), eta, diss,
-                                        epi, aux_out, status);
+  kern<<<grid, T::NT, smem, stream()>>>(g, map, (typename InRef<Tin>::type)in, aux_in, table_of<R>(rfm), eta, epi,
+                                        aux_out, status);
   NRGPU_LAUNCH_CHECK();
   return NRGPU_OK;
 }
@@ -520,13 +471,13 @@ int staged_ricci_launch_t(const rfm_struct *rfm, const paramstruct *p, const voi
                           void *aux) {
   if (prec == NRGPU_PREC_FP64)
     return staged_launch<double, double, CS, ORDER, double, stage::RICCI>(rfm, p, in, nullptr, (double *)aux, 0.0,
-                                                                        0.0, RKEpilogue<double>{});
+                                                                        RKEpilogue<double>{});
   if (in_is_f64) return NRGPU_ERR_UNSUPPORTED;
   if (pair_precision(prec))
     return staged_launch<float, Pair32, CS, ORDER, float2, stage::RICCI>(rfm, p, in, nullptr, (float *)aux, 0.f,
-                                                                        0.f, RKEpilogue<float2>{});
+                                                                        RKEpilogue<float2>{});
   return staged_launch<float, float, CS, ORDER, float, stage::RICCI>(rfm, p, in, nullptr, (float *)aux, 0.f,
-                                                                    0.f, RKEpilogue<float>{});
+                                                                    RKEpilogue<float>{});
 }
 
 // fused: Ricci computed in the block (auxevol neither read nor written).
@@ -535,27 +486,26 @@ int staged_rhs_launch_t(const rfm_struct *rfm, const paramstruct *p, const Stage
   Grid g = make_grid(p);
   if (a.prec == NRGPU_PREC_FP64) {
     RKEpilogue<double> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (double *)a.out};
-    const double diss = p->diss_strength;
     return fused ? staged_launch<double, double, CS, ORDER, double, stage::FUSED>(rfm, p, a.in, nullptr, nullptr,
-                                                                                  p->eta, diss, epi)
+                                                                                  p->eta, epi)
                  : staged_launch<double, double, CS, ORDER, double, stage::RHS>(
-                       rfm, p, a.in, (const double *)a.auxevol, nullptr, p->eta, diss, epi);
+                       rfm, p, a.in, (const double *)a.auxevol, nullptr, p->eta, epi);
   }
   if (a.in_is_f64) return NRGPU_ERR_UNSUPPORTED;
-  const float eta32 = (float)p->eta, diss32 = (float)p->diss_strength;
+  const float eta32 = (float)p->eta;
   if (pair_precision(a.prec)) {
     RKEpilogue<float2> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float2 *)a.out, stage_consts(a.dt),
                            a.prec == NRGPU_PREC_COMPENSATED_FP64RK};
     return fused ? staged_launch<float, Pair32, CS, ORDER, float2, stage::FUSED>(rfm, p, a.in, nullptr, nullptr,
-                                                                                 eta32, diss32, epi)
+                                                                                 eta32, epi)
                  : staged_launch<float, Pair32, CS, ORDER, float2, stage::RHS>(
-                       rfm, p, a.in, (const float *)a.auxevol, nullptr, eta32, diss32, epi);
+                       rfm, p, a.in, (const float *)a.auxevol, nullptr, eta32, epi);
   }
   RKEpilogue<float> epi{a.stage, a.dt, g.ntot, a.y_n, a.rt, (float *)a.out, stage_consts(a.dt)};
   return fused ? staged_launch<float, float, CS, ORDER, float, stage::FUSED>(rfm, p, a.in, nullptr, nullptr, eta32,
-                                                                             diss32, epi)
+                                                                             epi)
                : staged_launch<float, float, CS, ORDER, float, stage::RHS>(rfm, p, a.in, (const float *)a.auxevol,
-                                                                           nullptr, eta32, diss32, epi);
+                                                                           nullptr, eta32, epi);
 }
 
 #define NRGPU_BSSN_STAGED_DECLARE(CS, ORDER)                                                                  \

@@ -98,13 +98,6 @@ template <typename TStage> struct RKEpilogue {
     if constexpr (std::is_same<TStage, float2>::value) out[i] = split_pair(v);
     else out[i] = (TStage)v;
   }
-  // A value stored where the RHS of (gf, idx) goes, as the plain store
-  // (stage -1) stores it.
-  template <typename R> __device__ __forceinline__ void put_raw(int gf, long long idx, R value) const {
-    const long long i = (long long)gf * ntot + idx;
-    if constexpr (std::is_same<TStage, float2>::value) out[i] = make_float2((float)value, 0.f);
-    else out[i] = (TStage)value;
-  }
   // Stage value (a normalised pair) into an FP32 stage buffer: the pair, or
   // its leading part (the FP32 rounding of the sum) for plain FP32 stages.
   __device__ __forceinline__ void put_pair(long long i, float2 v) const {
