@@ -30,12 +30,12 @@ static int g_kernels = NRGPU_BSSN_KERNELS_AUTO;
 // The family a grid and precision run on.  AUTO: the fastest whole step
 // measured on GB300 with the split RK update (graph replay, one call; ms per
 // step, 128^3 Cartesian and 128x64x16 curvilinear grids):
-//   pairs, Cartesian FD2 / 4 / 6 / 8:  point 5.40 / 8.30 / 13.02 / 18.82,
-//     staged 6.17 / 7.80 / 11.85 / 16.80, fused 5.73 / 7.47 / 11.96 / 15.77;
+//   pairs, Cartesian FD2 / 4 / 6 / 8:  point 5.40 / 8.30 / 13.36 / 19.28,
+//     staged 6.17 / 7.80 / 9.94 / 15.50, fused 5.73 / 7.47 / 10.78 / 15.77;
 //   pairs, SinhSpherical / SinhCylindrical / SinhSymTP FD4:  point 0.938 /
 //     0.934 / 1.020, staged 0.831 / 0.851 / 0.849, fused 0.802 / 0.804 / 0.882;
-//   plain FP32, Cartesian FD2 / FD6:  point 4.13 / 8.26, staged 5.03 / 8.41,
-//     fused 5.16 / 7.69 (grids whose FP32 rows are not a multiple of 16 bytes,
+//   plain FP32, Cartesian FD2 / FD6:  point 4.13 / 8.35, staged 5.03 / 8.42,
+//     fused 5.02 / 7.69 (grids whose FP32 rows are not a multiple of 16 bytes,
 //     e.g. 134 points, run the point kernels whatever the selection).
 // FP64 is FP64-pipe bound and keeps the point kernels.
 static int family(const paramstruct *p, int prec) {
@@ -44,7 +44,8 @@ static int family(const paramstruct *p, int prec) {
   if (prec == NRGPU_PREC_FP64) return NRGPU_BSSN_KERNELS_POINT;
   if (cs == NRGPU_COORD_CARTESIAN) {
     if (p->FD_order <= 2) return NRGPU_BSSN_KERNELS_POINT;
-    return (pair_precision(prec) || p->FD_order >= 6) ? NRGPU_BSSN_KERNELS_FUSED : NRGPU_BSSN_KERNELS_POINT;
+    if (pair_precision(prec)) return p->FD_order >= 6 ? NRGPU_BSSN_KERNELS_STAGED : NRGPU_BSSN_KERNELS_FUSED;
+    return p->FD_order >= 6 ? NRGPU_BSSN_KERNELS_FUSED : NRGPU_BSSN_KERNELS_POINT;
   }
   if (pair_precision(prec)) return cs == NRGPU_COORD_SINHSYMTP ? NRGPU_BSSN_KERNELS_STAGED : NRGPU_BSSN_KERNELS_FUSED;
   return NRGPU_BSSN_KERNELS_STAGED;

@@ -95,9 +95,19 @@ template <typename R, typename E, int ORDER, int V> struct Tile {
   static constexpr int BX = (TX + 2 * H + QX - 1) / QX * QX, BY = TY + 2 * H, BZ = TZ + 2 * H;
   static constexpr int BOX_BYTES = BX * BY * BZ * ES;
   static constexpr int BOX_STRIDE = (BOX_BYTES + 127) / 128 * 128;
-  // boxes in flight per block (the fused variant's larger slot array leaves
-  // room for two at two blocks per SM)
-  static constexpr int NBUF = V == FUSED ? 2 : NRGPU_STAGED_NBUF;
+  // Boxes in flight per block: the most (up to NRGPU_STAGED_NBUF) with which
+  // two blocks still fit an SM's shared memory (228 KB, 1 KB reserved per
+  // block).  FD4: the fused variant's larger slot array leaves room for two
+  // boxes, the others for three; FD6: one box for the fused variant and two
+  // for RHS (deeper rings would leave one block, 4 warps, per SM: 128^3
+  // Cartesian compensated step 11.85 -> 9.94 ms on the RHS variant).  When
+  // not even one box leaves room for two blocks (FD8 fused), two boxes: a
+  // single box would expose every copy's latency at one block per SM
+  // (15.8 -> 20.9 ms).
+  static constexpr int SLOT_BYTES = total_slots(V) * NT * (int)sizeof(R);
+  static constexpr int kTwoBlockSmem = 113 * 1024;
+  static constexpr bool fits(int nb) { return 128 + nb * BOX_STRIDE + SLOT_BYTES <= kTwoBlockSmem; }
+  static constexpr int NBUF = (NRGPU_STAGED_NBUF >= 3 && fits(3)) ? 3 : fits(2) ? 2 : fits(1) ? 1 : 2;
   static constexpr int SLOT_OFFSET = 128 + NBUF * BOX_STRIDE;
   static_assert(TX % QX == 0, "box start must stay 16-byte aligned");
 };
