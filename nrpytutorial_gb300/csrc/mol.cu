@@ -338,8 +338,9 @@ static int prep_state(int system, const paramstruct *p, MoL_gridfunctions *gfs) 
 }
 
 // A split step (bssn_split_update): the RHS kernel stores k and the RK
-// update runs as rk4_update_interior_kernel; the arithmetic is the fused
-// epilogue's, so both forms give the same bits.
+// update runs as rk4_update_interior_kernel (float-float) or
+// rk4_update_interior_f64_kernel (FP64-accumulation form); the arithmetic is
+// the fused epilogue's, so both forms give the same bits.
 static bool split_step(int system, const paramstruct *p, int prec) {
   return system == NRGPU_SYS_BSSN && bssn_split_update(p, prec);
 }
